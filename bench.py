@@ -1,0 +1,324 @@
+"""Benchmark: particle-updates/s of the FluidSim hot path on the 4M-particle FSI case.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = one fluid step of the full hot path (cell sort, fluid-solid coupling,
+virtual walls, fused fluid sweep + update, 4 solid sub-steps) over the
+``fsi_4m`` workload: 4,194,304 fluid + 27,000 solid + 912,600 wall particles
+(dx = 0.005 m, dt = 5e-5 s).  particle-updates/s = (N_fluid + N_solid) * steps
+/ time; wall particles are not counted (their cost is included).
+
+* ``value``: device time of K steps (CUDA-graph replays; state resident in
+  HBM; the 300+ MB particle state is larger than the 129 MB L2), CUDA events
+  on the handle's stream, max over ranks.
+* ``e2e``: the same metric through the C ABI with host buffers: every step
+  copies the fluid and solid state in from pinned host memory
+  (fsim_set_field), advances one step (fsim_step) and reads the state back
+  (fsim_get_field).
+* ``roofline``: the fluid sweep kernel (the dominant kernel) against the
+  measured HBM bandwidth, with the algorithmic 64 B per fluid particle-step.
+* ``cpu_baseline``: the FP64 CPU oracle on this host's cores, 2 steps of the
+  same workload.
+
+``--impl reference`` times the CPU restatement of the reference path (FP32
+oracle, all host threads): the reference itself is a CUDA program with no CPU
+path, and its CUDA sources cannot be built here (they need the unvendored glm
+library).  Multi-GPU: replicas only (independent instances, no collective).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALG_BYTES_FLUID = 64   # per fluid particle-step (pos, vel, rho read+write; cell key write+read)
+ALG_BYTES_SOLID = 132  # per solid particle-sub-step
+ALG_BYTES_SOLID_STEP = 16
+ALG_BYTES_VIRT = 32    # per wall particle-step
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-reduction across replicas (gloo on host tensors)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = _dist()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo", rank=self.rank, world_size=self.ws)
+            self.pg = td
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        return summarize_clocks(self.lines)
+
+
+def summarize_clocks(lines):
+    sm, smax, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in lines:
+        f = [x.strip() for x in ln.split(",")]
+        if len(f) < 9:
+            continue
+        try:
+            sm.append(float(f[1]))
+            smax.append(float(f[2]))
+        except ValueError:
+            continue
+        for name, v in zip(names, f[5:9]):
+            if v.lower() == "active":
+                reasons.add(name)
+    if not sm:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+    sm.sort()
+    return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def workload(args):
+    from fluidsim_gb300 import cases
+
+    cfg, pa = cases.make(cases.fsi_4m())
+    return cfg, pa
+
+
+def workload_desc(cfg, pa):
+    return {
+        "workload": "fsi_4m: dam break, %d fluid + %d solid (free 30^3 cube) + %d wall particles, dx=0.005 m, "
+                    "dt=5e-5 s, %d solid sub-steps, Gaussian kernel h=1.3dx, FP32" %
+                    (pa.n_fluid, pa.n_solid, pa.n_virt, cfg.solid_sub_step),
+        "n_fluid": pa.n_fluid, "n_solid": pa.n_solid, "n_virt": pa.n_virt,
+        "l2": "inputs larger than L2 (particle state > 300 MB vs 129 MB L2); no flush",
+    }
+
+
+def cpu_oracle_rate(cfg, pa, precision, steps, threads=0):
+    from oracle import oracle as orc
+
+    o = orc.OracleSim(cfg, pa, precision, threads=threads)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return (pa.n_fluid + pa.n_solid) * steps / dt, dt
+
+
+def run_reference(args, dist):
+    """CPU restatement of the reference path (FP32 oracle, all host threads)."""
+    if dist.rank != 0:
+        return 0
+    cfg, pa = workload(args)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_oracle_rate(cfg, pa, "f32", 1, cores)
+    rate, dt = cpu_oracle_rate(cfg, pa, "f32", args.steps, cores)
+    desc = workload_desc(cfg, pa)
+    line = {
+        "impl": "reference", "metric": "particle-updates/s", "value": rate, "unit": "particle-updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": desc,
+        "cpu_baseline": {"value": rate, "unit": "particle-updates/s", "cores": cores, "kind": "port",
+                         "sample": "%d fluid steps of the full workload (oracle FP32 restatement of the "
+                                   "reference CUDA path, OpenMP)" % args.steps},
+        "e2e": {"value": rate, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is a CUDA-only program; its CUDA sources need the unvendored glm library and are "
+                "not built here, so the reference arm is the CPU restatement of its algorithm",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, dist):
+    from fluidsim_gb300 import api
+
+    dev = dist.local
+    cfg, pa = workload(args)
+    nupd = pa.n_fluid + pa.n_solid
+    sim = api.Simulation(cfg, pa, device=dev)
+    launches = sim.launches_per_step()
+    sim.step(max(args.warmup, 3))
+    sim.sync()
+
+    # ---- device-resident timed region
+    clocks = ClockSampler(dev)
+    dist.barrier()
+    sim.sync()
+    clocks.start()
+    t_wall = time.perf_counter()
+    ms = sim.time_steps(args.steps)
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    dist.barrier()
+    ms = dist.max(ms)
+    value = nupd * args.steps * dist.ws / (ms * 1e-3)
+
+    # ---- per-kernel timing of the dominant kernel (fluid sweep), CUDA events on the handle's stream
+    tot_ms, sweep_ms = sim.time_sweep(args.steps)
+    sweep_ms = dist.max(sweep_ms)
+    t_launch = sweep_ms * 1e-3 / args.steps
+    alg_bytes = ALG_BYTES_FLUID * pa.n_fluid
+    peaks, peak_src = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / t_launch / 1e9
+    step_bytes = (ALG_BYTES_FLUID * pa.n_fluid + pa.n_solid * (ALG_BYTES_SOLID * cfg.solid_sub_step +
+                                                               ALG_BYTES_SOLID_STEP) + ALG_BYTES_VIRT * pa.n_virt)
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "fluid_sweep_traffic.json")
+    if os.path.exists(prof):
+        try:
+            with open(prof) as f:
+                traffic = json.load(f).get("bytes_per_launch_full_size")
+        except (OSError, ValueError):
+            traffic = None
+
+    # ---- end to end through the C ABI with pinned host buffers
+    bufs = {k: api.PinnedBuffer(shape) for k, shape in (
+        ("fluid_pos", (pa.n_fluid, 3)), ("fluid_vel", (pa.n_fluid, 3)), ("fluid_rho", (pa.n_fluid,)),
+        ("fluid_p", (pa.n_fluid,)), ("solid_pos", (pa.n_solid, 3)), ("solid_vel", (pa.n_solid, 3)))}
+    for k, b in bufs.items():
+        sim.get(k, out=b.array)
+    h2d = sum(b.nbytes for b in bufs.values())
+    d2h = h2d
+    e2e_steps = max(1, min(args.steps, 20))
+    dist.barrier()
+    sim.sync()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for k, b in bufs.items():
+            sim.set_ptr(k, b.ptr, b.nbytes)
+        sim.step(1)
+        for k, b in bufs.items():
+            sim.get_ptr(k, b.ptr, b.nbytes)
+    sim.sync()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = nupd * e2e_steps * dist.ws / e2e_s
+    for b in bufs.values():
+        b.free()
+    sim.close()
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if dist.ws == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        rate, dt = cpu_oracle_rate(cfg, pa, "f64", args.cpu_steps, cores)
+        cpu = {"value": rate, "unit": "particle-updates/s", "cores": cores, "kind": "port",
+               "sample": "%d fluid steps of the full workload in the FP64 oracle (%.1f s)" % (args.cpu_steps, dt)}
+
+    if dist.rank == 0:
+        line = {
+            "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": dist.ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(workload_desc(cfg, pa), parallelism="replicas%d" % dist.ws),
+            "e2e": {"value": e2e, "unit": "particle-updates/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "roofline": {"bound": "hbm", "kernel": "k_fluid_sweep", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "peak_source": peak_src,
+                         "alg_bytes_per_launch": alg_bytes, "launch_ms": t_launch * 1e3,
+                         "step_alg_bytes": step_bytes,
+                         "step_frac": step_bytes / (ms * 1e-3 / args.steps) / 1e9 / hbm_peak},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": launches * args.steps,
+            "wall_s_timed": t_wall,
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, dist)
+        return run_gb300(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,1846 @@
+// fsim_sim.cu — device state, sm_103a kernels and the simulation half of the
+// C ABI (include/fluidsim.h).
+//
+// Layout in HBM (one handle = one instance):
+//   fluid    float4 posr = (x, y, z, rho), float4 velp = (u, v, w, p), int orig,
+//            all double-buffered; particles are kept sorted by cell.  The cell
+//            phase sorts buffer `cur` into the other one; the fused fluid
+//            sweep + update reads the sorted buffer and writes the updated
+//            state into the other, in the same order.
+//   solid    float4 pos/vel/ref, int type/orig, double-buffered the same way;
+//            per-step products (normal+pressure, F, P, L^-1, du/dt) single.
+//   virtual  sorted by cell once at creation (walls never move); float4 posr
+//            (rho in .w) and velp (mirrored velocity, pressure) rewritten every
+//            step; float4 normal computed once (a static quantity).
+//   cells    per species an exclusive-scan start array of cell_number_total+1
+//            ints: the particles of cell c are [start[c], start[c+1]).
+//            Because cells are linearised x-major (src/pair.cu:20-23), the
+//            three cells (x, y, z-1..z+1) are contiguous, so the 27-cell
+//            neighbourhood is 9 contiguous index ranges.
+//
+// The neighbour sweeps gather every particle's neighbours (one owner per
+// output, no atomics on physics sums): results are deterministic.
+#include "fsim_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstring>
+#include <new>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- params
+struct DevParams {
+    // kernel (src/kernel.cpp:43-60)
+    float R2, h, h_inv2, kdiff, kc1, kc2, eps_h2;
+    // fluid (src/properties.cpp:47-57)
+    float c0, c0_inv, rho0, rho0_inv, gamma, rho2p, min_p, min_rho, max_rho, mu10, vmax;
+    int viscid;
+    // solid (src/properties.cpp:59-66)
+    float rho_s_inv, lambda, mu_s, cs_s, alpha, beta;
+    // physics, time
+    float gx, gy, gz, dt, dt_sub;
+    // domain
+    float dmin[3], dmax[3], cmin[3], cinv[3];
+    int nx, ny, nz, ncell;
+};
+
+enum : unsigned { FLAG_OUT_OF_GRID = 1u };
+
+constexpr int kBlock = 256;
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int kMaxScanTiles = 16384; // cell grids up to 67M cells
+
+__host__ __device__ inline int blocks_for(long long n, int b) { return (int)((n + b - 1) / b); }
+
+// ------------------------------------------------------------- cell math
+// findPositionCell (src/pair.cu:8-24): per-axis truncation of the FP32
+// (p - min) * inv.  Out-of-grid indices (impossible for clamped positions)
+// are clamped and flagged instead of indexing out of bounds.
+__device__ __forceinline__ int axis_cell(float p, float mn, float inv, int n, bool &bad)
+{
+    int c = (int)__fmul_rn(__fsub_rn(p, mn), inv);
+    if (c < 0 || c >= n) {
+        bad = true;
+        c = c < 0 ? 0 : n - 1;
+    }
+    return c;
+}
+
+__device__ __forceinline__ int cell_index(const DevParams &P, float x, float y, float z, unsigned *flags)
+{
+    bool bad = false;
+    const int cx = axis_cell(x, P.cmin[0], P.cinv[0], P.nx, bad);
+    const int cy = axis_cell(y, P.cmin[1], P.cinv[1], P.ny, bad);
+    const int cz = axis_cell(z, P.cmin[2], P.cinv[2], P.nz, bad);
+    if (bad && flags) atomicOr(flags, FLAG_OUT_OF_GRID);
+    return cx * P.ny * P.nz + cy * P.nz + cz;
+}
+
+// FP32 squared distance; the oracle's neighbour counts use the same formula.
+__device__ __forceinline__ float dist2(float dx, float dy, float dz)
+{
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// The 9 z-contiguous rows of the 27-cell neighbourhood of cell c.
+struct Rows {
+    int base[9];
+    int z0, z1, count;
+};
+__device__ __forceinline__ void neighbor_rows(const DevParams &P, int c, Rows &r)
+{
+    const int cx = c / (P.ny * P.nz);
+    const int rem = c - cx * P.ny * P.nz;
+    const int cy = rem / P.nz;
+    const int cz = rem - cy * P.nz;
+    r.z0 = max(cz - 1, 0);
+    r.z1 = min(cz + 1, P.nz - 1) + 1;
+    r.count = 0;
+    for (int ox = -1; ox <= 1; ++ox) {
+        const int x = cx + ox;
+        if (x < 0 || x >= P.nx) continue;
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int y = cy + oy;
+            if (y < 0 || y >= P.ny) continue;
+            r.base[r.count++] = (x * P.ny + y) * P.nz;
+        }
+    }
+}
+
+// ------------------------------------------------------- counting sort
+__global__ void k_hash(DevParams P, const float4 *__restrict__ pos, int n, int *__restrict__ key,
+                       int *__restrict__ slot, int *__restrict__ cnt, unsigned *flags)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const float4 p = pos[s];
+    const int c = cell_index(P, p.x, p.y, p.z, flags);
+    key[s] = c;
+    slot[s] = atomicAdd(&cnt[c], 1);
+}
+
+struct ScanJob {
+    const int *in;
+    int *out;
+    int n;
+    int *partial;
+};
+struct ScanJobs {
+    ScanJob j[2];
+};
+
+__device__ __forceinline__ int warp_inclusive_scan(int v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// exclusive scan of one value per thread over a 1024-thread block; returns the
+// block total in *total
+__device__ __forceinline__ int block_exclusive_scan(int v, int *total)
+{
+    __shared__ int warp_sums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int inc = warp_inclusive_scan(v);
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        int w = lane < nw ? warp_sums[lane] : 0;
+        w = warp_inclusive_scan(w);
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const int before = warp == 0 ? 0 : warp_sums[warp - 1];
+    *total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before + inc - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(ScanJobs jobs)
+{
+    const ScanJob J = jobs.j[blockIdx.y];
+    const int tiles = blocks_for(J.n, kScanTile);
+    if ((int)blockIdx.x >= tiles) return;
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < J.n) s += J.in[base + k];
+    int total;
+    block_exclusive_scan(s, &total);
+    if (threadIdx.x == 0) J.partial[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_partials(ScanJobs jobs)
+{
+    const ScanJob J = jobs.j[blockIdx.x];
+    const int tiles = blocks_for(J.n, kScanTile);
+    int carry = 0;
+    for (int b0 = 0; b0 < tiles; b0 += kScanThreads) {
+        const int i = b0 + threadIdx.x;
+        const int v = i < tiles ? J.partial[i] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, &total);
+        if (i < tiles) J.partial[i] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) J.out[J.n] = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(ScanJobs jobs)
+{
+    const ScanJob J = jobs.j[blockIdx.y];
+    const int tiles = blocks_for(J.n, kScanTile);
+    if ((int)blockIdx.x >= tiles) return;
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < J.n ? J.in[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int run = block_exclusive_scan(s, &total) + J.partial[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < J.n) J.out[base + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void k_scatter(const int *__restrict__ key, const int *__restrict__ slot, const int *__restrict__ start,
+                          int *__restrict__ tmp, int n)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    tmp[start[key[s]] + slot[s]] = s;
+}
+
+// Rank inside the cell by previous position: the new order is sorted by
+// (cell, previous sorted position), a stable and deterministic order.
+__device__ __forceinline__ int stable_dst(const int *__restrict__ tmp, const int *__restrict__ key,
+                                          const int *__restrict__ start, int d, int &src, int &cell)
+{
+    src = tmp[d];
+    cell = key[src];
+    const int b = start[cell], e = start[cell + 1];
+    int rank = 0;
+    for (int t = b; t < e; ++t) rank += tmp[t] < src;
+    return b + rank;
+}
+
+__global__ void k_gather_fluid(const int *__restrict__ tmp, const int *__restrict__ key, const int *__restrict__ start,
+                               int n, const float4 *__restrict__ posr_in, const float4 *__restrict__ velp_in,
+                               const int *__restrict__ orig_in, float4 *__restrict__ posr_out,
+                               float4 *__restrict__ velp_out, int *__restrict__ orig_out, int *__restrict__ cell_out)
+{
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    int src, cell;
+    const int dst = stable_dst(tmp, key, start, d, src, cell);
+    posr_out[dst] = posr_in[src];
+    velp_out[dst] = velp_in[src];
+    orig_out[dst] = orig_in[src];
+    cell_out[dst] = cell;
+}
+
+__global__ void k_gather_solid(const int *__restrict__ tmp, const int *__restrict__ key, const int *__restrict__ start,
+                               int n, const float4 *__restrict__ pos_in, const float4 *__restrict__ vel_in,
+                               const float4 *__restrict__ ref_in, const int *__restrict__ type_in,
+                               const int *__restrict__ orig_in, float4 *__restrict__ pos_out,
+                               float4 *__restrict__ vel_out, float4 *__restrict__ ref_out, int *__restrict__ type_out,
+                               int *__restrict__ orig_out, int *__restrict__ cell_out)
+{
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    int src, cell;
+    const int dst = stable_dst(tmp, key, start, d, src, cell);
+    pos_out[dst] = pos_in[src];
+    vel_out[dst] = vel_in[src];
+    ref_out[dst] = ref_in[src];
+    type_out[dst] = type_in[src];
+    orig_out[dst] = orig_in[src];
+    cell_out[dst] = cell;
+}
+
+// ------------------------------------------------------------ EOS
+// densityToPressure (src/fluid.cu:16-24): Tait EOS, floored at min_pressure.
+__device__ __forceinline__ float tait_pressure(const DevParams &P, float rho)
+{
+    const float p = (__powf(rho * P.rho0_inv, P.gamma) - 1.0f) * P.rho2p;
+    return fmaxf(p, P.min_p);
+}
+
+// ------------------------------------------------------ Riemann pair term
+// fluidFluidCalculate / fluidSolidCalculate / fluidVirtCalculate
+// (src/fluid.cu:26-167), algebraically regrouped:
+//   P*   = (rho_i p_j + rho_j p_i)/(rho_i+rho_j) [+ rho_i rho_j du/(rho_i+rho_j) * lim]
+//   (u_i - v*).dx = (rho_j (u_i-u_j).dx - (p_i-p_j) r / c0) / (rho_i+rho_j)
+//   du/dt += w dx (-2 P* + 10 mu vis) / rho_i,  drho/dt += 2 rho_i w (u_i - v*).dx
+// The caller multiplies by 1/rho_i and 2 rho_i once per particle.
+struct PairAcc {
+    float drho, ax, ay, az;
+};
+
+template <bool LIMITER, bool CLAMP_PS>
+__device__ __forceinline__ void riemann_pair(const DevParams &P, float dx, float dy, float dz, float r2, float uix,
+                                             float uiy, float uiz, float rhoi, float pi, float ujx, float ujy,
+                                             float ujz, float rhoj, float pj, PairAcc &A)
+{
+    const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+    const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+    const float rs_inv = __fdividef(1.0f, rhoi + rhoj);
+    const float a = (uix - ujx) * dx + (uiy - ujy) * dy + (uiz - ujz) * dz;
+    const float du = a * inv_r;
+    float ps = (rhoi * pj + rhoj * pi) * rs_inv;
+    if (du >= 0.0f) ps += rhoi * rhoj * du * rs_inv * (LIMITER ? fminf(3.0f * du, P.c0) : P.c0);
+    if (CLAMP_PS) ps = fmaxf(ps, 0.0f);
+    const float r = r2 * inv_r;
+    A.drho += (rhoj * a - (pi - pj) * r * P.c0_inv) * rs_inv * w;
+    float f = -2.0f * ps;
+    if (P.viscid) f += P.mu10 * __fdividef(-a, r2 + P.eps_h2);
+    f *= w;
+    A.ax += f * dx;
+    A.ay += f * dy;
+    A.az += f * dz;
+}
+
+// ------------------------------------------------------- fluid sweep
+struct FluidSweepArgs {
+    const float4 *posr, *velp;   // sorted step-start state
+    const int *start_f, *cell_f, *orig_in;
+    const float4 *s_pos, *s_vel, *s_np; // solid position, velocity, (normal, pressure)
+    const int *start_s;
+    const float4 *v_posr, *v_velp;
+    const int *start_v;
+    float4 *posr_out, *velp_out;
+    int *orig_out;
+    float *drho_out;
+    float4 *dudt_out;
+    int n;
+};
+
+// findFluidPair + fluidUpdate (src/fluid.cu:169-269), fused: the sweep reads
+// the step-start buffer and writes the integrated state to the other buffer.
+template <bool KEEP>
+__global__ void __launch_bounds__(kBlock) k_fluid_sweep(const DevParams P, const FluidSweepArgs A)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    const float4 pr = A.posr[i], vp = A.velp[i];
+    Rows rows;
+    neighbor_rows(P, A.cell_f[i], rows);
+    PairAcc acc = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int r = 0; r < rows.count; ++r) {
+        const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+        // fluid neighbours
+        for (int j = A.start_f[c0], je = A.start_f[c1]; j < je; ++j) {
+            const float4 q = A.posr[j];
+            const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2) {
+                const float4 u = A.velp[j];
+                riemann_pair<true, false>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q.w, u.w,
+                                          acc);
+            }
+        }
+        // virtual neighbours (P* >= 0)
+        for (int j = A.start_v[c0], je = A.start_v[c1]; j < je; ++j) {
+            const float4 q = A.v_posr[j];
+            const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2) {
+                const float4 u = A.v_velp[j];
+                riemann_pair<true, true>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q.w, u.w,
+                                         acc);
+            }
+        }
+        // solid neighbours: mirrored velocity, Shepard pressure, rho_j = rho_i, no limiter
+        for (int j = A.start_s[c0], je = A.start_s[c1]; j < je; ++j) {
+            const float4 q = A.s_pos[j];
+            const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2) {
+                const float4 np = A.s_np[j], sv = A.s_vel[j];
+                const float k2 = 2.0f * ((vp.x - sv.x) * np.x + (vp.y - sv.y) * np.y + (vp.z - sv.z) * np.z);
+                riemann_pair<false, false>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, vp.x - k2 * np.x,
+                                           vp.y - k2 * np.y, vp.z - k2 * np.z, pr.w, np.w, acc);
+            }
+        }
+    }
+    const float rho_inv = __fdividef(1.0f, pr.w);
+    float drho = 2.0f * pr.w * acc.drho;
+    float ax = acc.ax * rho_inv, ay = acc.ay * rho_inv, az = acc.az * rho_inv;
+    // fluidUpdate: NaN scrub, Euler step with the old velocity, clamps, EOS, speed cap
+    if (!(drho == drho)) drho = 0.0f;
+    if (!(ax == ax && ay == ay && az == az)) ax = ay = az = 0.0f;
+    float x = pr.x + vp.x * P.dt, y = pr.y + vp.y * P.dt, z = pr.z + vp.z * P.dt;
+    float ux = vp.x + (ax + P.gx) * P.dt, uy = vp.y + (ay + P.gy) * P.dt, uz = vp.z + (az + P.gz) * P.dt;
+    float rho = pr.w + drho * P.dt;
+    rho = fminf(fmaxf(rho, P.min_rho), P.max_rho);
+    const float p = tait_pressure(P, rho);
+    x = fminf(fmaxf(x, P.dmin[0]), P.dmax[0]);
+    y = fminf(fmaxf(y, P.dmin[1]), P.dmax[1]);
+    z = fminf(fmaxf(z, P.dmin[2]), P.dmax[2]);
+    const float speed = sqrtf(ux * ux + uy * uy + uz * uz);
+    if (speed > P.vmax) {
+        const float s = P.vmax / speed;
+        ux *= s;
+        uy *= s;
+        uz *= s;
+    }
+    A.posr_out[i] = make_float4(x, y, z, rho);
+    A.velp_out[i] = make_float4(ux, uy, uz, p);
+    A.orig_out[i] = A.orig_in[i];
+    if (KEEP) {
+        A.drho_out[i] = drho;
+        A.dudt_out[i] = make_float4(ax, ay, az, 0.0f);
+    }
+}
+
+// ------------------------------------------------------- virtual particles
+// getVirtData (src/virt.cu:9-75): nearest fluid particle's rho, hydrostatically
+// corrected p and velocity mirrored about the (static) wall normal.  Ties in
+// distance go to the smaller input id.
+__global__ void __launch_bounds__(kBlock) k_virt(const DevParams P, const float4 *__restrict__ v_posr_in,
+                                                 const float4 *__restrict__ v_normal, const int *__restrict__ v_cell,
+                                                 const float4 *__restrict__ fposr, const float4 *__restrict__ fvelp,
+                                                 const int *__restrict__ forig, const int *__restrict__ start_f,
+                                                 float4 *__restrict__ v_posr, float4 *__restrict__ v_velp, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xi = v_posr_in[i];
+    Rows rows;
+    neighbor_rows(P, v_cell[i], rows);
+    float best = FSIM_LARGE_FLOAT;
+    int best_j = -1, best_orig = INT_MAX;
+    for (int r = 0; r < rows.count; ++r) {
+        for (int j = start_f[rows.base[r] + rows.z0], je = start_f[rows.base[r] + rows.z1]; j < je; ++j) {
+            const float4 q = fposr[j];
+            const float d2 = dist2(q.x - xi.x, q.y - xi.y, q.z - xi.z);
+            if (d2 < best) {
+                best = d2;
+                best_j = j;
+                best_orig = forig[j];
+            } else if (d2 == best) {
+                const int o = forig[j];
+                if (o < best_orig) {
+                    best_j = j;
+                    best_orig = o;
+                }
+            }
+        }
+    }
+    float rho = P.rho0, p = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
+    if (best_j >= 0) {
+        const float4 q = fposr[best_j], u = fvelp[best_j];
+        rho = q.w;
+        p = u.w - rho * (P.gx * (q.x - xi.x) + P.gy * (q.y - xi.y) + P.gz * (q.z - xi.z));
+        ux = u.x;
+        uy = u.y;
+        uz = u.z;
+    }
+    const float4 nrm = v_normal[i];
+    const float k2 = 2.0f * (ux * nrm.x + uy * nrm.y + uz * nrm.z);
+    v_posr[i] = make_float4(xi.x, xi.y, xi.z, rho);
+    v_velp[i] = make_float4(ux - k2 * nrm.x, uy - k2 * nrm.y, uz - k2 * nrm.z, p);
+}
+
+// Wall normal of every virtual particle (src/virt.cu:52-70): minus the kernel
+// gradient sum over the other virtual particles, normalised, zero when its
+// squared length is below EPS_FOR_SUM.  Walls never move: computed once.
+__global__ void k_virt_normal(const DevParams P, const float4 *__restrict__ v_posr, const int *__restrict__ v_cell,
+                              const int *__restrict__ start_v, float4 *__restrict__ v_normal, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xi = v_posr[i];
+    Rows rows;
+    neighbor_rows(P, v_cell[i], rows);
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    for (int r = 0; r < rows.count; ++r) {
+        for (int j = start_v[rows.base[r] + rows.z0], je = start_v[rows.base[r] + rows.z1]; j < je; ++j) {
+            if (j == i) continue;
+            const float4 q = v_posr[j];
+            const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2) {
+                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+                nx -= dx * w;
+                ny -= dy * w;
+                nz -= dz * w;
+            }
+        }
+    }
+    const float l2 = nx * nx + ny * ny + nz * nz;
+    if (l2 < FSIM_EPS_FOR_SUM) {
+        nx = ny = nz = 0.0f;
+    } else {
+        const float s = rsqrtf(l2);
+        nx *= s;
+        ny *= s;
+        nz *= s;
+    }
+    v_normal[i] = make_float4(nx, ny, nz, 0.0f);
+}
+
+// ------------------------------------------------------- fluid-solid coupling
+// solidCoupleUpdate (src/solid.cu:262-344): solid normal from the solid
+// neighbours' kernel gradients, solid pressure as the Shepard average of the
+// fluid pressure.
+__global__ void __launch_bounds__(kBlock) k_couple(const DevParams P, const float4 *__restrict__ s_pos,
+                                                   const int *__restrict__ s_cell, const int *__restrict__ start_s,
+                                                   const float4 *__restrict__ fposr, const float4 *__restrict__ fvelp,
+                                                   const int *__restrict__ start_f, float4 *__restrict__ s_np, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xi = s_pos[i];
+    Rows rows;
+    neighbor_rows(P, s_cell[i], rows);
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f, psum = 0.0f, wsum = 0.0f;
+    for (int r = 0; r < rows.count; ++r) {
+        const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+        for (int j = start_f[c0], je = start_f[c1]; j < je; ++j) {
+            const float4 q = fposr[j];
+            const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2) {
+                const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
+                wsum += w;
+                psum += fvelp[j].w * w;
+            }
+        }
+        for (int j = start_s[c0], je = start_s[c1]; j < je; ++j) {
+            const float4 q = s_pos[j];
+            const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2) {
+                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+                nx -= dx * w;
+                ny -= dy * w;
+                nz -= dz * w;
+            }
+        }
+    }
+    const float l2 = nx * nx + ny * ny + nz * nz;
+    if (l2 < FSIM_EPS_FOR_SUM) {
+        nx = ny = nz = 0.0f;
+    } else {
+        const float s = rsqrtf(l2);
+        nx *= s;
+        ny *= s;
+        nz *= s;
+    }
+    const float p = wsum > FSIM_EPS_FLOAT ? fmaxf(psum / wsum, P.min_p) : 0.0f;
+    s_np[i] = make_float4(nx, ny, nz, p);
+}
+
+// ------------------------------------------------------------ solid
+struct SolidArgs {
+    float4 *pos, *vel;
+    const float4 *ref;
+    const int *type, *cell, *start_s;
+    const float4 *np;
+    float *F, *Pk, *L, *PL, *AV; // 9 floats per particle, row-major
+    float4 *dudt, *couple;
+    const float4 *fposr, *fvelp;
+    const int *start_f;
+    int n;
+};
+
+struct M3 {
+    float m[9];
+};
+__device__ __forceinline__ M3 mmul(const M3 &a, const M3 &b)
+{
+    M3 r;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            r.m[3 * i + j] = a.m[3 * i] * b.m[j] + a.m[3 * i + 1] * b.m[3 + j] + a.m[3 * i + 2] * b.m[6 + j];
+    return r;
+}
+__device__ __forceinline__ M3 cofactor(const M3 &a)
+{
+    M3 c;
+    c.m[0] = a.m[4] * a.m[8] - a.m[5] * a.m[7];
+    c.m[1] = a.m[5] * a.m[6] - a.m[3] * a.m[8];
+    c.m[2] = a.m[3] * a.m[7] - a.m[4] * a.m[6];
+    c.m[3] = a.m[2] * a.m[7] - a.m[1] * a.m[8];
+    c.m[4] = a.m[0] * a.m[8] - a.m[2] * a.m[6];
+    c.m[5] = a.m[1] * a.m[6] - a.m[0] * a.m[7];
+    c.m[6] = a.m[1] * a.m[5] - a.m[2] * a.m[4];
+    c.m[7] = a.m[2] * a.m[3] - a.m[0] * a.m[5];
+    c.m[8] = a.m[0] * a.m[4] - a.m[1] * a.m[3];
+    return c;
+}
+
+// solidDeformationCalculate (src/solid.cu:10-79): F and L over the
+// reference-configuration neighbours, L^-1 (identity when singular),
+// F <- F L^-1, Green strain, St-Venant-Kirchhoff 2nd Piola, P = F S.
+// Also stores P L^-1 and cof(F) L^-1 (= det(F) F^-T L^-1) for the force sweep.
+__global__ void __launch_bounds__(kBlock) k_solid_deform(const DevParams P, const SolidArgs S)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const float4 Xi = S.ref[i], xi = S.pos[i];
+    Rows rows;
+    neighbor_rows(P, S.cell[i], rows);
+    M3 F, L;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) F.m[k] = L.m[k] = 0.0f;
+    for (int r = 0; r < rows.count; ++r) {
+        for (int j = S.start_s[rows.base[r] + rows.z0], je = S.start_s[rows.base[r] + rows.z1]; j < je; ++j) {
+            const float4 Xj = S.ref[j];
+            const float dX[3] = {Xj.x - Xi.x, Xj.y - Xi.y, Xj.z - Xi.z};
+            const float r2 = dist2(dX[0], dX[1], dX[2]);
+            if (r2 < P.R2) {
+                const float4 xj = S.pos[j];
+                const float dx[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
+                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float ra = dx[a] * w, la = dX[a] * w;
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) {
+                        F.m[3 * a + b] += ra * dX[b];
+                        L.m[3 * a + b] += la * dX[b];
+                    }
+                }
+            }
+        }
+    }
+    const M3 cl = cofactor(L);
+    const float det = L.m[0] * cl.m[0] + L.m[1] * cl.m[1] + L.m[2] * cl.m[2];
+    M3 Linv;
+    if (det != 0.0f) {
+        const float id = 1.0f / det;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) Linv.m[3 * a + b] = cl.m[3 * b + a] * id;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Linv.m[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+    }
+    F = mmul(F, Linv);
+    // E = (F^T F - I)/2, S = 2 mu E + lambda tr(E) I, P = F S
+    M3 E;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+            E.m[3 * a + b] =
+                0.5f * (F.m[a] * F.m[b] + F.m[3 + a] * F.m[3 + b] + F.m[6 + a] * F.m[6 + b] - (a == b ? 1.0f : 0.0f));
+    const float tr = E.m[0] + E.m[4] + E.m[8];
+    M3 Sm;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Sm.m[k] = 2.0f * P.mu_s * E.m[k] + ((k % 4 == 0) ? P.lambda * tr : 0.0f);
+    const M3 Pk = mmul(F, Sm);
+    const M3 PL = mmul(Pk, Linv);
+    const M3 AV = mmul(cofactor(F), Linv);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        S.F[9 * i + k] = F.m[k];
+        S.Pk[9 * i + k] = Pk.m[k];
+        S.L[9 * i + k] = Linv.m[k];
+        S.PL[9 * i + k] = PL.m[k];
+        S.AV[9 * i + k] = AV.m[k];
+    }
+}
+
+// solidForceCalculate (src/solid.cu:81-207): stress divergence + artificial
+// viscosity over solid neighbours (reference configuration), fluid traction
+// over fluid neighbours (current configuration, fluid already advanced).
+__global__ void __launch_bounds__(kBlock) k_solid_force(const DevParams P, const SolidArgs S)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const float4 xi = S.pos[i], Xi = S.ref[i], vi = S.vel[i], ni = S.np[i];
+    Rows rows;
+    neighbor_rows(P, S.cell[i], rows);
+    float PLi[9], AVi[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        PLi[k] = S.PL[9 * i + k];
+        AVi[k] = S.AV[9 * i + k];
+    }
+    float cx = 0.0f, cy = 0.0f, cz = 0.0f, ax = 0.0f, ay = 0.0f, az = 0.0f;
+    for (int r = 0; r < rows.count; ++r) {
+        const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+        // solidFluidCouple (src/solid.cu:81-117)
+        for (int j = S.start_f[c0], je = S.start_f[c1]; j < je; ++j) {
+            const float4 q = S.fposr[j];
+            const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2) {
+                const float4 u = S.fvelp[j];
+                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+                const float k2 = 2.0f * ((u.x - vi.x) * ni.x + (u.y - vi.y) * ni.y + (u.z - vi.z) * ni.z);
+                // u_i - u_j = -k2 n ; du = (u_i - u_j).e
+                const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+                const float du = -k2 * (ni.x * dx + ni.y * dy + ni.z * dz) * inv_r;
+                float ps = 0.5f * (ni.w + u.w);
+                if (du >= 0.0f) ps += 0.5f * q.w * du * P.c0;
+                const float f = -2.0f * ps * P.rho_s_inv * w;
+                cx += f * dx;
+                cy += f * dy;
+                cz += f * dz;
+            }
+        }
+        // solidSolidForce (src/solid.cu:119-157)
+        for (int j = S.start_s[c0], je = S.start_s[c1]; j < je; ++j) {
+            const float4 Xj = S.ref[j];
+            const float dX = Xj.x - Xi.x, dY = Xj.y - Xi.y, dZ = Xj.z - Xi.z;
+            const float r2 = dist2(dX, dY, dZ);
+            if (r2 < P.R2) {
+                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+                const float *PLj = S.PL + 9 * j;
+                const float ws = w * P.rho_s_inv;
+                ax += ((PLj[0] + PLi[0]) * dX + (PLj[1] + PLi[1]) * dY + (PLj[2] + PLi[2]) * dZ) * ws;
+                ay += ((PLj[3] + PLi[3]) * dX + (PLj[4] + PLi[4]) * dY + (PLj[5] + PLi[5]) * dZ) * ws;
+                az += ((PLj[6] + PLi[6]) * dX + (PLj[7] + PLi[7]) * dY + (PLj[8] + PLi[8]) * dZ) * ws;
+                const float4 xj = S.pos[j], vj = S.vel[j];
+                const float ddx = xj.x - xi.x, ddy = xj.y - xi.y, ddz = xj.z - xi.z;
+                const float dvdx = (vj.x - vi.x) * ddx + (vj.y - vi.y) * ddy + (vj.z - vi.z) * ddz;
+                const float nu = P.h * dvdx / (ddx * ddx + ddy * ddy + ddz * ddz + P.eps_h2);
+                const float visc = (P.alpha * nu * P.cs_s - P.beta * nu * nu) * w;
+                ax += (AVi[0] * dX + AVi[1] * dY + AVi[2] * dZ) * visc;
+                ay += (AVi[3] * dX + AVi[4] * dY + AVi[5] * dZ) * visc;
+                az += (AVi[6] * dX + AVi[7] * dY + AVi[8] * dZ) * visc;
+            }
+        }
+    }
+    S.couple[i] = make_float4(cx, cy, cz, 0.0f);
+    S.dudt[i] = make_float4(ax + cx, ay + cy, az + cz, 0.0f);
+}
+
+// solidUpdate (src/solid.cu:209-239)
+__global__ void k_solid_update(const DevParams P, const SolidArgs S)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const int t = S.type[i];
+    if (t == 1) { // FIXED_SOLID
+        float4 v = S.vel[i];
+        S.vel[i] = make_float4(0.0f, 0.0f, 0.0f, v.w);
+        S.dudt[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    } else if (t == 0) { // UNCONSTRAINED_SOLID
+        const float4 x = S.pos[i], v = S.vel[i], a = S.dudt[i];
+        float nx = x.x + v.x * P.dt_sub, ny = x.y + v.y * P.dt_sub, nz = x.z + v.z * P.dt_sub;
+        S.vel[i] = make_float4(v.x + (a.x + P.gx) * P.dt_sub, v.y + (a.y + P.gy) * P.dt_sub,
+                               v.z + (a.z + P.gz) * P.dt_sub, v.w);
+        nx = fminf(fmaxf(nx, P.dmin[0]), P.dmax[0]);
+        ny = fminf(fmaxf(ny, P.dmin[1]), P.dmax[1]);
+        nz = fminf(fmaxf(nz, P.dmin[2]), P.dmax[2]);
+        S.pos[i] = make_float4(nx, ny, nz, x.w);
+    }
+}
+
+// ------------------------------------------------------- neighbour counts
+__global__ void k_neighbor_counts(const DevParams P, const float4 *__restrict__ fposr, const int *__restrict__ cell_f,
+                                  const int *__restrict__ start_f, const float4 *__restrict__ s_pos,
+                                  const int *__restrict__ start_s, const float4 *__restrict__ v_posr,
+                                  const int *__restrict__ start_v, int *__restrict__ out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = fposr[i];
+    Rows rows;
+    neighbor_rows(P, cell_f[i], rows);
+    int cf = 0, cs = 0, cv = 0;
+    for (int r = 0; r < rows.count; ++r) {
+        const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+        for (int j = start_f[c0]; j < start_f[c1]; ++j) {
+            const float4 q = fposr[j];
+            cf += dist2(q.x - p.x, q.y - p.y, q.z - p.z) < P.R2;
+        }
+        for (int j = start_s[c0]; j < start_s[c1]; ++j) {
+            const float4 q = s_pos[j];
+            cs += dist2(q.x - p.x, q.y - p.y, q.z - p.z) < P.R2;
+        }
+        for (int j = start_v[c0]; j < start_v[c1]; ++j) {
+            const float4 q = v_posr[j];
+            cv += dist2(q.x - p.x, q.y - p.y, q.z - p.z) < P.R2;
+        }
+    }
+    out[3 * i] = cf;
+    out[3 * i + 1] = cs;
+    out[3 * i + 2] = cv;
+}
+
+// --------------------------------------------------- (un)permutation
+// out[orig[s]] = component(s) of a float4 array: width 3 -> xyz, width 1 -> comp
+__global__ void k_unpermute_f4(const float4 *__restrict__ src, const int *__restrict__ orig, int n, int comp, int width,
+                               float *__restrict__ out)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const float4 v = src[s];
+    const int o = orig[s];
+    if (width == 3) {
+        out[3 * o] = v.x;
+        out[3 * o + 1] = v.y;
+        out[3 * o + 2] = v.z;
+    } else {
+        out[o] = comp == 0 ? v.x : comp == 1 ? v.y : comp == 2 ? v.z : v.w;
+    }
+}
+__global__ void k_unpermute_words(const int *__restrict__ src, const int *__restrict__ orig, int n, int width,
+                                  int *__restrict__ out)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int o = orig[s];
+    for (int k = 0; k < width; ++k) out[width * o + k] = src[width * s + k];
+}
+__global__ void k_permute_in_f4(float4 *__restrict__ dst, const int *__restrict__ orig, int n, int comp, int width,
+                                const float *__restrict__ in)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int o = orig[s];
+    float4 v = dst[s];
+    if (width == 3) {
+        v.x = in[3 * o];
+        v.y = in[3 * o + 1];
+        v.z = in[3 * o + 2];
+    } else if (comp == 3) {
+        v.w = in[o];
+    }
+    dst[s] = v;
+}
+__global__ void k_iota(int *a, int n)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) a[s] = s;
+}
+__global__ void k_pack_f4(const float *__restrict__ xyz, const float *__restrict__ w, int n, float wconst,
+                          float4 *__restrict__ out)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    out[s] = make_float4(xyz[3 * s], xyz[3 * s + 1], xyz[3 * s + 2], w ? w[s] : wconst);
+}
+
+} // namespace
+
+// =================================================================== handle
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int f_after = 0, s_after = 0;
+};
+
+struct fsim_sim {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    fsim_config cfg;
+    fsim_derived der;
+    DevParams P;
+    int nf = 0, ns = 0, nv = 0, ncell = 0;
+    bool keep = false;
+    // fluid
+    float4 *f_posr[2] = {}, *f_velp[2] = {};
+    int *f_orig[2] = {};
+    int *f_cell = nullptr, *f_key = nullptr, *f_slot = nullptr, *f_tmp = nullptr;
+    int *f_cnt = nullptr, *f_start = nullptr;
+    float *f_drho = nullptr;
+    float4 *f_dudt = nullptr;
+    int f_cur = 0;
+    bool f_sorted = false;   // start/cell arrays describe the order of f_cur
+    bool f_deriv_ok = false; // derivative arrays are in the order of f_cur
+    // solid
+    float4 *s_pos[2] = {}, *s_vel[2] = {}, *s_ref[2] = {};
+    int *s_type[2] = {}, *s_orig[2] = {};
+    int *s_cell = nullptr, *s_key = nullptr, *s_slot = nullptr, *s_tmp = nullptr;
+    int *s_cnt = nullptr, *s_start = nullptr;
+    float4 *s_np = nullptr, *s_dudt = nullptr, *s_couple = nullptr;
+    float *s_F = nullptr, *s_P = nullptr, *s_L = nullptr, *s_PL = nullptr, *s_AV = nullptr;
+    int s_cur = 0;
+    bool s_sorted = false;
+    bool s_np_ok = false;    // normal + pressure are in the order of s_cur
+    bool s_mech_ok = false;  // F, P, L^-1, du/dt are in the order of s_cur
+    // virtual
+    float4 *v_posr = nullptr, *v_velp = nullptr, *v_normal = nullptr;
+    int *v_orig = nullptr, *v_cell = nullptr, *v_start = nullptr;
+    // misc
+    int *scan_partials = nullptr; // 2 * kMaxScanTiles
+    unsigned *d_flags = nullptr;
+    void *staging = nullptr;
+    size_t staging_bytes = 0;
+    GraphEntry graphs[2][2];
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> sweep_events;
+    bool instrument = false;
+    int instr_step = 0;
+    std::vector<void *> allocations;
+    int launches = 0; // kernel launches issued by the last enqueued step
+};
+
+namespace {
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            fsim_set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return FSIM_ECUDA;                                                                          \
+        }                                                                                               \
+    } while (0)
+
+#define CK_LAUNCH()                                                                                            \
+    do {                                                                                                       \
+        cudaError_t e_ = cudaGetLastError();                                                                   \
+        if (e_ != cudaSuccess) {                                                                               \
+            fsim_set_error("kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__);    \
+            return FSIM_ECUDA;                                                                                 \
+        }                                                                                                      \
+    } while (0)
+
+template <typename T>
+fsim_status dalloc(fsim_sim *h, T **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fsim_set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+        return FSIM_ENOMEM;
+    }
+    h->allocations.push_back((void *)*p);
+    return FSIM_OK;
+}
+
+void free_all(fsim_sim *h)
+{
+    for (auto &row : h->graphs)
+        for (auto &g : row)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+    for (void *p : h->allocations) cudaFree(p);
+    h->allocations.clear();
+    for (cudaEvent_t e : h->sweep_events) cudaEventDestroy(e);
+    h->sweep_events.clear();
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+void fill_params(fsim_sim *h)
+{
+    const fsim_config &c = h->cfg;
+    const fsim_derived &d = h->der;
+    DevParams &P = h->P;
+    std::memset(&P, 0, sizeof P);
+    P.R2 = d.impact_distance_square;
+    P.h = c.smoothing_length;
+    P.h_inv2 = d.smoothing_length_inverse_square;
+    P.kdiff = d.kernel_differential;
+    P.kc1 = d.kernel_coefficient_1;
+    P.kc2 = d.kernel_coefficient_2;
+    P.eps_h2 = 0.01f * d.smoothing_length_square;
+    P.c0 = c.fluid_sound_speed;
+    P.c0_inv = 1.0f / c.fluid_sound_speed;
+    P.rho0 = c.fluid_density;
+    P.rho0_inv = d.reference_density_inverse;
+    P.gamma = c.gamma;
+    P.rho2p = d.coefficient_rho2p;
+    P.min_p = c.min_pressure;
+    P.min_rho = d.min_density;
+    P.max_rho = d.max_density;
+    P.mu10 = 10.0f * c.viscosity;
+    P.vmax = 0.3f * c.fluid_sound_speed;
+    P.viscid = c.is_viscid ? 1 : 0;
+    P.rho_s_inv = 1.0f / c.solid_density;
+    P.lambda = d.lambda;
+    P.mu_s = d.shear_modulus;
+    P.cs_s = d.solid_sound_speed;
+    P.alpha = c.arti_vis_alpha;
+    P.beta = c.arti_vis_beta;
+    P.gx = d.gravity_vec[0];
+    P.gy = d.gravity_vec[1];
+    P.gz = d.gravity_vec[2];
+    P.dt = c.dt;
+    P.dt_sub = c.dt / (float)c.solid_sub_step;
+    const float lo[3] = {c.xmin, c.ymin, c.zmin}, hi[3] = {c.xmax, c.ymax, c.zmax};
+    for (int k = 0; k < 3; ++k) {
+        P.dmin[k] = lo[k];
+        P.dmax[k] = hi[k];
+        P.cmin[k] = d.cell_min[k];
+        P.cinv[k] = d.interval_inv[k];
+    }
+    P.nx = d.cell_number[0];
+    P.ny = d.cell_number[1];
+    P.nz = d.cell_number[2];
+    P.ncell = d.cell_number_total;
+}
+
+// ---------------------------------------------------------------- phases
+// Counting sort of one species: hash -> scan -> scatter -> stable gather.
+fsim_status enqueue_scan(fsim_sim *h, const int *cnt_f, int *start_f, const int *cnt_s, int *start_s)
+{
+    ScanJobs jobs;
+    std::memset(&jobs, 0, sizeof jobs);
+    int njobs = 0;
+    if (cnt_f) jobs.j[njobs++] = ScanJob{cnt_f, start_f, h->ncell, h->scan_partials};
+    if (cnt_s) jobs.j[njobs++] = ScanJob{cnt_s, start_s, h->ncell, h->scan_partials + kMaxScanTiles};
+    if (!njobs) return FSIM_OK;
+    const int tiles = blocks_for(h->ncell, kScanTile);
+    dim3 g(tiles, njobs);
+    k_scan_reduce<<<g, kScanThreads, 0, h->stream>>>(jobs);
+    CK_LAUNCH();
+    k_scan_partials<<<njobs, kScanThreads, 0, h->stream>>>(jobs);
+    CK_LAUNCH();
+    k_scan_apply<<<g, kScanThreads, 0, h->stream>>>(jobs);
+    CK_LAUNCH();
+    h->launches += 3;
+    return FSIM_OK;
+}
+
+fsim_status enqueue_cell_phase(fsim_sim *h)
+{
+    const int fo = h->f_cur ^ 1, so = h->s_cur ^ 1;
+    if (h->nf) CK(cudaMemsetAsync(h->f_cnt, 0, sizeof(int) * h->ncell, h->stream));
+    if (h->ns) CK(cudaMemsetAsync(h->s_cnt, 0, sizeof(int) * h->ncell, h->stream));
+    if (h->nf) {
+        k_hash<<<blocks_for(h->nf, kBlock), kBlock, 0, h->stream>>>(h->P, h->f_posr[h->f_cur], h->nf, h->f_key,
+                                                                     h->f_slot, h->f_cnt, h->d_flags);
+        CK_LAUNCH();
+        h->launches++;
+    }
+    if (h->ns) {
+        k_hash<<<blocks_for(h->ns, kBlock), kBlock, 0, h->stream>>>(h->P, h->s_pos[h->s_cur], h->ns, h->s_key,
+                                                                     h->s_slot, h->s_cnt, h->d_flags);
+        CK_LAUNCH();
+        h->launches++;
+    }
+    fsim_status st = enqueue_scan(h, h->nf ? h->f_cnt : nullptr, h->f_start, h->ns ? h->s_cnt : nullptr, h->s_start);
+    if (st) return st;
+    if (h->nf) {
+        k_scatter<<<blocks_for(h->nf, kBlock), kBlock, 0, h->stream>>>(h->f_key, h->f_slot, h->f_start, h->f_tmp,
+                                                                        h->nf);
+        CK_LAUNCH();
+        k_gather_fluid<<<blocks_for(h->nf, kBlock), kBlock, 0, h->stream>>>(
+            h->f_tmp, h->f_key, h->f_start, h->nf, h->f_posr[h->f_cur], h->f_velp[h->f_cur], h->f_orig[h->f_cur],
+            h->f_posr[fo], h->f_velp[fo], h->f_orig[fo], h->f_cell);
+        CK_LAUNCH();
+        h->launches += 2;
+        h->f_cur = fo;
+    }
+    if (h->ns) {
+        k_scatter<<<blocks_for(h->ns, kBlock), kBlock, 0, h->stream>>>(h->s_key, h->s_slot, h->s_start, h->s_tmp,
+                                                                        h->ns);
+        CK_LAUNCH();
+        k_gather_solid<<<blocks_for(h->ns, kBlock), kBlock, 0, h->stream>>>(
+            h->s_tmp, h->s_key, h->s_start, h->ns, h->s_pos[h->s_cur], h->s_vel[h->s_cur], h->s_ref[h->s_cur],
+            h->s_type[h->s_cur], h->s_orig[h->s_cur], h->s_pos[so], h->s_vel[so], h->s_ref[so], h->s_type[so],
+            h->s_orig[so], h->s_cell);
+        CK_LAUNCH();
+        h->launches += 2;
+        h->s_cur = so;
+    }
+    h->f_sorted = true;
+    h->s_sorted = true;
+    h->f_deriv_ok = false;
+    h->s_np_ok = false;
+    h->s_mech_ok = false;
+    return FSIM_OK;
+}
+
+fsim_status enqueue_couple(fsim_sim *h)
+{
+    if (!h->nf || !h->ns) return FSIM_OK;
+    k_couple<<<blocks_for(h->ns, kBlock), kBlock, 0, h->stream>>>(h->P, h->s_pos[h->s_cur], h->s_cell, h->s_start,
+                                                                   h->f_posr[h->f_cur], h->f_velp[h->f_cur],
+                                                                   h->f_start, h->s_np, h->ns);
+    CK_LAUNCH();
+    h->launches++;
+    h->s_np_ok = true;
+    return FSIM_OK;
+}
+
+fsim_status enqueue_virt(fsim_sim *h)
+{
+    if (!h->nv) return FSIM_OK;
+    k_virt<<<blocks_for(h->nv, kBlock), kBlock, 0, h->stream>>>(h->P, h->v_posr, h->v_normal, h->v_cell,
+                                                                 h->f_posr[h->f_cur], h->f_velp[h->f_cur],
+                                                                 h->f_orig[h->f_cur], h->f_start, h->v_posr,
+                                                                 h->v_velp, h->nv);
+    CK_LAUNCH();
+    h->launches++;
+    return FSIM_OK;
+}
+
+fsim_status enqueue_fluid(fsim_sim *h)
+{
+    if (!h->nf) return FSIM_OK;
+    const int fo = h->f_cur ^ 1;
+    FluidSweepArgs A;
+    A.posr = h->f_posr[h->f_cur];
+    A.velp = h->f_velp[h->f_cur];
+    A.start_f = h->f_start;
+    A.cell_f = h->f_cell;
+    A.orig_in = h->f_orig[h->f_cur];
+    A.s_pos = h->s_pos[h->s_cur];
+    A.s_vel = h->s_vel[h->s_cur];
+    A.s_np = h->s_np;
+    A.start_s = h->s_start;
+    A.v_posr = h->v_posr;
+    A.v_velp = h->v_velp;
+    A.start_v = h->v_start;
+    A.posr_out = h->f_posr[fo];
+    A.velp_out = h->f_velp[fo];
+    A.orig_out = h->f_orig[fo];
+    A.drho_out = h->f_drho;
+    A.dudt_out = h->f_dudt;
+    A.n = h->nf;
+    const bool timed = h->instrument && (size_t)(2 * h->instr_step + 1) < h->sweep_events.size();
+    if (timed) CK(cudaEventRecord(h->sweep_events[2 * h->instr_step], h->stream));
+    if (h->keep)
+        k_fluid_sweep<true><<<blocks_for(h->nf, kBlock), kBlock, 0, h->stream>>>(h->P, A);
+    else
+        k_fluid_sweep<false><<<blocks_for(h->nf, kBlock), kBlock, 0, h->stream>>>(h->P, A);
+    CK_LAUNCH();
+    if (timed) CK(cudaEventRecord(h->sweep_events[2 * h->instr_step + 1], h->stream));
+    h->launches++;
+    h->f_cur = fo;
+    h->f_deriv_ok = h->keep;
+    return FSIM_OK;
+}
+
+SolidArgs solid_args(fsim_sim *h)
+{
+    SolidArgs S;
+    S.pos = h->s_pos[h->s_cur];
+    S.vel = h->s_vel[h->s_cur];
+    S.ref = h->s_ref[h->s_cur];
+    S.type = h->s_type[h->s_cur];
+    S.cell = h->s_cell;
+    S.start_s = h->s_start;
+    S.np = h->s_np;
+    S.F = h->s_F;
+    S.Pk = h->s_P;
+    S.L = h->s_L;
+    S.PL = h->s_PL;
+    S.AV = h->s_AV;
+    S.dudt = h->s_dudt;
+    S.couple = h->s_couple;
+    S.fposr = h->f_posr[h->f_cur];
+    S.fvelp = h->f_velp[h->f_cur];
+    S.start_f = h->f_start;
+    S.n = h->ns;
+    return S;
+}
+
+fsim_status enqueue_solid(fsim_sim *h)
+{
+    if (!h->ns) return FSIM_OK;
+    const SolidArgs S = solid_args(h);
+    const int g = blocks_for(h->ns, kBlock);
+    for (int k = 0; k < h->cfg.solid_sub_step; ++k) {
+        k_solid_deform<<<g, kBlock, 0, h->stream>>>(h->P, S);
+        CK_LAUNCH();
+        k_solid_force<<<g, kBlock, 0, h->stream>>>(h->P, S);
+        CK_LAUNCH();
+        k_solid_update<<<g, kBlock, 0, h->stream>>>(h->P, S);
+        CK_LAUNCH();
+        h->launches += 3;
+    }
+    h->s_mech_ok = true;
+    return FSIM_OK;
+}
+
+// DeviceCalculation::calculation loop body (src/calculation.cu:23-33)
+fsim_status enqueue_step(fsim_sim *h)
+{
+    fsim_status st;
+    if ((st = enqueue_cell_phase(h))) return st;
+    if ((st = enqueue_couple(h))) return st;
+    if ((st = enqueue_virt(h))) return st;
+    if ((st = enqueue_fluid(h))) return st;
+    if ((st = enqueue_solid(h))) return st;
+    return FSIM_OK;
+}
+
+fsim_status run_step_graph(fsim_sim *h)
+{
+    GraphEntry &g = h->graphs[h->f_cur][h->s_cur];
+    if (!g.exec) {
+        const int f0 = h->f_cur, s0 = h->s_cur;
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        h->launches = 0;
+        fsim_status st = enqueue_step(h);
+        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        if (st) {
+            if (graph) cudaGraphDestroy(graph);
+            h->f_cur = f0;
+            h->s_cur = s0;
+            return st;
+        }
+        if (e != cudaSuccess) {
+            fsim_set_error("stream capture failed: %s", cudaGetErrorString(e));
+            h->f_cur = f0;
+            h->s_cur = s0;
+            return FSIM_ECUDA;
+        }
+        e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            g.exec = nullptr;
+            fsim_set_error("graph instantiate failed: %s", cudaGetErrorString(e));
+            h->f_cur = f0;
+            h->s_cur = s0;
+            return FSIM_ECUDA;
+        }
+        g.f_after = h->f_cur;
+        g.s_after = h->s_cur;
+        h->f_cur = f0;
+        h->s_cur = s0;
+    }
+    CK(cudaGraphLaunch(g.exec, h->stream));
+    h->f_cur = g.f_after;
+    h->s_cur = g.s_after;
+    h->f_sorted = h->s_sorted = true;
+    h->f_deriv_ok = h->keep && h->nf > 0;
+    h->s_np_ok = h->ns > 0 && h->nf > 0;
+    h->s_mech_ok = h->ns > 0;
+    return FSIM_OK;
+}
+
+fsim_status check_flags(fsim_sim *h)
+{
+    unsigned flags = 0;
+    CK(cudaMemcpyAsync(&flags, h->d_flags, sizeof flags, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (flags & FLAG_OUT_OF_GRID) {
+        fsim_set_error("a particle position fell outside the cell grid (clamped)");
+        CK(cudaMemsetAsync(h->d_flags, 0, sizeof(unsigned), h->stream));
+        return FSIM_ENUMERIC;
+    }
+    return FSIM_OK;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+// counting-sort the virtual particles once (walls are static)
+fsim_status sort_virtual(fsim_sim *h, const float *vpos_host)
+{
+    const int n = h->nv;
+    float *d_xyz = nullptr;
+    float4 *tmp_pos = nullptr;
+    int *key = nullptr, *slot = nullptr, *tmp = nullptr, *cnt = nullptr, *orig0 = nullptr;
+    fsim_status st;
+    if ((st = dalloc(h, &d_xyz, 3 * (size_t)n)) || (st = dalloc(h, &tmp_pos, n)) || (st = dalloc(h, &key, n)) ||
+        (st = dalloc(h, &slot, n)) || (st = dalloc(h, &tmp, n)) || (st = dalloc(h, &cnt, h->ncell)) ||
+        (st = dalloc(h, &orig0, n)))
+        return st;
+    CK(cudaMemcpyAsync(d_xyz, vpos_host, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+    k_pack_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(d_xyz, nullptr, n, h->P.rho0, tmp_pos);
+    k_iota<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(orig0, n);
+    CK(cudaMemsetAsync(cnt, 0, sizeof(int) * h->ncell, h->stream));
+    k_hash<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(h->P, tmp_pos, n, key, slot, cnt, h->d_flags);
+    CK_LAUNCH();
+    if ((st = enqueue_scan(h, cnt, h->v_start, nullptr, nullptr))) return st;
+    k_scatter<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(key, slot, h->v_start, tmp, n);
+    // reuse the fluid gather (posr) with a dummy velocity stream
+    k_gather_fluid<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(tmp, key, h->v_start, n, tmp_pos, tmp_pos, orig0,
+                                                                     h->v_posr, h->v_velp, h->v_orig, h->v_cell);
+    CK_LAUNCH();
+    CK(cudaMemsetAsync(h->v_velp, 0, sizeof(float4) * n, h->stream));
+    k_virt_normal<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(h->P, h->v_posr, h->v_cell, h->v_start,
+                                                                    h->v_normal, n);
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(h->stream));
+    // temporaries are released now
+    void *tmps[] = {d_xyz, tmp_pos, key, slot, tmp, cnt, orig0};
+    for (void *p : tmps) {
+        cudaFree(p);
+        for (auto it = h->allocations.begin(); it != h->allocations.end(); ++it)
+            if (*it == p) {
+                h->allocations.erase(it);
+                break;
+            }
+    }
+    return FSIM_OK;
+}
+
+fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
+{
+    const int nf = p->n_fluid, ns = p->n_solid, nv = p->n_virt, nc = h->ncell;
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&h->ev0));
+    CK(cudaEventCreate(&h->ev1));
+    fsim_status st;
+    if ((st = dalloc(h, &h->d_flags, 1))) return st;
+    if ((st = dalloc(h, &h->scan_partials, 2 * kMaxScanTiles))) return st;
+    CK(cudaMemsetAsync(h->d_flags, 0, sizeof(unsigned), h->stream));
+    // fluid
+    for (int b = 0; b < 2; ++b) {
+        if ((st = dalloc(h, &h->f_posr[b], nf)) || (st = dalloc(h, &h->f_velp[b], nf)) ||
+            (st = dalloc(h, &h->f_orig[b], nf)))
+            return st;
+    }
+    if ((st = dalloc(h, &h->f_cell, nf)) || (st = dalloc(h, &h->f_key, nf)) || (st = dalloc(h, &h->f_slot, nf)) ||
+        (st = dalloc(h, &h->f_tmp, nf)) || (st = dalloc(h, &h->f_cnt, nc)) || (st = dalloc(h, &h->f_start, nc + 1)))
+        return st;
+    if (h->keep && ((st = dalloc(h, &h->f_drho, nf)) || (st = dalloc(h, &h->f_dudt, nf)))) return st;
+    // solid
+    for (int b = 0; b < 2; ++b) {
+        if ((st = dalloc(h, &h->s_pos[b], ns)) || (st = dalloc(h, &h->s_vel[b], ns)) ||
+            (st = dalloc(h, &h->s_ref[b], ns)) || (st = dalloc(h, &h->s_type[b], ns)) ||
+            (st = dalloc(h, &h->s_orig[b], ns)))
+            return st;
+    }
+    if ((st = dalloc(h, &h->s_cell, ns)) || (st = dalloc(h, &h->s_key, ns)) || (st = dalloc(h, &h->s_slot, ns)) ||
+        (st = dalloc(h, &h->s_tmp, ns)) || (st = dalloc(h, &h->s_cnt, nc)) || (st = dalloc(h, &h->s_start, nc + 1)) ||
+        (st = dalloc(h, &h->s_np, ns)) || (st = dalloc(h, &h->s_dudt, ns)) || (st = dalloc(h, &h->s_couple, ns)) ||
+        (st = dalloc(h, &h->s_F, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_P, 9 * (size_t)ns)) ||
+        (st = dalloc(h, &h->s_L, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_PL, 9 * (size_t)ns)) ||
+        (st = dalloc(h, &h->s_AV, 9 * (size_t)ns)))
+        return st;
+    // virtual
+    if ((st = dalloc(h, &h->v_posr, nv)) || (st = dalloc(h, &h->v_velp, nv)) || (st = dalloc(h, &h->v_normal, nv)) ||
+        (st = dalloc(h, &h->v_orig, nv)) || (st = dalloc(h, &h->v_cell, nv)) || (st = dalloc(h, &h->v_start, nc + 1)))
+        return st;
+    // staging for field copies (input order)
+    size_t words = 3 * (size_t)nf;
+    if (9 * (size_t)ns > words) words = 9 * (size_t)ns;
+    if (3 * (size_t)nv > words) words = 3 * (size_t)nv;
+    h->staging_bytes = 4 * (words ? words : 1);
+    if ((st = dalloc(h, (char **)&h->staging, h->staging_bytes))) return st;
+
+    // empty cell structures are valid before the first cell phase
+    CK(cudaMemsetAsync(h->f_start, 0, sizeof(int) * (nc + 1), h->stream));
+    CK(cudaMemsetAsync(h->s_start, 0, sizeof(int) * (nc + 1), h->stream));
+    CK(cudaMemsetAsync(h->v_start, 0, sizeof(int) * (nc + 1), h->stream));
+    CK(cudaMemsetAsync(h->s_np, 0, sizeof(float4) * (ns ? ns : 1), h->stream));
+
+    float *stg = (float *)h->staging;
+    if (nf) {
+        CK(cudaMemcpyAsync(stg, p->fluid_pos, sizeof(float) * 3 * nf, cudaMemcpyHostToDevice, h->stream));
+        float *d_rho = nullptr;
+        if ((st = dalloc(h, &d_rho, nf))) return st;
+        CK(cudaMemcpyAsync(d_rho, p->fluid_rho, sizeof(float) * nf, cudaMemcpyHostToDevice, h->stream));
+        k_pack_f4<<<blocks_for(nf, kBlock), kBlock, 0, h->stream>>>(stg, d_rho, nf, 0.0f, h->f_posr[0]);
+        CK(cudaMemcpyAsync(d_rho, p->fluid_p, sizeof(float) * nf, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        CK(cudaMemcpyAsync(stg, p->fluid_vel, sizeof(float) * 3 * nf, cudaMemcpyHostToDevice, h->stream));
+        k_pack_f4<<<blocks_for(nf, kBlock), kBlock, 0, h->stream>>>(stg, d_rho, nf, 0.0f, h->f_velp[0]);
+        k_iota<<<blocks_for(nf, kBlock), kBlock, 0, h->stream>>>(h->f_orig[0], nf);
+        CK_LAUNCH();
+        CK(cudaStreamSynchronize(h->stream));
+        cudaFree(d_rho);
+        h->allocations.pop_back();
+    }
+    if (ns) {
+        CK(cudaMemcpyAsync(stg, p->solid_pos, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice, h->stream));
+        k_pack_f4<<<blocks_for(ns, kBlock), kBlock, 0, h->stream>>>(stg, nullptr, ns, 0.0f, h->s_pos[0]);
+        CK(cudaStreamSynchronize(h->stream));
+        CK(cudaMemcpyAsync(stg, p->solid_vel, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice, h->stream));
+        k_pack_f4<<<blocks_for(ns, kBlock), kBlock, 0, h->stream>>>(stg, nullptr, ns, 0.0f, h->s_vel[0]);
+        CK(cudaStreamSynchronize(h->stream));
+        CK(cudaMemcpyAsync(stg, p->solid_ref_pos, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice, h->stream));
+        k_pack_f4<<<blocks_for(ns, kBlock), kBlock, 0, h->stream>>>(stg, nullptr, ns, 0.0f, h->s_ref[0]);
+        CK(cudaMemcpyAsync(h->s_type[0], p->solid_type, sizeof(int) * ns, cudaMemcpyHostToDevice, h->stream));
+        k_iota<<<blocks_for(ns, kBlock), kBlock, 0, h->stream>>>(h->s_orig[0], ns);
+        CK_LAUNCH();
+        CK(cudaStreamSynchronize(h->stream));
+        // F = L = I, P = 0 until the first solid phase (include/host_data.cuh:95-97)
+        std::vector<float> eye(9 * (size_t)ns, 0.0f);
+        for (int i = 0; i < ns; ++i) eye[9 * i] = eye[9 * i + 4] = eye[9 * i + 8] = 1.0f;
+        CK(cudaMemcpy(h->s_F, eye.data(), sizeof(float) * 9 * ns, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->s_L, eye.data(), sizeof(float) * 9 * ns, cudaMemcpyHostToDevice));
+        CK(cudaMemset(h->s_P, 0, sizeof(float) * 9 * ns));
+        CK(cudaMemset(h->s_dudt, 0, sizeof(float4) * ns));
+        CK(cudaMemset(h->s_couple, 0, sizeof(float4) * ns));
+        h->s_mech_ok = true; // initial values, in input order (= s_orig[0])
+        h->s_np_ok = true;
+    }
+    if (nv && (st = sort_virtual(h, p->virt_pos))) return st;
+    CK(cudaStreamSynchronize(h->stream));
+    return check_flags(h);
+}
+
+} // namespace
+
+// =================================================================== C ABI
+extern "C" fsim_status fsim_create(const fsim_config *cfg, const fsim_particles *p, int device, fsim_handle *out)
+{
+    if (!cfg || !p || !out) return FSIM_EINVAL;
+    *out = nullptr;
+    if (p->n_fluid < 0 || p->n_solid < 0 || p->n_virt < 0 || (p->n_fluid && (!p->fluid_pos || !p->fluid_vel ||
+                                                                             !p->fluid_rho || !p->fluid_p)) ||
+        (p->n_solid && (!p->solid_pos || !p->solid_vel || !p->solid_ref_pos || !p->solid_type)) ||
+        (p->n_virt && !p->virt_pos)) {
+        fsim_set_error("invalid particle arrays");
+        return FSIM_EINVAL;
+    }
+    if (cfg->solid_sub_step < 1 || !(cfg->dt > 0.0f)) {
+        fsim_set_error("dt must be > 0 and solid_sub_step >= 1");
+        return FSIM_EINVAL;
+    }
+    auto *h = new (std::nothrow) fsim_sim;
+    if (!h) return FSIM_ENOMEM;
+    h->cfg = *cfg;
+    fsim_status st = fsim_derive(cfg, &h->der);
+    if (st) {
+        delete h;
+        return st;
+    }
+    if (blocks_for(h->der.cell_number_total, kScanTile) > kMaxScanTiles) {
+        fsim_set_error("cell grid of %d cells exceeds the supported %d", h->der.cell_number_total,
+                       kMaxScanTiles * kScanTile);
+        delete h;
+        return FSIM_EINVAL;
+    }
+    if (device < 0) {
+        if (cudaGetDevice(&device) != cudaSuccess) {
+            fsim_set_error("no CUDA device");
+            delete h;
+            return FSIM_ECUDA;
+        }
+    }
+    h->device = device;
+    DeviceGuard guard(device);
+    fill_params(h);
+    h->nf = p->n_fluid;
+    h->ns = p->n_solid;
+    h->nv = p->n_virt;
+    h->ncell = h->der.cell_number_total;
+    h->keep = cfg->keep_derivatives != 0;
+    st = create_impl(h, p);
+    if (st) {
+        free_all(h);
+        delete h;
+        return st;
+    }
+    *out = h;
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_destroy(fsim_handle h)
+{
+    if (!h) return FSIM_OK;
+    DeviceGuard guard(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_step(fsim_handle h, int nsteps)
+{
+    if (!h || nsteps < 0) return FSIM_EINVAL;
+    DeviceGuard guard(h->device);
+    for (int k = 0; k < nsteps; ++k) {
+        fsim_status st = run_step_graph(h);
+        if (st) return st;
+    }
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_sync(fsim_handle h)
+{
+    if (!h) return FSIM_EINVAL;
+    DeviceGuard guard(h->device);
+    CK(cudaStreamSynchronize(h->stream));
+    return check_flags(h);
+}
+
+extern "C" fsim_status fsim_run_phase(fsim_handle h, int phase)
+{
+    if (!h) return FSIM_EINVAL;
+    DeviceGuard guard(h->device);
+    h->launches = 0;
+    switch (phase) {
+    case FSIM_PHASE_CELL: return enqueue_cell_phase(h);
+    case FSIM_PHASE_COUPLE:
+    case FSIM_PHASE_VIRT:
+    case FSIM_PHASE_FLUID:
+    case FSIM_PHASE_SOLID:
+        if (!h->f_sorted || !h->s_sorted) {
+            fsim_set_error("run FSIM_PHASE_CELL first");
+            return FSIM_EINVAL;
+        }
+        if (phase == FSIM_PHASE_COUPLE) return enqueue_couple(h);
+        if (phase == FSIM_PHASE_VIRT) return enqueue_virt(h);
+        if (phase == FSIM_PHASE_FLUID) return enqueue_fluid(h);
+        return enqueue_solid(h);
+    default: fsim_set_error("unknown phase %d", phase); return FSIM_EINVAL;
+    }
+}
+
+extern "C" int fsim_field_width(int field)
+{
+    switch (field) {
+    case FSIM_FLUID_POS: case FSIM_FLUID_VEL: case FSIM_FLUID_DU_DT:
+    case FSIM_SOLID_POS: case FSIM_SOLID_VEL: case FSIM_SOLID_REF_POS: case FSIM_SOLID_NORMAL:
+    case FSIM_SOLID_DU_DT: case FSIM_SOLID_COUPLE_DUDT:
+    case FSIM_VIRT_POS: case FSIM_VIRT_NORMAL: case FSIM_VIRT_VEL:
+        return 3;
+    case FSIM_FLUID_RHO: case FSIM_FLUID_P: case FSIM_FLUID_DRHO_DT: case FSIM_FLUID_CELL_ID:
+    case FSIM_SOLID_TYPE: case FSIM_SOLID_P: case FSIM_SOLID_CELL_ID:
+    case FSIM_VIRT_P: case FSIM_VIRT_RHO: case FSIM_VIRT_CELL_ID:
+        return 1;
+    case FSIM_SOLID_F: case FSIM_SOLID_PK1: case FSIM_SOLID_LINV:
+        return 9;
+    default: return 0;
+    }
+}
+
+static int field_count(fsim_sim *h, int field)
+{
+    if (field < 10) return h->nf;
+    if (field < 30) return h->ns;
+    return h->nv;
+}
+
+extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_t bytes)
+{
+    if (!h || (!dst && bytes)) return FSIM_EINVAL;
+    const int width = fsim_field_width(field);
+    if (!width) {
+        fsim_set_error("unknown field %d", field);
+        return FSIM_EINVAL;
+    }
+    const int n = field_count(h, field);
+    if (bytes != (size_t)n * width * 4) {
+        fsim_set_error("field %d needs %zu bytes, got %zu", field, (size_t)n * width * 4, bytes);
+        return FSIM_EINVAL;
+    }
+    if (n == 0) return FSIM_OK;
+    DeviceGuard guard(h->device);
+    const int g = blocks_for(n, kBlock);
+    float *stg = (float *)h->staging;
+    const int *forig = h->f_orig[h->f_cur];
+    const int *sorig = h->s_orig[h->s_cur];
+    switch (field) {
+    case FSIM_FLUID_POS: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->f_posr[h->f_cur], forig, n, 0, 3, stg); break;
+    case FSIM_FLUID_RHO: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->f_posr[h->f_cur], forig, n, 3, 1, stg); break;
+    case FSIM_FLUID_VEL: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->f_velp[h->f_cur], forig, n, 0, 3, stg); break;
+    case FSIM_FLUID_P: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->f_velp[h->f_cur], forig, n, 3, 1, stg); break;
+    case FSIM_FLUID_DRHO_DT:
+    case FSIM_FLUID_DU_DT:
+        if (!h->f_deriv_ok) {
+            fsim_set_error("derivatives unavailable (set keep_derivatives and run the fluid phase)");
+            return FSIM_EINVAL;
+        }
+        if (field == FSIM_FLUID_DU_DT)
+            k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->f_dudt, forig, n, 0, 3, stg);
+        else
+            k_unpermute_words<<<g, kBlock, 0, h->stream>>>((const int *)h->f_drho, forig, n, 1, (int *)stg);
+        break;
+    case FSIM_FLUID_CELL_ID:
+        if (!h->f_sorted) {
+            fsim_set_error("cell ids unavailable before the first cell phase");
+            return FSIM_EINVAL;
+        }
+        k_unpermute_words<<<g, kBlock, 0, h->stream>>>(h->f_cell, forig, n, 1, (int *)stg);
+        break;
+    case FSIM_SOLID_POS: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->s_pos[h->s_cur], sorig, n, 0, 3, stg); break;
+    case FSIM_SOLID_VEL: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->s_vel[h->s_cur], sorig, n, 0, 3, stg); break;
+    case FSIM_SOLID_REF_POS:
+        k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->s_ref[h->s_cur], sorig, n, 0, 3, stg);
+        break;
+    case FSIM_SOLID_TYPE:
+        k_unpermute_words<<<g, kBlock, 0, h->stream>>>(h->s_type[h->s_cur], sorig, n, 1, (int *)stg);
+        break;
+    case FSIM_SOLID_CELL_ID:
+        if (!h->s_sorted) {
+            fsim_set_error("cell ids unavailable before the first cell phase");
+            return FSIM_EINVAL;
+        }
+        k_unpermute_words<<<g, kBlock, 0, h->stream>>>(h->s_cell, sorig, n, 1, (int *)stg);
+        break;
+    case FSIM_SOLID_NORMAL:
+    case FSIM_SOLID_P:
+        if (!h->s_np_ok) {
+            fsim_set_error("solid normal/pressure are stale after a cell phase; run the coupling phase first");
+            return FSIM_EINVAL;
+        }
+        if (field == FSIM_SOLID_NORMAL) k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->s_np, sorig, n, 0, 3, stg);
+        else k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->s_np, sorig, n, 3, 1, stg);
+        break;
+    case FSIM_SOLID_DU_DT:
+    case FSIM_SOLID_COUPLE_DUDT:
+    case FSIM_SOLID_F:
+    case FSIM_SOLID_PK1:
+    case FSIM_SOLID_LINV:
+        if (!h->s_mech_ok) {
+            fsim_set_error("solid stress products are stale after a cell phase; run the solid phase first");
+            return FSIM_EINVAL;
+        }
+        if (field == FSIM_SOLID_DU_DT) k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->s_dudt, sorig, n, 0, 3, stg);
+        else if (field == FSIM_SOLID_COUPLE_DUDT)
+            k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->s_couple, sorig, n, 0, 3, stg);
+        else {
+            const float *src = field == FSIM_SOLID_F ? h->s_F : field == FSIM_SOLID_PK1 ? h->s_P : h->s_L;
+            k_unpermute_words<<<g, kBlock, 0, h->stream>>>((const int *)src, sorig, n, 9, (int *)stg);
+        }
+        break;
+    case FSIM_VIRT_POS: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->v_posr, h->v_orig, n, 0, 3, stg); break;
+    case FSIM_VIRT_RHO: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->v_posr, h->v_orig, n, 3, 1, stg); break;
+    case FSIM_VIRT_VEL: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->v_velp, h->v_orig, n, 0, 3, stg); break;
+    case FSIM_VIRT_P: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->v_velp, h->v_orig, n, 3, 1, stg); break;
+    case FSIM_VIRT_NORMAL: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->v_normal, h->v_orig, n, 0, 3, stg); break;
+    case FSIM_VIRT_CELL_ID:
+        k_unpermute_words<<<g, kBlock, 0, h->stream>>>(h->v_cell, h->v_orig, n, 1, (int *)stg);
+        break;
+    default: return FSIM_EINVAL;
+    }
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(dst, stg, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src, size_t bytes)
+{
+    if (!h || (!src && bytes)) return FSIM_EINVAL;
+    const int width = fsim_field_width(field);
+    const int n = field_count(h, field);
+    float4 *dst = nullptr;
+    const int *orig = nullptr;
+    int comp = 0;
+    switch (field) {
+    case FSIM_FLUID_POS: dst = h->f_posr[h->f_cur]; comp = 0; break;
+    case FSIM_FLUID_RHO: dst = h->f_posr[h->f_cur]; comp = 3; break;
+    case FSIM_FLUID_VEL: dst = h->f_velp[h->f_cur]; comp = 0; break;
+    case FSIM_FLUID_P: dst = h->f_velp[h->f_cur]; comp = 3; break;
+    case FSIM_SOLID_POS: dst = h->s_pos[h->s_cur]; comp = 0; break;
+    case FSIM_SOLID_VEL: dst = h->s_vel[h->s_cur]; comp = 0; break;
+    default: fsim_set_error("field %d is not settable", field); return FSIM_EINVAL;
+    }
+    orig = field < 10 ? h->f_orig[h->f_cur] : h->s_orig[h->s_cur];
+    if (bytes != (size_t)n * width * 4) {
+        fsim_set_error("field %d needs %zu bytes, got %zu", field, (size_t)n * width * 4, bytes);
+        return FSIM_EINVAL;
+    }
+    if (n == 0) return FSIM_OK;
+    DeviceGuard guard(h->device);
+    CK(cudaMemcpyAsync(h->staging, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    k_permute_in_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(dst, orig, n, comp, width,
+                                                                      (const float *)h->staging);
+    CK_LAUNCH();
+    // positions changed: derived per-step products are stale until the next phases
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_neighbor_counts(fsim_handle h, int *out, size_t bytes)
+{
+    if (!h || (!out && bytes)) return FSIM_EINVAL;
+    if (bytes != (size_t)h->nf * 3 * 4) {
+        fsim_set_error("neighbor counts need %zu bytes", (size_t)h->nf * 12);
+        return FSIM_EINVAL;
+    }
+    if (!h->f_sorted) {
+        fsim_set_error("run FSIM_PHASE_CELL first");
+        return FSIM_EINVAL;
+    }
+    if (!h->nf) return FSIM_OK;
+    DeviceGuard guard(h->device);
+    int *d_counts = (int *)h->staging; // 3 * nf words fit the staging buffer
+    const int g = blocks_for(h->nf, kBlock);
+    k_neighbor_counts<<<g, kBlock, 0, h->stream>>>(h->P, h->f_posr[h->f_cur], h->f_cell, h->f_start,
+                                                    h->s_pos[h->s_cur], h->s_start, h->v_posr, h->v_start, d_counts,
+                                                    h->nf);
+    CK_LAUNCH();
+    // reorder to input order in place is not possible; copy sorted and unpermute on the host
+    std::vector<int> sorted(3 * (size_t)h->nf), orig(h->nf);
+    CK(cudaMemcpyAsync(sorted.data(), d_counts, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(orig.data(), h->f_orig[h->f_cur], sizeof(int) * h->nf, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int s = 0; s < h->nf; ++s)
+        for (int k = 0; k < 3; ++k) out[3 * orig[s] + k] = sorted[3 * s + k];
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_get_cells(fsim_handle h, int species, int *cell_start, size_t start_bytes, int *ids,
+                                      size_t ids_bytes)
+{
+    if (!h || species < 0 || species > 2) return FSIM_EINVAL;
+    const int n = species == 0 ? h->nf : species == 1 ? h->ns : h->nv;
+    if (start_bytes != (size_t)(h->ncell + 1) * 4 || ids_bytes != (size_t)n * 4 || !cell_start || (n && !ids)) {
+        fsim_set_error("fsim_get_cells: wrong buffer sizes");
+        return FSIM_EINVAL;
+    }
+    if ((species == 0 && !h->f_sorted) || (species == 1 && !h->s_sorted)) {
+        fsim_set_error("run FSIM_PHASE_CELL first");
+        return FSIM_EINVAL;
+    }
+    DeviceGuard guard(h->device);
+    const int *start = species == 0 ? h->f_start : species == 1 ? h->s_start : h->v_start;
+    const int *orig = species == 0 ? h->f_orig[h->f_cur] : species == 1 ? h->s_orig[h->s_cur] : h->v_orig;
+    CK(cudaMemcpyAsync(cell_start, start, start_bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (n) CK(cudaMemcpyAsync(ids, orig, ids_bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_write_vtk(fsim_handle h, const char *out_dir, int file_step)
+{
+    if (!h || !out_dir) return FSIM_EINVAL;
+    std::vector<float> fpos(3 * (size_t)h->nf), fvel(3 * (size_t)h->nf), frho(h->nf), fp(h->nf);
+    std::vector<float> spos(3 * (size_t)h->ns), svel(3 * (size_t)h->ns), sp(h->ns), snormal(3 * (size_t)h->ns);
+    std::vector<float> vpos(3 * (size_t)h->nv), vnormal(3 * (size_t)h->nv), vp(h->nv);
+    fsim_status st;
+    if ((st = fsim_get_field(h, FSIM_FLUID_POS, fpos.data(), fpos.size() * 4)) ||
+        (st = fsim_get_field(h, FSIM_FLUID_VEL, fvel.data(), fvel.size() * 4)) ||
+        (st = fsim_get_field(h, FSIM_FLUID_RHO, frho.data(), frho.size() * 4)) ||
+        (st = fsim_get_field(h, FSIM_FLUID_P, fp.data(), fp.size() * 4)) ||
+        (st = fsim_get_field(h, FSIM_SOLID_POS, spos.data(), spos.size() * 4)) ||
+        (st = fsim_get_field(h, FSIM_SOLID_VEL, svel.data(), svel.size() * 4)) ||
+        (st = fsim_get_field(h, FSIM_VIRT_POS, vpos.data(), vpos.size() * 4)) ||
+        (st = fsim_get_field(h, FSIM_VIRT_NORMAL, vnormal.data(), vnormal.size() * 4)) ||
+        (st = fsim_get_field(h, FSIM_VIRT_P, vp.data(), vp.size() * 4)))
+        return st;
+    if (h->ns && h->s_np_ok) {
+        if ((st = fsim_get_field(h, FSIM_SOLID_P, sp.data(), sp.size() * 4)) ||
+            (st = fsim_get_field(h, FSIM_SOLID_NORMAL, snormal.data(), snormal.size() * 4)))
+            return st;
+    }
+    VtkHostState vs;
+    vs.n_fluid = h->nf;
+    vs.n_solid = h->ns;
+    vs.n_virt = h->nv;
+    vs.fpos = fpos.data();
+    vs.fvel = fvel.data();
+    vs.frho = frho.data();
+    vs.fp = fp.data();
+    vs.spos = spos.data();
+    vs.svel = svel.data();
+    vs.sp = sp.data();
+    vs.snormal = snormal.data();
+    vs.solid_density = h->cfg.solid_density;
+    vs.vpos = vpos.data();
+    vs.vnormal = vnormal.data();
+    vs.vp = vp.data();
+    return fsim_write_vtk_host(out_dir, file_step, vs);
+}
+
+extern "C" fsim_status fsim_time_steps(fsim_handle h, int nsteps, float *ms)
+{
+    if (!h || nsteps < 0 || !ms) return FSIM_EINVAL;
+    DeviceGuard guard(h->device);
+    // capture outside the timed region
+    fsim_status st;
+    CK(cudaEventRecord(h->ev0, h->stream));
+    for (int k = 0; k < nsteps; ++k)
+        if ((st = run_step_graph(h))) return st;
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaEventSynchronize(h->ev1));
+    CK(cudaEventElapsedTime(ms, h->ev0, h->ev1));
+    return check_flags(h);
+}
+
+extern "C" fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_ms, float *sweep_ms)
+{
+    if (!h || nsteps < 0 || !total_ms || !sweep_ms) return FSIM_EINVAL;
+    DeviceGuard guard(h->device);
+    while ((int)h->sweep_events.size() < 2 * nsteps) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        h->sweep_events.push_back(e);
+    }
+    fsim_status st = FSIM_OK;
+    CK(cudaEventRecord(h->ev0, h->stream));
+    h->instrument = true;
+    for (int k = 0; k < nsteps && !st; ++k) {
+        h->instr_step = k;
+        h->launches = 0;
+        st = enqueue_step(h);
+    }
+    h->instrument = false;
+    if (st) return st;
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaEventSynchronize(h->ev1));
+    CK(cudaEventElapsedTime(total_ms, h->ev0, h->ev1));
+    float sum = 0.0f;
+    if (h->nf) {
+        for (int k = 0; k < nsteps; ++k) {
+            float t = 0.0f;
+            CK(cudaEventElapsedTime(&t, h->sweep_events[2 * k], h->sweep_events[2 * k + 1]));
+            sum += t;
+        }
+    }
+    *sweep_ms = sum;
+    return check_flags(h);
+}
+
+extern "C" fsim_status fsim_launches_per_step(fsim_handle h, int *n)
+{
+    if (!h || !n) return FSIM_EINVAL;
+    // count by enqueuing nothing: the formula mirrors enqueue_step
+    int c = 0;
+    if (h->nf) c += 1 + 2;                  // hash, scatter, gather
+    if (h->ns) c += 1 + 2;
+    if (h->nf || h->ns) c += 3;             // scan
+    if (h->nf && h->ns) c += 1;             // couple
+    if (h->nv) c += 1;                      // virtual
+    if (h->nf) c += 1;                      // fluid sweep
+    if (h->ns) c += 3 * h->cfg.solid_sub_step;
+    *n = c;
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_counts(fsim_handle h, int *nf, int *ns, int *nv)
+{
+    if (!h) return FSIM_EINVAL;
+    if (nf) *nf = h->nf;
+    if (ns) *ns = h->ns;
+    if (nv) *nv = h->nv;
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_get_derived(fsim_handle h, fsim_derived *out)
+{
+    if (!h || !out) return FSIM_EINVAL;
+    *out = h->der;
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_host_alloc(size_t bytes, void **out)
+{
+    if (!out) return FSIM_EINVAL;
+    *out = nullptr;
+    cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fsim_set_error("cudaMallocHost(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        return FSIM_ENOMEM;
+    }
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_host_free(void *p)
+{
+    if (p) cudaFreeHost(p);
+    return FSIM_OK;
+}

@@ -1,0 +1,253 @@
+/*
+ * fluidsim.h — C ABI of the GB300-native FluidSim particle hot path.
+ *
+ * The reference (niji127/FluidSim) is one Windows executable with no library
+ * API.  Its hot path sits behind two seams, and every entry point below names
+ * the reference piece it replaces:
+ *   - the process contract: config/input.ini + data/{fluid,solid,virt}_particle.dat
+ *     in, out/{fluid,solid,virtual}/ *-k.vtk out
+ *     (src/parameter.cpp:36-63, src/sim.cu:40-151, src/output.cu:299-335);
+ *   - the static phase functions DeviceCalculation::{particleCellUpdate, fillCell,
+ *     coupleCalculation, virtUpdate, fluidCalculation, solidCalculation}
+ *     (include/calculation.cuh:9-21) driven by DeviceCalculation::calculation
+ *     (src/calculation.cu:20-35).
+ *
+ * Conventions
+ *   - Plain C types only: pointers, sizes, ints, floats.  No CUDA or torch types.
+ *   - Every call returns an fsim_status; nothing calls exit(), abort() or __trap().
+ *   - A handle owns its device state and one CUDA stream.  Handles are independent
+ *     (no globals); one handle is not thread-safe, different handles may run on
+ *     different host threads at once.
+ *   - Vectors are 3 consecutive floats (x, y, z).  3x3 matrices are 9 floats in
+ *     row-major order: element (r, c) at index 3*r + c.
+ *   - Per-particle fields are read and written in the ORIGINAL input order (the
+ *     order of the rows of the .dat files), although the device keeps particles
+ *     sorted by cell.
+ *   - The vertical axis is y and gravity points along -y (src/physics.cpp:12-15).
+ */
+#ifndef FLUIDSIM_H
+#define FLUIDSIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef int fsim_status;
+enum {
+    FSIM_OK = 0,
+    FSIM_EINVAL = 1,    /* bad argument, bad config, malformed input file      */
+    FSIM_ENOMEM = 2,    /* device or host allocation failed                    */
+    FSIM_ECUDA = 3,     /* a CUDA runtime call failed                          */
+    FSIM_ETIMEOUT = 4,  /* a bounded device-side wait gave up                  */
+    FSIM_ENUMERIC = 5,  /* the device raised a numeric/out-of-grid flag        */
+    FSIM_EIO = 6        /* file could not be opened, read or written           */
+};
+
+/* Human-readable name of a status code (static string, never NULL). */
+const char *fsim_status_string(fsim_status s);
+/* Last error message recorded on this host thread (static per thread). */
+const char *fsim_last_error(void);
+
+/* ------------------------------------------------------------------ config */
+/* Precision forms (an extension; the reference is FP32 only). */
+enum { FSIM_PRECISION_FP32 = 0, FSIM_PRECISION_MIXED = 1 };
+
+/* Every key the reference reads from input.ini, with the same meaning.
+ * Replaces Physics/FluidProperties/SolidProperties/Domain/SimTime/Kernel::
+ * readParameter (src/physics.cpp:9-19, src/properties.cpp:34-43,95-104,
+ * src/domain.cpp:9-26, src/sim_time.cpp:8-24, src/kernel.cpp:9-23). */
+typedef struct fsim_config {
+    /* [physics] */
+    float gravity;                  /* magnitude, applied along -y          */
+    /* [fluid] */
+    int   is_viscid;
+    float min_pressure, fluid_sound_speed, fluid_density, gamma, viscosity;
+    /* [solid] */
+    float solid_density, youngs_modulus, poisson_ratio, arti_vis_alpha, arti_vis_beta;
+    /* [domain] */
+    float xmin, ymin, zmin, xmax, ymax, zmax;
+    /* [time] */
+    float dt;
+    int   istart, iend, solid_sub_step, result_interval, sort_every_step;
+    /* [kernel] */
+    float smoothing_length, particle_diameter, impact_length_hsml_ratio;
+    int   thread_num;
+    /* extension keys (a [gb300] section the reference ignores) */
+    int   precision;                /* FSIM_PRECISION_*                       */
+    int   keep_derivatives;         /* 1: keep drho_dt/du_dt readable         */
+} fsim_config;
+
+/* Derived constants, as Parameter::initiateParameter computes them in FP32
+ * (src/parameter.cpp:25-34 -> src/kernel.cpp:43-60, src/properties.cpp:47-66,
+ * src/domain.cpp:28-47). */
+typedef struct fsim_derived {
+    float smoothing_length_square, smoothing_length_inverse, smoothing_length_inverse_square;
+    float impact_distance_square, particle_volume;
+    float kernel_coefficient_1, kernel_coefficient_2, kernel_differential;
+    float coefficient_p2rho, coefficient_rho2p, gamma_inv, reference_density_inverse;
+    float min_density, max_density;
+    float lambda, shear_modulus, bulk_modulus, solid_sound_speed;
+    float gravity_vec[3];
+    float cell_min[3], cell_max[3], interval[3], interval_inv[3];
+    int   cell_number[3];
+    int   cell_number_total;
+} fsim_derived;
+
+/* Fill *cfg with the reference defaults (keys absent from an INI file). */
+fsim_status fsim_config_defaults(fsim_config *cfg);
+/* Parse an input.ini file / text with the reference's Config semantics
+ * (src/config.cpp:59-129: '#' comments, '[section]' lines ignored, values
+ * continued on following key-less lines, the last duplicate key wins) and
+ * apply the reference defaults.  Replaces Parameter::readFieldParameter
+ * (src/parameter.cpp:36-52), including its validity checks. */
+fsim_status fsim_config_from_ini(const char *path, fsim_config *cfg);
+fsim_status fsim_config_from_ini_text(const char *text, fsim_config *cfg);
+/* Replaces Parameter::initiateParameter (src/parameter.cpp:25-34). */
+fsim_status fsim_derive(const fsim_config *cfg, fsim_derived *out);
+
+/* -------------------------------------------------------------- particles */
+/* Host particle arrays in input order.  Replaces the .dat row layouts of
+ * Fluid/Solid/Virt_Host_List::addList (include/host_data.cuh:20-38,79-101,147-163). */
+typedef struct fsim_particles {
+    int n_fluid;
+    const float *fluid_pos, *fluid_vel;     /* 3*n_fluid each                  */
+    const float *fluid_rho, *fluid_p;       /* n_fluid each                    */
+    int n_solid;
+    const float *solid_pos, *solid_vel, *solid_ref_pos;  /* 3*n_solid each    */
+    const int *solid_type;                  /* 0 UNCONSTRAINED, 1 FIXED        */
+    int n_virt;
+    const float *virt_pos;                  /* 3*n_virt                        */
+    const int *virt_type;                   /* 0 FIXED, 1 MOVING (unused)      */
+} fsim_particles;
+
+/* Host-owned particle set read from .dat files. */
+typedef struct fsim_particle_set *fsim_particle_set_t;
+/* Read data_dir/{fluid,solid,virt}_particle.dat.  Replaces
+ * {Fluid,Solid,Virtual}Properties::readNumber (src/properties.cpp:7-32,68-93,
+ * 107-132: first line is N, then exactly N rows) and Sim::readParticleData
+ * (src/sim.cu:40-151).  All three files must exist (a count of 0 is allowed);
+ * a missing file, a count line that disagrees with the number of rows, or a
+ * row that does not parse returns FSIM_EIO / FSIM_EINVAL. */
+fsim_status fsim_particles_read(const char *data_dir, fsim_particle_set_t *out);
+fsim_status fsim_particles_view(fsim_particle_set_t set, fsim_particles *view);
+fsim_status fsim_particles_free(fsim_particle_set_t set);
+/* Write the three .dat files (same row layouts; 9 significant digits). */
+fsim_status fsim_particles_write(const char *data_dir, const fsim_particles *p);
+
+/* Project case generator for the benchmark configurations: a closed tank on
+ * the lattice (i + 0.5) * dx, a fluid block at the origin, an elastic block
+ * (plate or cube) and virtual wall layers outside the domain; y vertical.
+ * Follows the classification of cases/dam_break/particle_generate.cpp:50-91
+ * (solid first, then wall, then fluid).  Hydrostatic start: p = rho0 g (H - y)
+ * with H the block height, rho from the inverse Tait EOS (src/fluid.cu:7-14).
+ * The config supplies rho0, c0, gamma and g. */
+typedef struct fsim_case {
+    float dx;                       /* lattice spacing                          */
+    int   tank_n[3];                /* tank extents in lattice cells (x, y, z)  */
+    int   fluid_n[3];               /* fluid block cells, lower corner at 0     */
+    int   solid_lo[3];              /* solid block lower corner (lattice index) */
+    int   solid_n[3];               /* solid block cells (0 = no solid)         */
+    int   solid_fixed_layers;       /* solid continued below the floor, FIXED   */
+    int   virt_layers;              /* wall layers of virtual particles         */
+    int   hydrostatic;              /* 1: hydrostatic initial density/pressure  */
+    float jitter;                   /* uniform +-jitter*dx on fluid/solid pos   */
+    uint64_t seed;
+} fsim_case;
+fsim_status fsim_case_generate(const fsim_case *c, const fsim_config *cfg,
+                               fsim_particle_set_t *out);
+
+/* -------------------------------------------------------------- simulation */
+typedef struct fsim_sim *fsim_handle;
+
+/* Copy a particle set to the device and build the initial cell structure.
+ * Replaces Sim::initiate (include/sim.cuh:33-43: createCell, fillCell,
+ * copyData) + MemoryCopy::copyConstant (src/memory_copy.cu:8-12).
+ * device < 0 keeps the current device. */
+fsim_status fsim_create(const fsim_config *cfg, const fsim_particles *p,
+                        int device, fsim_handle *out);
+fsim_status fsim_destroy(fsim_handle h);
+
+/* Advance nsteps fluid steps (each with solid_sub_step solid sub-steps);
+ * enqueued on the handle's stream, returns without waiting.  Equals the loop
+ * body of DeviceCalculation::calculation (src/calculation.cu:23-33) without
+ * output, repeated nsteps times. */
+fsim_status fsim_step(fsim_handle h, int nsteps);
+/* Wait for the handle's stream; reports device-side error flags. */
+fsim_status fsim_sync(fsim_handle h);
+
+/* Phases, for parity tests.  One call runs one reference phase function. */
+enum {
+    FSIM_PHASE_CELL = 0,    /* particleCellUpdate + fillCell   src/pair.cu:53-70,195-207 */
+    FSIM_PHASE_COUPLE = 1,  /* coupleCalculation               src/solid.cu:346-359      */
+    FSIM_PHASE_VIRT = 2,    /* virtUpdate                      src/virt.cu:77-87         */
+    FSIM_PHASE_FLUID = 3,   /* fluidCalculation                src/fluid.cu:271-284      */
+    FSIM_PHASE_SOLID = 4    /* solidCalculation (all sub-steps) src/solid.cu:241-260     */
+};
+fsim_status fsim_run_phase(fsim_handle h, int phase);
+
+/* Per-particle fields (input order). */
+enum {
+    FSIM_FLUID_POS = 0, FSIM_FLUID_VEL = 1, FSIM_FLUID_RHO = 2, FSIM_FLUID_P = 3,
+    FSIM_FLUID_DRHO_DT = 4, FSIM_FLUID_DU_DT = 5, FSIM_FLUID_CELL_ID = 6,
+    FSIM_SOLID_POS = 10, FSIM_SOLID_VEL = 11, FSIM_SOLID_REF_POS = 12,
+    FSIM_SOLID_TYPE = 13, FSIM_SOLID_NORMAL = 14, FSIM_SOLID_P = 15,
+    FSIM_SOLID_DU_DT = 16, FSIM_SOLID_COUPLE_DUDT = 17, FSIM_SOLID_F = 18,
+    FSIM_SOLID_PK1 = 19, FSIM_SOLID_LINV = 20, FSIM_SOLID_CELL_ID = 21,
+    FSIM_VIRT_POS = 30, FSIM_VIRT_NORMAL = 31, FSIM_VIRT_VEL = 32,
+    FSIM_VIRT_P = 33, FSIM_VIRT_RHO = 34, FSIM_VIRT_CELL_ID = 35
+};
+/* Number of float/int components per particle of a field (1, 3 or 9); 0 if unknown. */
+int fsim_field_width(int field);
+/* Copy a field to host memory in input order; bytes must be exactly
+ * count*width*4.  Cell ids are int32, everything else float32.  Replaces the
+ * thrust device->host copies of Output::write* (src/output.cu:9-10 etc.). */
+fsim_status fsim_get_field(fsim_handle h, int field, void *host_dst, size_t bytes);
+/* Overwrite a state field from host memory (input order).  Settable:
+ * FLUID_POS/VEL/RHO/P, SOLID_POS/VEL.  Used by the end-to-end benchmark
+ * (host->device inputs per step) and by tests. */
+fsim_status fsim_set_field(fsim_handle h, int field, const void *host_src, size_t bytes);
+
+/* Neighbour search products.
+ * counts: for every fluid particle (input order) the number of fluid, solid
+ * and virtual particles within the impact distance among its 27 cells
+ * (3*n_fluid ints), using the same FP32 distance test as the sweep. */
+fsim_status fsim_neighbor_counts(fsim_handle h, int *host_counts, size_t bytes);
+/* Cell structure of one species (0 fluid, 1 solid, 2 virtual): cell_start
+ * (cell_number_total+1 ints) and the input ids in cell order (n ints). */
+fsim_status fsim_get_cells(fsim_handle h, int species, int *cell_start, size_t start_bytes,
+                           int *ids_in_cell_order, size_t ids_bytes);
+
+/* Write the reference's VTK files for the current state into out_dir
+ * (out_dir/fluid, out_dir/solid, out_dir/virtual, created if absent), with
+ * file index file_step.  Reproduces Output::outputData (src/output.cu:299-335)
+ * byte for byte, including fluid_pressure-k.vtk carrying the always-zero
+ * color field (src/output.cu:75); real fluid pressure goes to the extra file
+ * fluid/fluid_true_pressure-k.vtk. */
+fsim_status fsim_write_vtk(fsim_handle h, const char *out_dir, int file_step);
+
+/* Device timing: run nsteps (CUDA-graph replays) on the handle's stream
+ * bracketed by CUDA events recorded on that stream; *ms = elapsed device time. */
+fsim_status fsim_time_steps(fsim_handle h, int nsteps, float *ms);
+/* Instrumented timing: run nsteps launch by launch with an event pair around
+ * every launch of the fluid sweep kernel; *total_ms = elapsed device time of
+ * the nsteps, *sweep_ms = summed device time of the nsteps sweep launches. */
+fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_ms, float *sweep_ms);
+/* Kernel launches one fsim_step(h, 1) issues (for launch accounting). */
+fsim_status fsim_launches_per_step(fsim_handle h, int *n);
+
+/* Pinned (page-locked) host memory for fast host<->device field copies. */
+fsim_status fsim_host_alloc(size_t bytes, void **out);
+fsim_status fsim_host_free(void *p);
+
+/* Sizes of the instance. */
+fsim_status fsim_counts(fsim_handle h, int *n_fluid, int *n_solid, int *n_virt);
+fsim_status fsim_get_derived(fsim_handle h, fsim_derived *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUIDSIM_H */
