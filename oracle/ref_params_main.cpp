@@ -24,7 +24,10 @@
 
 static void pf(const char *k, float v, bool comma = true)
 {
-    std::printf("  \"%s\": %.9g%s\n", k, (double)v, comma ? "," : "");
+    if (v != v || v - v != 0.0f) // NaN or infinity: JSON has no literal for them
+        std::printf("  \"%s\": \"%.9g\"%s\n", k, (double)v, comma ? "," : "");
+    else
+        std::printf("  \"%s\": %.9g%s\n", k, (double)v, comma ? "," : "");
 }
 static void pi(const char *k, long v, bool comma = true)
 {
