@@ -300,6 +300,20 @@ def run_gb300(args, dist):
     return 0
 
 
+def run_profile(args):
+    """Fewest launches for an ncu capture: creation, then N graph-free steps
+    (the same kernels as the timed region)."""
+    from fluidsim_gb300 import api
+
+    cfg, pa = workload(args)
+    sim = api.Simulation(cfg, pa, device=0)
+    tot, sweep = sim.time_sweep(args.profile_steps)
+    sim.close()
+    print(json.dumps({"profile_steps": args.profile_steps, "ms_per_step": tot / args.profile_steps,
+                      "sweep_ms": sweep / args.profile_steps}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -308,7 +322,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="profiling run for ncu: create the workload, run this many steps, print nothing else")
     args = ap.parse_args()
+    if args.profile_steps:
+        return run_profile(args)
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     dist = Dist()
