@@ -143,6 +143,7 @@ def load():
         "fsim_host_free": (C.c_int, [P]),
         "fsim_counts": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "fsim_get_derived": (C.c_int, [P, C.POINTER(Derived)]),
+        "fsim_cell_sort_noalloc": (C.c_int, [C.POINTER(Derived), P, C.c_int, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -159,6 +160,7 @@ EXPORTED = [
     "fsim_step", "fsim_sync", "fsim_run_phase", "fsim_field_width", "fsim_get_field", "fsim_set_field",
     "fsim_neighbor_counts", "fsim_get_cells", "fsim_write_vtk", "fsim_time_steps", "fsim_time_sweep",
     "fsim_launches_per_step", "fsim_host_alloc", "fsim_host_free", "fsim_counts", "fsim_get_derived",
+    "fsim_cell_sort_noalloc",
 ]
 
 

@@ -243,6 +243,28 @@ fsim_status fsim_launches_per_step(fsim_handle h, int *n);
 fsim_status fsim_host_alloc(size_t bytes, void **out);
 fsim_status fsim_host_free(void *p);
 
+/* Allocation-free cell sort.  No counterpart in the reference.
+ * For callers that cannot allocate device memory while they run (hosts that
+ * reserve all GPU memory up front under their own allocator or budget, and
+ * real-time loops that cannot take the device synchronisation of
+ * cudaMalloc/cudaFree).  Sorts n positions (device memory, 3 floats each) into
+ * the cell grid of *grid (from fsim_derive): d_cell_start receives
+ * cell_number_total + 1 exclusive-scan offsets, d_ids the input indices in cell
+ * order, ordered by input index inside a cell — the same result as the cell
+ * phase of a handle.  Both outputs are caller-owned device memory; work is
+ * enqueued on `stream` (a cudaStream_t, NULL for the default stream).
+ * Scratch is one fixed device array inside the library (4 MiB, held by every
+ * GPU that loads the library until the process exits): at most
+ * FSIM_NOALLOC_MAX_PARTICLES positions and FSIM_NOALLOC_MAX_CELLS cells, else
+ * FSIM_EINVAL.  Positions outside the grid are clamped into its boundary cells.
+ * The first call on a device looks up the array's device address (make it
+ * before any stream capture).  All calls share the array: calls that overlap
+ * on the GPU race, so order them. */
+#define FSIM_NOALLOC_MAX_PARTICLES 262144
+#define FSIM_NOALLOC_MAX_CELLS 262144
+fsim_status fsim_cell_sort_noalloc(const fsim_derived *grid, const float *d_pos, int n,
+                                   int *d_cell_start, int *d_ids, void *stream);
+
 /* Sizes of the instance. */
 fsim_status fsim_counts(fsim_handle h, int *n_fluid, int *n_solid, int *n_virt);
 fsim_status fsim_get_derived(fsim_handle h, fsim_derived *out);
