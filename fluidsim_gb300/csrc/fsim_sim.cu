@@ -35,7 +35,7 @@ namespace {
 // ---------------------------------------------------------------- params
 struct DevParams {
     // kernel (src/kernel.cpp:43-60)
-    float R2, h, h_inv2, kdiff, kc1, kc2, eps_h2;
+    float R2, h, h_inv2, kdiff, kc1, kc2, eps_h2, exp2_scale;
     // fluid (src/properties.cpp:47-57)
     float c0, c0_inv, rho0, rho0_inv, gamma, rho2p, min_p, min_rho, max_rho, mu10, vmax;
     int viscid;
@@ -288,35 +288,59 @@ __device__ __forceinline__ float tait_pressure(const DevParams &P, float rho)
 // ------------------------------------------------------ Riemann pair term
 // fluidFluidCalculate / fluidSolidCalculate / fluidVirtCalculate
 // (src/fluid.cu:26-167), algebraically regrouped:
-//   P*   = (rho_i p_j + rho_j p_i)/(rho_i+rho_j) [+ rho_i rho_j du/(rho_i+rho_j) * lim]
+//   P*   = (rho_i p_j + rho_j p_i)/(rho_i+rho_j) [+ rho_i rho_j du/(rho_i+rho_j) * lim  if du >= 0]
 //   (u_i - v*).dx = (rho_j (u_i-u_j).dx - (p_i-p_j) r / c0) / (rho_i+rho_j)
 //   du/dt += w dx (-2 P* + 10 mu vis) / rho_i,  drho/dt += 2 rho_i w (u_i - v*).dx
-// The caller multiplies by 1/rho_i and 2 rho_i once per particle.
+// with w = exp(-r^2/h^2) * kernel_differential (so that w dx = V grad W).
+// The caller multiplies by 1/rho_i and 2 rho_i once per particle.  The
+// transcendental parts use the PTX approximations ex2/rsqrt/rcp.approx (the
+// reference's release build is compiled with -use_fast_math).
 struct PairAcc {
     float drho, ax, ay, az;
 };
 
-template <bool LIMITER, bool CLAMP_PS>
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// LIMITER: min(3 du, c0) (fluid, wall) or c0 (solid).  clamp_ps: P* >= 0 (wall).
+template <bool LIMITER, bool VISCID>
 __device__ __forceinline__ void riemann_pair(const DevParams &P, float dx, float dy, float dz, float r2, float uix,
                                              float uiy, float uiz, float rhoi, float pi, float ujx, float ujy,
-                                             float ujz, float rhoj, float pj, PairAcc &A)
+                                             float ujz, float rhoj, float pj, bool clamp_ps, PairAcc &A)
 {
-    const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
-    const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
-    const float rs_inv = __fdividef(1.0f, rhoi + rhoj);
+    const float w = ex2_approx(r2 * P.exp2_scale) * P.kdiff;
+    const float inv_r = rsqrt_approx(fmaxf(r2, 1e-30f)); // r2 = 0 (the particle itself) contributes 0
+    const float rs_inv = rcp_approx(rhoi + rhoj);
     const float a = (uix - ujx) * dx + (uiy - ujy) * dy + (uiz - ujz) * dz;
-    const float du = a * inv_r;
+    const float du = fmaxf(a * inv_r, 0.0f); // only du >= 0 adds dissipation
+    const float lim = LIMITER ? fminf(3.0f * du, P.c0) : P.c0;
     float ps = (rhoi * pj + rhoj * pi) * rs_inv;
-    if (du >= 0.0f) ps += rhoi * rhoj * du * rs_inv * (LIMITER ? fminf(3.0f * du, P.c0) : P.c0);
-    if (CLAMP_PS) ps = fmaxf(ps, 0.0f);
+    ps = fmaf(rhoi * rhoj * rs_inv * du, lim, ps);
+    if (clamp_ps) ps = fmaxf(ps, 0.0f);
     const float r = r2 * inv_r;
-    A.drho += (rhoj * a - (pi - pj) * r * P.c0_inv) * rs_inv * w;
+    A.drho = fmaf((rhoj * a - (pi - pj) * r * P.c0_inv) * rs_inv, w, A.drho);
     float f = -2.0f * ps;
-    if (P.viscid) f += P.mu10 * __fdividef(-a, r2 + P.eps_h2);
+    if (VISCID) f = fmaf(P.mu10 * -a, rcp_approx(r2 + P.eps_h2), f);
     f *= w;
-    A.ax += f * dx;
-    A.ay += f * dy;
-    A.az += f * dz;
+    A.ax = fmaf(f, dx, A.ax);
+    A.ay = fmaf(f, dy, A.ay);
+    A.az = fmaf(f, dz, A.az);
 }
 
 // ------------------------------------------------------- fluid sweep
@@ -391,7 +415,7 @@ constexpr int kChunk = 16;    // candidates between capacity checks
 
 enum Species { kFluid = 0, kVirt = 1, kSolid = 2 };
 
-template <int SP>
+template <int SP, bool VISCID>
 __device__ __forceinline__ void flush_list(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
                                            int &cnt, float4 pr, float4 vp, PairAcc &acc)
 {
@@ -404,22 +428,22 @@ __device__ __forceinline__ void flush_list(const DevParams &P, const FluidSweepA
                 const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
                 const float r2 = dist2(dx, dy, dz);
                 const float k2 = 2.0f * ((vp.x - sv.x) * np.x + (vp.y - sv.y) * np.y + (vp.z - sv.z) * np.z);
-                riemann_pair<false, false>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, vp.x - k2 * np.x,
-                                           vp.y - k2 * np.y, vp.z - k2 * np.z, pr.w, np.w, acc);
+                riemann_pair<false, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, vp.x - k2 * np.x,
+                                           vp.y - k2 * np.y, vp.z - k2 * np.z, pr.w, np.w, false, acc);
             } else {
                 const float4 q = SP == kFluid ? A.posr[j] : A.v_posr[j];
                 const float4 u = SP == kFluid ? A.velp[j] : A.v_velp[j];
                 const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
                 const float r2 = dist2(dx, dy, dz);
-                riemann_pair<true, SP == kVirt>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q.w,
-                                                u.w, acc);
+                riemann_pair<true, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q.w,
+                                                u.w, SP == kVirt, acc);
             }
         }
     }
     cnt = 0;
 }
 
-template <int SP, bool CHECK_Z>
+template <int SP, bool CHECK_Z, bool VISCID>
 __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
                                                int &cnt, bool in, int cz, int cx, int cy, int z0, int z1, float4 pr,
                                                float4 vp, PairAcc &acc)
@@ -437,7 +461,7 @@ __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSw
             const int je = start[base + z1];
             while (j < je) {
                 if (__reduce_max_sync(kFull, cnt) > kListCap - kChunk)
-                    flush_list<SP>(P, A, lst, lane, cnt, pr, vp, acc);
+                    flush_list<SP, VISCID>(P, A, lst, lane, cnt, pr, vp, acc);
                 const int jend = min(j + kChunk, je);
 #pragma unroll 4
                 for (; j < jend; ++j) {
@@ -453,10 +477,10 @@ __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSw
             }
         }
     }
-    flush_list<SP>(P, A, lst, lane, cnt, pr, vp, acc);
+    flush_list<SP, VISCID>(P, A, lst, lane, cnt, pr, vp, acc);
 }
 
-template <bool KEEP, bool CHECK_Z>
+template <bool KEEP, bool CHECK_Z, bool VISCID>
 __global__ void __launch_bounds__(kSweepWarps * 32) k_fluid_sweep(const DevParams P, const FluidSweepArgs A)
 {
     __shared__ int lists[kSweepWarps][kListCap][32];
@@ -481,9 +505,9 @@ __global__ void __launch_bounds__(kSweepWarps * 32) k_fluid_sweep(const DevParam
         const int zhi = __reduce_max_sync(kFull, in ? cz : INT_MIN);
         const int z0 = max(zlo - 1, 0), z1 = min(zhi + 1, P.nz - 1) + 1;
         const int cx = grow / P.ny, cy = grow - cx * P.ny;
-        gather_species<kFluid, CHECK_Z>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
-        gather_species<kVirt, CHECK_Z>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
-        gather_species<kSolid, CHECK_Z>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
+        gather_species<kFluid, CHECK_Z, VISCID>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
+        gather_species<kVirt, CHECK_Z, VISCID>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
+        gather_species<kSolid, CHECK_Z, VISCID>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
     }
     if (valid) fluid_update_store<KEEP>(P, A, i, pr, vp, acc);
 }
@@ -1070,6 +1094,7 @@ void fill_params(fsim_sim *h)
     P.kc1 = d.kernel_coefficient_1;
     P.kc2 = d.kernel_coefficient_2;
     P.eps_h2 = 0.01f * d.smoothing_length_square;
+    P.exp2_scale = -d.smoothing_length_inverse_square * 1.4426950408889634f;
     P.c0 = c.fluid_sound_speed;
     P.c0_inv = 1.0f / c.fluid_sound_speed;
     P.rho0 = c.fluid_density;
@@ -1228,13 +1253,12 @@ fsim_status enqueue_fluid(fsim_sim *h)
     const bool timed = h->instrument && (size_t)(2 * h->instr_step + 1) < h->sweep_events.size();
     if (timed) CK(cudaEventRecord(h->sweep_events[2 * h->instr_step], h->stream));
     const int gs = blocks_for(h->nf, kSweepWarps * 32);
-    if (h->keep) {
-        if (h->check_z) k_fluid_sweep<true, true><<<gs, kSweepWarps * 32, 0, h->stream>>>(h->P, A);
-        else k_fluid_sweep<true, false><<<gs, kSweepWarps * 32, 0, h->stream>>>(h->P, A);
-    } else {
-        if (h->check_z) k_fluid_sweep<false, true><<<gs, kSweepWarps * 32, 0, h->stream>>>(h->P, A);
-        else k_fluid_sweep<false, false><<<gs, kSweepWarps * 32, 0, h->stream>>>(h->P, A);
-    }
+    using SweepFn = void (*)(const DevParams, const FluidSweepArgs);
+    static const SweepFn table[8] = {
+        k_fluid_sweep<false, false, false>, k_fluid_sweep<false, false, true>, k_fluid_sweep<false, true, false>,
+        k_fluid_sweep<false, true, true>,   k_fluid_sweep<true, false, false>,  k_fluid_sweep<true, false, true>,
+        k_fluid_sweep<true, true, false>,   k_fluid_sweep<true, true, true>};
+    table[(h->keep ? 4 : 0) + (h->check_z ? 2 : 0) + (h->P.viscid ? 1 : 0)]<<<gs, kSweepWarps * 32, 0, h->stream>>>(h->P, A);
     CK_LAUNCH();
     if (timed) CK(cudaEventRecord(h->sweep_events[2 * h->instr_step + 1], h->stream));
     h->launches++;
