@@ -181,18 +181,19 @@ def run_reference(args, dist):
         return 0
     cfg, pa = workload(args)
     cores = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        cpu_oracle_rate(cfg, pa, "f32", 1, cores)
-    rate, dt = cpu_oracle_rate(cfg, pa, "f32", args.steps, cores)
+    # one untimed warm-up step sizes the sample: at most K steps and about 45 s
+    _, t1 = cpu_oracle_rate(cfg, pa, "f32", 1, cores)
+    steps = max(1, min(args.steps, int(45.0 / max(t1, 1e-3))))
+    rate, dt = cpu_oracle_rate(cfg, pa, "f32", steps, cores)
     desc = workload_desc(cfg, pa)
     line = {
         "impl": "reference", "metric": "particle-updates/s", "value": rate, "unit": "particle-updates/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "n_gpus": args.gpus, "steps": steps, "warmup": 1, "ms_per_step": dt * 1e3 / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": desc,
         "cpu_baseline": {"value": rate, "unit": "particle-updates/s", "cores": cores, "kind": "port",
                          "sample": "%d fluid steps of the full workload (oracle FP32 restatement of the "
-                                   "reference CUDA path, OpenMP)" % args.steps},
+                                   "reference CUDA path, OpenMP), sized to ~45 s" % steps},
         "e2e": {"value": rate, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference is a CUDA-only program; its CUDA sources need the unvendored glm library and are "
                 "not built here, so the reference arm is the CPU restatement of its algorithm",
@@ -269,6 +270,11 @@ def run_gb300(args, dist):
         b.free()
     sim.close()
 
+    # ---- the batched form on the ensemble workload
+    forms = None
+    if not args.no_forms:
+        forms = {"ensemble64": run_ensemble(dev, max(10, min(args.steps, 50)))}
+
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if dist.ws == 1 and not args.no_cpu_baseline:
@@ -293,11 +299,45 @@ def run_gb300(args, dist):
                          "step_frac": step_bytes / (ms * 1e-3 / args.steps) / 1e9 / hbm_peak},
             "cpu_baseline": cpu,
             "clocks": clk,
+            "forms": forms,
             "gpu_launches": launches * args.steps,
             "wall_s_timed": t_wall,
         }
         print(json.dumps(line), flush=True)
     return 0
+
+
+def run_ensemble(dev, steps):
+    """BASELINE config 3: 64 seeded dam-break instances (8k-250k fluid
+    particles, plate E log-uniform 1e5-1e7 Pa, nu 0.3-0.45, gate 0.6-1.0 m),
+    advanced (a) one instance after another in the plain form and (b) all at
+    once by batched launches.  Returns aggregate particle-updates/s of both."""
+    from fluidsim_gb300 import api, cases
+
+    members = [cases.make(s) for s in cases.ensemble(64, 2024)]
+    total = sum(pa.n_fluid + pa.n_solid for _, pa in members)
+    sims = [api.Simulation(cfg, pa, device=dev) for cfg, pa in members]
+    for sm in sims:
+        sm.step(3)
+        sm.sync()
+    one_by_one_ms = sum(sm.time_steps(steps) for sm in sims)
+    with api.Batch(sims) as b:
+        b.step(3)
+        b.sync()
+        batched_ms = b.time_steps(steps)
+        launches = b.launches_per_step()
+    for sm in sims:
+        sm.close()
+    return {
+        "workload": "ensemble of 64 dam-break instances (seed 2024), %d fluid+solid particles in total, "
+                    "dx=0.01, dt=1e-4, 4-5 solid sub-steps" % total,
+        "steps": steps,
+        "batched": total * steps / (batched_ms * 1e-3),
+        "one_by_one": total * steps / (one_by_one_ms * 1e-3),
+        "ratio": one_by_one_ms / batched_ms,
+        "unit": "particle-updates/s",
+        "batched_launches_per_step": launches,
+    }
 
 
 def run_profile(args):
@@ -322,6 +362,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling run for ncu: create the workload, run this many steps, print nothing else")
     args = ap.parse_args()

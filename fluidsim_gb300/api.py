@@ -144,6 +144,12 @@ def load():
         "fsim_counts": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "fsim_get_derived": (C.c_int, [P, C.POINTER(Derived)]),
         "fsim_cell_sort_noalloc": (C.c_int, [C.POINTER(Derived), P, C.c_int, P, P, P]),
+        "fsim_batch_create": (C.c_int, [C.POINTER(P), C.c_int, C.POINTER(P)]),
+        "fsim_batch_step": (C.c_int, [P, C.c_int]),
+        "fsim_batch_sync": (C.c_int, [P]),
+        "fsim_batch_time_steps": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
+        "fsim_batch_launches_per_step": (C.c_int, [P, C.POINTER(C.c_int)]),
+        "fsim_batch_destroy": (C.c_int, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -160,7 +166,8 @@ EXPORTED = [
     "fsim_step", "fsim_sync", "fsim_run_phase", "fsim_field_width", "fsim_get_field", "fsim_set_field",
     "fsim_neighbor_counts", "fsim_get_cells", "fsim_write_vtk", "fsim_time_steps", "fsim_time_sweep",
     "fsim_launches_per_step", "fsim_host_alloc", "fsim_host_free", "fsim_counts", "fsim_get_derived",
-    "fsim_cell_sort_noalloc",
+    "fsim_cell_sort_noalloc", "fsim_batch_create", "fsim_batch_step", "fsim_batch_sync", "fsim_batch_time_steps",
+    "fsim_batch_launches_per_step", "fsim_batch_destroy",
 ]
 
 
@@ -410,5 +417,49 @@ class PinnedBuffer:
     def __del__(self):
         try:
             self.free()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Several Simulations advanced in lockstep by batched launches (fsim_batch_*)."""
+
+    def __init__(self, sims):
+        self.lib = load()
+        self.sims = list(sims)
+        arr = (C.c_void_p * len(self.sims))(*[sm.h.value for sm in self.sims])
+        self.b = C.c_void_p()
+        check(self.lib.fsim_batch_create(arr, len(self.sims), C.byref(self.b)))
+
+    def step(self, n=1):
+        check(self.lib.fsim_batch_step(self.b, n))
+
+    def sync(self):
+        check(self.lib.fsim_batch_sync(self.b))
+
+    def time_steps(self, n):
+        ms = C.c_float()
+        check(self.lib.fsim_batch_time_steps(self.b, n, C.byref(ms)))
+        return ms.value
+
+    def launches_per_step(self):
+        n = C.c_int()
+        check(self.lib.fsim_batch_launches_per_step(self.b, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if self.b:
+            self.lib.fsim_batch_destroy(self.b)
+            self.b = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass

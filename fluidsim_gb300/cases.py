@@ -18,6 +18,8 @@ impact_length_hsml_ratio = 2 (config/input.ini:40 of the reference).
   (seed 12345).
 * ``tiny_box`` — a few thousand particles for fast tests.
 """
+import math
+
 from . import api
 
 
@@ -96,3 +98,39 @@ def make(cfg_case):
     """Generate the particles of a (config, case) pair."""
     cfg, case = cfg_case
     return cfg, api.generate_case(case, cfg)
+
+
+def _solid_substeps(cfg, base=4):
+    """Solid sub-steps for stability: the explicit TLSPH step must stay below
+    about 0.25 h / c_s (c_s from the bulk modulus); never fewer than `base`."""
+    E, nu, rho = cfg.youngs_modulus, cfg.poisson_ratio, cfg.solid_density
+    cs = math.sqrt(E / (3.0 * (1.0 - 2.0 * nu)) / rho)
+    limit = 0.25 * cfg.smoothing_length / cs
+    return max(base, int(math.ceil(cfg.dt / limit)))
+
+
+def ensemble_member(rng, dx=0.01, n_range=(8000, 250000), steps=500):
+    """One dam-break instance of the batched ensemble: fluid count log-uniform
+    in n_range (random block dims), plate E log-uniform in [1e5, 1e7] Pa, nu
+    uniform in [0.3, 0.45], gate x uniform in [0.6, 1.0] m; tank 1.6 m long and
+    0.8 m wide, tall enough for the column."""
+    target = math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))
+    gate = int(round(rng.uniform(0.6, 1.0) / dx))
+    nz = int(rng.integers(30, 81))
+    nx = int(rng.integers(max(10, gate // 3), gate - 2 + 1))
+    ny = max(4, int(round(target / (nx * nz))))
+    tank = (int(round(1.6 / dx)), max(int(round(0.4 / dx)), ny + 10), int(round(0.8 / dx)))
+    E = math.exp(rng.uniform(math.log(1e5), math.log(1e7)))
+    nu = float(rng.uniform(0.3, 0.45))
+    cfg = _config(dx, tank, rho_s=1100.0, E=E, nu=nu, dt=1e-4, sub=4, steps=steps)
+    cfg.solid_sub_step = _solid_substeps(cfg)
+    case = _case(dx, tank, (nx, ny, nz), (gate, 0, 0), (4, min(20, tank[1] - 1), min(40, tank[2])), 3)
+    return cfg, case
+
+
+def ensemble(n=64, seed=2024, **kw):
+    """The batched-ensemble workload: n independent instances (seeded)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    return [ensemble_member(rng, **kw) for _ in range(n)]

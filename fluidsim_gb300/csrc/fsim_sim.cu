@@ -24,6 +24,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -114,26 +115,73 @@ __device__ __forceinline__ void neighbor_rows(const DevParams &P, int c, Rows &r
     }
 }
 
-// ------------------------------------------------------- counting sort
-__global__ void k_hash(DevParams P, const float4 *__restrict__ pos, int n, int *__restrict__ key,
-                       int *__restrict__ slot, int *__restrict__ cnt, unsigned *flags)
+// ------------------------------------------------------- batched launches
+// Every step kernel has a body taking (params, args, local block index) and a
+// batched wrapper: one launch serves many instances, each with its own
+// parameters and buffers.  The wrapper finds its instance by binary search in
+// a per-launch prefix table of block counts (bstart[ninst] = total blocks) and
+// reads that instance's {params, args} item from the read-only item array.
+template <class Args>
+struct Item {
+    DevParams P;
+    Args A;
+};
+
+__device__ __forceinline__ int locate_instance(const int *__restrict__ bstart, int ninst, int b)
 {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const float4 p = pos[s];
-    const int c = cell_index(P, p.x, p.y, p.z, flags);
-    key[s] = c;
-    slot[s] = atomicAdd(&cnt[c], 1);
+    int lo = 0, hi = ninst;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (bstart[mid] <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
-struct ScanJob {
+#define FSIM_BATCHED_KERNEL(NAME, ARGS, BODY, BOUNDS)                                                      \
+    __global__ void __launch_bounds__(BOUNDS) NAME(const Item<ARGS> *__restrict__ items,                 \
+                                                   const int *__restrict__ bstart, int ninst)            \
+    {                                                                                                     \
+        const int inst = locate_instance(bstart, ninst, blockIdx.x);                                     \
+        const DevParams P = items[inst].P;                                                                \
+        const ARGS &A = items[inst].A;                                                                    \
+        BODY(P, A, (int)blockIdx.x - bstart[inst]);                                                       \
+    }
+
+// ------------------------------------------------------- counting sort
+struct HashArgs {
+    const float4 *pos;
+    int n;
+    int *key, *slot, *cnt;
+    unsigned *flags;
+};
+__device__ __forceinline__ void hash_body(const DevParams &P, const HashArgs &A, int blk)
+{
+    const int s = blk * blockDim.x + threadIdx.x;
+    if (s >= A.n) return;
+    const float4 p = A.pos[s];
+    const int c = cell_index(P, p.x, p.y, p.z, A.flags);
+    A.key[s] = c;
+    A.slot[s] = atomicAdd(&A.cnt[c], 1);
+}
+FSIM_BATCHED_KERNEL(kb_hash, HashArgs, hash_body, kBlock)
+
+struct ZeroArgs {
+    int *p;
+    int n;
+};
+__device__ __forceinline__ void zero_body(const DevParams &, const ZeroArgs &A, int blk)
+{
+    const int s = blk * blockDim.x + threadIdx.x;
+    if (s < A.n) A.p[s] = 0;
+}
+FSIM_BATCHED_KERNEL(kb_zero, ZeroArgs, zero_body, kBlock)
+
+struct ScanArgs {
     const int *in;
     int *out;
     int n;
     int *partial;
-};
-struct ScanJobs {
-    ScanJob j[2];
 };
 
 __device__ __forceinline__ int warp_inclusive_scan(int v)
@@ -169,24 +217,23 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *total)
     return before + inc - v;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(ScanJobs jobs)
+// scan pass 1: per-tile sums (one block per 4096-entry tile)
+__device__ __forceinline__ void scan_reduce_body(const DevParams &, const ScanArgs &J, int blk)
 {
-    const ScanJob J = jobs.j[blockIdx.y];
-    const int tiles = blocks_for(J.n, kScanTile);
-    if ((int)blockIdx.x >= tiles) return;
-    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    const int base = blk * kScanTile + threadIdx.x * kScanItems;
     int s = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k)
         if (base + k < J.n) s += J.in[base + k];
     int total;
     block_exclusive_scan(s, &total);
-    if (threadIdx.x == 0) J.partial[blockIdx.x] = total;
+    if (threadIdx.x == 0) J.partial[blk] = total;
 }
+FSIM_BATCHED_KERNEL(kb_scan_reduce, ScanArgs, scan_reduce_body, kScanThreads)
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_partials(ScanJobs jobs)
+// scan pass 2: exclusive scan of the tile sums (one block per array)
+__device__ __forceinline__ void scan_partials_body(const DevParams &, const ScanArgs &J, int)
 {
-    const ScanJob J = jobs.j[blockIdx.x];
     const int tiles = blocks_for(J.n, kScanTile);
     int carry = 0;
     for (int b0 = 0; b0 < tiles; b0 += kScanThreads) {
@@ -199,13 +246,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_partials(ScanJobs jobs)
     }
     if (threadIdx.x == 0) J.out[J.n] = carry;
 }
+FSIM_BATCHED_KERNEL(kb_scan_partials, ScanArgs, scan_partials_body, kScanThreads)
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_apply(ScanJobs jobs)
+// scan pass 3: scan inside each tile plus its offset
+__device__ __forceinline__ void scan_apply_body(const DevParams &, const ScanArgs &J, int blk)
 {
-    const ScanJob J = jobs.j[blockIdx.y];
-    const int tiles = blocks_for(J.n, kScanTile);
-    if ((int)blockIdx.x >= tiles) return;
-    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    const int base = blk * kScanTile + threadIdx.x * kScanItems;
     int v[kScanItems];
     int s = 0;
 #pragma unroll
@@ -214,21 +260,27 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(ScanJobs jobs)
         s += v[k];
     }
     int total;
-    int run = block_exclusive_scan(s, &total) + J.partial[blockIdx.x];
+    int run = block_exclusive_scan(s, &total) + J.partial[blk];
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
         if (base + k < J.n) J.out[base + k] = run;
         run += v[k];
     }
 }
+FSIM_BATCHED_KERNEL(kb_scan_apply, ScanArgs, scan_apply_body, kScanThreads)
 
-__global__ void k_scatter(const int *__restrict__ key, const int *__restrict__ slot, const int *__restrict__ start,
-                          int *__restrict__ tmp, int n)
+struct ScatterArgs {
+    const int *key, *slot, *start;
+    int *tmp;
+    int n;
+};
+__device__ __forceinline__ void scatter_body(const DevParams &, const ScatterArgs &A, int blk)
 {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    tmp[start[key[s]] + slot[s]] = s;
+    const int s = blk * blockDim.x + threadIdx.x;
+    if (s >= A.n) return;
+    A.tmp[A.start[A.key[s]] + A.slot[s]] = s;
 }
+FSIM_BATCHED_KERNEL(kb_scatter, ScatterArgs, scatter_body, kBlock)
 
 // Rank inside the cell by previous position: the new order is sorted by
 // (cell, previous sorted position), a stable and deterministic order.
@@ -243,39 +295,49 @@ __device__ __forceinline__ int stable_dst(const int *__restrict__ tmp, const int
     return b + rank;
 }
 
-__global__ void k_gather_fluid(const int *__restrict__ tmp, const int *__restrict__ key, const int *__restrict__ start,
-                               int n, const float4 *__restrict__ posr_in, const float4 *__restrict__ velp_in,
-                               const int *__restrict__ orig_in, float4 *__restrict__ posr_out,
-                               float4 *__restrict__ velp_out, int *__restrict__ orig_out, int *__restrict__ cell_out)
+struct GatherFluidArgs {
+    const int *tmp, *key, *start;
+    int n;
+    const float4 *posr_in, *velp_in;
+    const int *orig_in;
+    float4 *posr_out, *velp_out;
+    int *orig_out, *cell_out;
+};
+__device__ __forceinline__ void gather_fluid_body(const DevParams &, const GatherFluidArgs &A, int blk)
 {
-    const int d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= n) return;
+    const int d = blk * blockDim.x + threadIdx.x;
+    if (d >= A.n) return;
     int src, cell;
-    const int dst = stable_dst(tmp, key, start, d, src, cell);
-    posr_out[dst] = posr_in[src];
-    velp_out[dst] = velp_in[src];
-    orig_out[dst] = orig_in[src];
-    cell_out[dst] = cell;
+    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell);
+    A.posr_out[dst] = A.posr_in[src];
+    A.velp_out[dst] = A.velp_in[src];
+    A.orig_out[dst] = A.orig_in[src];
+    A.cell_out[dst] = cell;
 }
+FSIM_BATCHED_KERNEL(kb_gather_fluid, GatherFluidArgs, gather_fluid_body, kBlock)
 
-__global__ void k_gather_solid(const int *__restrict__ tmp, const int *__restrict__ key, const int *__restrict__ start,
-                               int n, const float4 *__restrict__ pos_in, const float4 *__restrict__ vel_in,
-                               const float4 *__restrict__ ref_in, const int *__restrict__ type_in,
-                               const int *__restrict__ orig_in, float4 *__restrict__ pos_out,
-                               float4 *__restrict__ vel_out, float4 *__restrict__ ref_out, int *__restrict__ type_out,
-                               int *__restrict__ orig_out, int *__restrict__ cell_out)
+struct GatherSolidArgs {
+    const int *tmp, *key, *start;
+    int n;
+    const float4 *pos_in, *vel_in, *ref_in;
+    const int *type_in, *orig_in;
+    float4 *pos_out, *vel_out, *ref_out;
+    int *type_out, *orig_out, *cell_out;
+};
+__device__ __forceinline__ void gather_solid_body(const DevParams &, const GatherSolidArgs &A, int blk)
 {
-    const int d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= n) return;
+    const int d = blk * blockDim.x + threadIdx.x;
+    if (d >= A.n) return;
     int src, cell;
-    const int dst = stable_dst(tmp, key, start, d, src, cell);
-    pos_out[dst] = pos_in[src];
-    vel_out[dst] = vel_in[src];
-    ref_out[dst] = ref_in[src];
-    type_out[dst] = type_in[src];
-    orig_out[dst] = orig_in[src];
-    cell_out[dst] = cell;
+    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell);
+    A.pos_out[dst] = A.pos_in[src];
+    A.vel_out[dst] = A.vel_in[src];
+    A.ref_out[dst] = A.ref_in[src];
+    A.type_out[dst] = A.type_in[src];
+    A.orig_out[dst] = A.orig_in[src];
+    A.cell_out[dst] = cell;
 }
+FSIM_BATCHED_KERNEL(kb_gather_solid, GatherSolidArgs, gather_solid_body, kBlock)
 
 // ------------------------------------------------------------ EOS
 // densityToPressure (src/fluid.cu:16-24): Tait EOS, floored at min_pressure.
@@ -319,7 +381,7 @@ __device__ __forceinline__ float rcp_approx(float x)
 }
 
 // LIMITER: min(3 du, c0) (fluid, wall) or c0 (solid).  clamp_ps: P* >= 0 (wall).
-template <bool LIMITER, bool VISCID>
+template <bool LIMITER, int VISCID>
 __device__ __forceinline__ void riemann_pair(const DevParams &P, float dx, float dy, float dz, float r2, float uix,
                                              float uiy, float uiz, float rhoi, float pi, float ujx, float ujy,
                                              float ujz, float rhoj, float pj, bool clamp_ps, PairAcc &A)
@@ -336,7 +398,7 @@ __device__ __forceinline__ void riemann_pair(const DevParams &P, float dx, float
     const float r = r2 * inv_r;
     A.drho = fmaf((rhoj * a - (pi - pj) * r * P.c0_inv) * rs_inv, w, A.drho);
     float f = -2.0f * ps;
-    if (VISCID) f = fmaf(P.mu10 * -a, rcp_approx(r2 + P.eps_h2), f);
+    if (VISCID == 1 || (VISCID == 2 && P.viscid)) f = fmaf(P.mu10 * -a, rcp_approx(r2 + P.eps_h2), f);
     f *= w;
     A.ax = fmaf(f, dx, A.ax);
     A.ay = fmaf(f, dy, A.ay);
@@ -356,12 +418,12 @@ struct FluidSweepArgs {
     float *drho_out;
     float4 *dudt_out;
     int n;
+    int keep; // write drho/dt and du/dt
 };
 
 // fluidUpdate (src/fluid.cu:234-269) applied to the sums of one particle: NaN
 // scrub, Euler step with the old velocity, density clamp, EOS, position clamp,
 // speed cap; writes the integrated state into the other buffer.
-template <bool KEEP>
 __device__ __forceinline__ void fluid_update_store(const DevParams &P, const FluidSweepArgs &A, int i, float4 pr,
                                                    float4 vp, const PairAcc &acc)
 {
@@ -388,7 +450,7 @@ __device__ __forceinline__ void fluid_update_store(const DevParams &P, const Flu
     A.posr_out[i] = make_float4(x, y, z, rho);
     A.velp_out[i] = make_float4(ux, uy, uz, p);
     A.orig_out[i] = A.orig_in[i];
-    if (KEEP) {
+    if (A.keep) {
         A.drho_out[i] = drho;
         A.dudt_out[i] = make_float4(ax, ay, az, 0.0f);
     }
@@ -415,7 +477,7 @@ constexpr int kChunk = 16;    // candidates between capacity checks
 
 enum Species { kFluid = 0, kVirt = 1, kSolid = 2 };
 
-template <int SP, bool VISCID>
+template <int SP, int VISCID>
 __device__ __forceinline__ void flush_list(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
                                            int &cnt, float4 pr, float4 vp, PairAcc &acc)
 {
@@ -443,7 +505,7 @@ __device__ __forceinline__ void flush_list(const DevParams &P, const FluidSweepA
     cnt = 0;
 }
 
-template <int SP, bool CHECK_Z, bool VISCID>
+template <int SP, bool CHECK_Z, int VISCID>
 __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
                                                int &cnt, bool in, int cz, int cx, int cy, int z0, int z1, float4 pr,
                                                float4 vp, PairAcc &acc)
@@ -480,12 +542,12 @@ __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSw
     flush_list<SP, VISCID>(P, A, lst, lane, cnt, pr, vp, acc);
 }
 
-template <bool KEEP, bool CHECK_Z, bool VISCID>
-__global__ void __launch_bounds__(kSweepWarps * 32) k_fluid_sweep(const DevParams P, const FluidSweepArgs A)
+template <bool CHECK_Z, int VISCID>
+__device__ __forceinline__ void fluid_sweep_body(const DevParams &P, const FluidSweepArgs &A, int blk)
 {
     __shared__ int lists[kSweepWarps][kListCap][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = (blockIdx.x * kSweepWarps + warp) * 32 + lane;
+    const int i = (blk * kSweepWarps + warp) * 32 + lane;
     const bool valid = i < A.n;
     int(*lst)[32] = lists[warp];
     const float4 pr = valid ? A.posr[i] : make_float4(0.0f, 0.0f, 0.0f, 1.0f);
@@ -509,36 +571,57 @@ __global__ void __launch_bounds__(kSweepWarps * 32) k_fluid_sweep(const DevParam
         gather_species<kVirt, CHECK_Z, VISCID>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
         gather_species<kSolid, CHECK_Z, VISCID>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
     }
-    if (valid) fluid_update_store<KEEP>(P, A, i, pr, vp, acc);
+    if (valid) fluid_update_store(P, A, i, pr, vp, acc);
+}
+
+template <bool CHECK_Z, int VISCID>
+__global__ void __launch_bounds__(kSweepWarps * 32) kb_fluid_sweep(const Item<FluidSweepArgs> *__restrict__ items,
+                                                                   const int *__restrict__ bstart, int ninst)
+{
+    const int inst = locate_instance(bstart, ninst, blockIdx.x);
+    const DevParams P = items[inst].P;
+    fluid_sweep_body<CHECK_Z, VISCID>(P, items[inst].A, (int)blockIdx.x - bstart[inst]);
+}
+
+// The one-instance sweep takes {params, args} by value: kernel parameters live
+// in the constant bank, where its hot loops read them without extra loads.
+template <bool CHECK_Z, int VISCID>
+__global__ void __launch_bounds__(kSweepWarps * 32) kb_fluid_sweep_1(const DevParams P, const FluidSweepArgs A)
+{
+    fluid_sweep_body<CHECK_Z, VISCID>(P, A, (int)blockIdx.x);
 }
 
 // ------------------------------------------------------- virtual particles
 // getVirtData (src/virt.cu:9-75): nearest fluid particle's rho, hydrostatically
 // corrected p and velocity mirrored about the (static) wall normal.  Ties in
 // distance go to the smaller input id.
-__global__ void __launch_bounds__(kBlock) k_virt(const DevParams P, const float4 *__restrict__ v_posr_in,
-                                                 const float4 *__restrict__ v_normal, const int *__restrict__ v_cell,
-                                                 const float4 *__restrict__ fposr, const float4 *__restrict__ fvelp,
-                                                 const int *__restrict__ forig, const int *__restrict__ start_f,
-                                                 float4 *__restrict__ v_posr, float4 *__restrict__ v_velp, int n)
+struct VirtArgs {
+    const float4 *v_posr_in, *v_normal;
+    const int *v_cell;
+    const float4 *fposr, *fvelp;
+    const int *forig, *start_f;
+    float4 *v_posr, *v_velp;
+    int n;
+};
+__device__ __forceinline__ void virt_body(const DevParams &P, const VirtArgs &A, int blk)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 xi = v_posr_in[i];
+    const int i = blk * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    const float4 xi = A.v_posr_in[i];
     Rows rows;
-    neighbor_rows(P, v_cell[i], rows);
+    neighbor_rows(P, A.v_cell[i], rows);
     float best = FSIM_LARGE_FLOAT;
     int best_j = -1, best_orig = INT_MAX;
     for (int r = 0; r < rows.count; ++r) {
-        for (int j = start_f[rows.base[r] + rows.z0], je = start_f[rows.base[r] + rows.z1]; j < je; ++j) {
-            const float4 q = fposr[j];
+        for (int j = A.start_f[rows.base[r] + rows.z0], je = A.start_f[rows.base[r] + rows.z1]; j < je; ++j) {
+            const float4 q = A.fposr[j];
             const float d2 = dist2(q.x - xi.x, q.y - xi.y, q.z - xi.z);
             if (d2 < best) {
                 best = d2;
                 best_j = j;
-                best_orig = forig[j];
+                best_orig = A.forig[j];
             } else if (d2 == best) {
-                const int o = forig[j];
+                const int o = A.forig[j];
                 if (o < best_orig) {
                     best_j = j;
                     best_orig = o;
@@ -548,18 +631,19 @@ __global__ void __launch_bounds__(kBlock) k_virt(const DevParams P, const float4
     }
     float rho = P.rho0, p = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
     if (best_j >= 0) {
-        const float4 q = fposr[best_j], u = fvelp[best_j];
+        const float4 q = A.fposr[best_j], u = A.fvelp[best_j];
         rho = q.w;
         p = u.w - rho * (P.gx * (q.x - xi.x) + P.gy * (q.y - xi.y) + P.gz * (q.z - xi.z));
         ux = u.x;
         uy = u.y;
         uz = u.z;
     }
-    const float4 nrm = v_normal[i];
+    const float4 nrm = A.v_normal[i];
     const float k2 = 2.0f * (ux * nrm.x + uy * nrm.y + uz * nrm.z);
-    v_posr[i] = make_float4(xi.x, xi.y, xi.z, rho);
-    v_velp[i] = make_float4(ux - k2 * nrm.x, uy - k2 * nrm.y, uz - k2 * nrm.z, p);
+    A.v_posr[i] = make_float4(xi.x, xi.y, xi.z, rho);
+    A.v_velp[i] = make_float4(ux - k2 * nrm.x, uy - k2 * nrm.y, uz - k2 * nrm.z, p);
 }
+FSIM_BATCHED_KERNEL(kb_virt, VirtArgs, virt_body, kBlock)
 
 // Wall normal of every virtual particle (src/virt.cu:52-70): minus the kernel
 // gradient sum over the other virtual particles, normalised, zero when its
@@ -615,32 +699,37 @@ __device__ __forceinline__ float warp_sum(float v)
 // solidCoupleUpdate (src/solid.cu:262-344): solid normal from the solid
 // neighbours' kernel gradients, solid pressure as the Shepard average of the
 // fluid pressure.  One warp per solid particle.
-__global__ void __launch_bounds__(kBlock) k_couple(const DevParams P, const float4 *__restrict__ s_pos,
-                                                   const int *__restrict__ s_cell, const int *__restrict__ start_s,
-                                                   const float4 *__restrict__ fposr, const float4 *__restrict__ fvelp,
-                                                   const int *__restrict__ start_f, float4 *__restrict__ s_np, int n)
+struct CoupleArgs {
+    const float4 *s_pos;
+    const int *s_cell, *start_s;
+    const float4 *fposr, *fvelp;
+    const int *start_f;
+    float4 *s_np;
+    int n;
+};
+__device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs &A, int blk)
 {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int i = (blk * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (i >= n) return; // whole warp
-    const float4 xi = s_pos[i];
+    if (i >= A.n) return; // whole warp
+    const float4 xi = A.s_pos[i];
     Rows rows;
-    neighbor_rows(P, s_cell[i], rows);
+    neighbor_rows(P, A.s_cell[i], rows);
     float nx = 0.0f, ny = 0.0f, nz = 0.0f, psum = 0.0f, wsum = 0.0f;
     for (int r = 0; r < rows.count; ++r) {
         const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-        for (int j = start_f[c0] + lane, je = start_f[c1]; j < je; j += 32) {
-            const float4 q = fposr[j];
+        for (int j = A.start_f[c0] + lane, je = A.start_f[c1]; j < je; j += 32) {
+            const float4 q = A.fposr[j];
             const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
             const float r2 = dist2(dx, dy, dz);
             if (r2 < P.R2) {
                 const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
                 wsum += w;
-                psum += fvelp[j].w * w;
+                psum += A.fvelp[j].w * w;
             }
         }
-        for (int j = start_s[c0] + lane, je = start_s[c1]; j < je; j += 32) {
-            const float4 q = s_pos[j];
+        for (int j = A.start_s[c0] + lane, je = A.start_s[c1]; j < je; j += 32) {
+            const float4 q = A.s_pos[j];
             const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
             const float r2 = dist2(dx, dy, dz);
             if (r2 < P.R2) {
@@ -667,8 +756,9 @@ __global__ void __launch_bounds__(kBlock) k_couple(const DevParams P, const floa
         nz *= s;
     }
     const float p = wsum > FSIM_EPS_FLOAT ? fmaxf(psum / wsum, P.min_p) : 0.0f;
-    s_np[i] = make_float4(nx, ny, nz, p);
+    A.s_np[i] = make_float4(nx, ny, nz, p);
 }
+FSIM_BATCHED_KERNEL(kb_couple, CoupleArgs, couple_body, kBlock)
 
 // ------------------------------------------------------------ solid
 struct SolidArgs {
@@ -716,9 +806,9 @@ __device__ __forceinline__ M3 cofactor(const M3 &a)
 // F <- F L^-1, Green strain, St-Venant-Kirchhoff 2nd Piola, P = F S.
 // Also stores P L^-1 and cof(F) L^-1 (= det(F) F^-T L^-1) for the force sweep.
 // One warp per solid particle.
-__global__ void __launch_bounds__(kBlock) k_solid_deform(const DevParams P, const SolidArgs S)
+__device__ __forceinline__ void solid_deform_body(const DevParams &P, const SolidArgs &S, int blk)
 {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int i = (blk * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= S.n) return; // whole warp
     const float4 Xi = S.ref[i], xi = S.pos[i];
@@ -793,14 +883,15 @@ __global__ void __launch_bounds__(kBlock) k_solid_deform(const DevParams P, cons
         S.AV[9 * i + k] = AV.m[k];
     }
 }
+FSIM_BATCHED_KERNEL(kb_solid_deform, SolidArgs, solid_deform_body, kBlock)
 
 // solidForceCalculate (src/solid.cu:81-207): stress divergence + artificial
 // viscosity over solid neighbours (reference configuration), fluid traction
 // over fluid neighbours (current configuration, fluid already advanced).
 // One warp per solid particle.
-__global__ void __launch_bounds__(kBlock) k_solid_force(const DevParams P, const SolidArgs S)
+__device__ __forceinline__ void solid_force_body(const DevParams &P, const SolidArgs &S, int blk)
 {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int i = (blk * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= S.n) return; // whole warp
     const float4 xi = S.pos[i], Xi = S.ref[i], vi = S.vel[i], ni = S.np[i];
@@ -868,11 +959,12 @@ __global__ void __launch_bounds__(kBlock) k_solid_force(const DevParams P, const
     S.couple[i] = make_float4(cx, cy, cz, 0.0f);
     S.dudt[i] = make_float4(ax + cx, ay + cy, az + cz, 0.0f);
 }
+FSIM_BATCHED_KERNEL(kb_solid_force, SolidArgs, solid_force_body, kBlock)
 
 // solidUpdate (src/solid.cu:209-239)
-__global__ void k_solid_update(const DevParams P, const SolidArgs S)
+__device__ __forceinline__ void solid_update_body(const DevParams &P, const SolidArgs &S, int blk)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blk * blockDim.x + threadIdx.x;
     if (i >= S.n) return;
     const int t = S.type[i];
     if (t == 1) { // FIXED_SOLID
@@ -890,6 +982,7 @@ __global__ void k_solid_update(const DevParams P, const SolidArgs S)
         S.pos[i] = make_float4(nx, ny, nz, x.w);
     }
 }
+FSIM_BATCHED_KERNEL(kb_solid_update, SolidArgs, solid_update_body, kBlock)
 
 // ------------------------------------------------------- neighbour counts
 __global__ void k_neighbor_counts(const DevParams P, const float4 *__restrict__ fposr, const int *__restrict__ cell_f,
@@ -980,11 +1073,11 @@ __global__ void k_pack_f4(const float *__restrict__ xyz, const float *__restrict
 } // namespace
 
 // =================================================================== handle
-struct GraphEntry {
-    cudaGraphExec_t exec = nullptr;
-    int f_after = 0, s_after = 0;
-};
+namespace {
+struct Plan; // the launches of a step (or of one phase) over a set of instances
+}
 
+struct fsim_batch;
 struct fsim_sim {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -1023,13 +1116,12 @@ struct fsim_sim {
     unsigned *d_flags = nullptr;
     void *staging = nullptr;
     size_t staging_bytes = 0;
-    GraphEntry graphs[2][2];
+    Plan *step_plans[2][2] = {};   // full step, by (fluid, solid) buffer parity
+    Plan *phase_plans[5][2][2] = {}; // one phase, by parity
+    fsim_batch *batch = nullptr;   // set while the handle belongs to a batch
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> sweep_events;
-    bool instrument = false;
-    int instr_step = 0;
     std::vector<void *> allocations;
-    int launches = 0; // kernel launches issued by the last enqueued step
 };
 
 namespace {
@@ -1067,11 +1159,21 @@ fsim_status dalloc(fsim_sim *h, T **p, size_t count)
     return FSIM_OK;
 }
 
+void free_plan(Plan *pl);
+
 void free_all(fsim_sim *h)
 {
-    for (auto &row : h->graphs)
-        for (auto &g : row)
-            if (g.exec) cudaGraphExecDestroy(g.exec);
+    for (auto &row : h->step_plans)
+        for (Plan *&pl : row) {
+            free_plan(pl);
+            pl = nullptr;
+        }
+    for (auto &ph : h->phase_plans)
+        for (auto &row : ph)
+            for (Plan *&pl : row) {
+                free_plan(pl);
+                pl = nullptr;
+            }
     for (void *p : h->allocations) cudaFree(p);
     h->allocations.clear();
     for (cudaEvent_t e : h->sweep_events) cudaEventDestroy(e);
@@ -1131,240 +1233,387 @@ void fill_params(fsim_sim *h)
     P.ncell = d.cell_number_total;
 }
 
-// ---------------------------------------------------------------- phases
-// Counting sort of one species: hash -> scan -> scatter -> stable gather.
-fsim_status enqueue_scan(fsim_sim *h, const int *cnt_f, int *start_f, const int *cnt_s, int *start_s)
+// ---------------------------------------------------------------- plans
+// A plan is the ordered list of batched launches that advance a set of
+// instances by one step (or one phase), with every launch's {params, args}
+// items and block prefix table in one device arena.  Buffer parities are the
+// same for all instances of a plan, so the plan is fixed and a whole step is
+// captured once into a CUDA graph.
+enum LaunchKind {
+    L_ZERO, L_HASH, L_SCAN_REDUCE, L_SCAN_PARTIALS, L_SCAN_APPLY, L_SCATTER, L_GATHER_F, L_GATHER_S,
+    L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE
+};
+
+struct Launch {
+    int kind;
+    size_t items_off, table_off; // arena offsets
+    int ninst, blocks, variant;
+};
+
+struct Plan {
+    int device = 0;
+    int pf = 0, ps = 0;           // buffer parities at the start
+    int pf_after = 0, ps_after = 0;
+    std::vector<Launch> launches;
+    char *arena = nullptr;
+    std::vector<char> host; // host image of the arena (one-instance launches pass items by value)
+    cudaGraphExec_t graph = nullptr;
+    int sweep_index = -1;         // launch index of the fluid sweep
+};
+
+void free_plan(Plan *pl)
 {
-    ScanJobs jobs;
-    std::memset(&jobs, 0, sizeof jobs);
-    int njobs = 0;
-    if (cnt_f) jobs.j[njobs++] = ScanJob{cnt_f, start_f, h->ncell, h->scan_partials};
-    if (cnt_s) jobs.j[njobs++] = ScanJob{cnt_s, start_s, h->ncell, h->scan_partials + kMaxScanTiles};
-    if (!njobs) return FSIM_OK;
-    const int tiles = blocks_for(h->ncell, kScanTile);
-    dim3 g(tiles, njobs);
-    k_scan_reduce<<<g, kScanThreads, 0, h->stream>>>(jobs);
-    CK_LAUNCH();
-    k_scan_partials<<<njobs, kScanThreads, 0, h->stream>>>(jobs);
-    CK_LAUNCH();
-    k_scan_apply<<<g, kScanThreads, 0, h->stream>>>(jobs);
-    CK_LAUNCH();
-    h->launches += 3;
-    return FSIM_OK;
+    if (!pl) return;
+    if (pl->graph) cudaGraphExecDestroy(pl->graph);
+    if (pl->arena) cudaFree(pl->arena);
+    delete pl;
 }
 
-fsim_status enqueue_cell_phase(fsim_sim *h)
-{
-    const int fo = h->f_cur ^ 1, so = h->s_cur ^ 1;
-    if (h->nf) CK(cudaMemsetAsync(h->f_cnt, 0, sizeof(int) * h->ncell, h->stream));
-    if (h->ns) CK(cudaMemsetAsync(h->s_cnt, 0, sizeof(int) * h->ncell, h->stream));
-    if (h->nf) {
-        k_hash<<<blocks_for(h->nf, kBlock), kBlock, 0, h->stream>>>(h->P, h->f_posr[h->f_cur], h->nf, h->f_key,
-                                                                     h->f_slot, h->f_cnt, h->d_flags);
-        CK_LAUNCH();
-        h->launches++;
+// Host image of a plan's arena.
+struct ArenaBuilder {
+    std::vector<char> bytes;
+    size_t put(const void *p, size_t n)
+    {
+        const size_t off = (bytes.size() + 255) & ~size_t(255);
+        bytes.resize(off + n);
+        std::memcpy(bytes.data() + off, p, n);
+        return off;
     }
-    if (h->ns) {
-        k_hash<<<blocks_for(h->ns, kBlock), kBlock, 0, h->stream>>>(h->P, h->s_pos[h->s_cur], h->ns, h->s_key,
-                                                                     h->s_slot, h->s_cnt, h->d_flags);
-        CK_LAUNCH();
-        h->launches++;
+};
+
+template <class Args>
+void add_launch(Plan &pl, ArenaBuilder &ab, int kind, const std::vector<Item<Args>> &items,
+                const std::vector<int> &blocks_per_item, int variant = 0)
+{
+    std::vector<int> table(items.size() + 1, 0);
+    for (size_t k = 0; k < items.size(); ++k) table[k + 1] = table[k] + blocks_per_item[k];
+    if (table.back() == 0) return; // nothing to do for any instance
+    Launch L;
+    L.kind = kind;
+    L.items_off = ab.put(items.data(), sizeof(Item<Args>) * items.size());
+    L.table_off = ab.put(table.data(), sizeof(int) * table.size());
+    L.ninst = (int)items.size();
+    L.blocks = table.back();
+    L.variant = variant;
+    pl.launches.push_back(L);
+}
+
+// The cell phase: counting sort of fluid and solid (parity pf -> 1-pf, ps -> 1-ps).
+void plan_cell(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
+{
+    std::vector<Item<ZeroArgs>> zi;
+    std::vector<Item<HashArgs>> hi;
+    std::vector<Item<ScanArgs>> si;
+    std::vector<Item<ScatterArgs>> ci;
+    std::vector<int> zb, hb, sb, sp, cb;
+    for (fsim_sim *h : m) {
+        for (int sp_ = 0; sp_ < 2; ++sp_) {
+            const int n = sp_ ? h->ns : h->nf;
+            Item<ZeroArgs> z{h->P, ZeroArgs{sp_ ? h->s_cnt : h->f_cnt, n ? h->ncell : 0}};
+            zi.push_back(z);
+            zb.push_back(blocks_for(z.A.n, kBlock));
+            Item<HashArgs> hh{h->P, sp_ ? HashArgs{h->s_pos[ps], h->ns, h->s_key, h->s_slot, h->s_cnt, h->d_flags}
+                                        : HashArgs{h->f_posr[pf], h->nf, h->f_key, h->f_slot, h->f_cnt, h->d_flags}};
+            hi.push_back(hh);
+            hb.push_back(blocks_for(n, kBlock));
+            Item<ScanArgs> sc{h->P, sp_ ? ScanArgs{h->s_cnt, h->s_start, h->ncell, h->scan_partials + kMaxScanTiles}
+                                        : ScanArgs{h->f_cnt, h->f_start, h->ncell, h->scan_partials}};
+            si.push_back(sc);
+            sb.push_back(n ? blocks_for(h->ncell, kScanTile) : 0);
+            sp.push_back(n ? 1 : 0);
+            Item<ScatterArgs> cc{h->P, sp_ ? ScatterArgs{h->s_key, h->s_slot, h->s_start, h->s_tmp, h->ns}
+                                           : ScatterArgs{h->f_key, h->f_slot, h->f_start, h->f_tmp, h->nf}};
+            ci.push_back(cc);
+            cb.push_back(blocks_for(n, kBlock));
+        }
     }
-    fsim_status st = enqueue_scan(h, h->nf ? h->f_cnt : nullptr, h->f_start, h->ns ? h->s_cnt : nullptr, h->s_start);
-    if (st) return st;
-    if (h->nf) {
-        k_scatter<<<blocks_for(h->nf, kBlock), kBlock, 0, h->stream>>>(h->f_key, h->f_slot, h->f_start, h->f_tmp,
-                                                                        h->nf);
-        CK_LAUNCH();
-        k_gather_fluid<<<blocks_for(h->nf, kBlock), kBlock, 0, h->stream>>>(
-            h->f_tmp, h->f_key, h->f_start, h->nf, h->f_posr[h->f_cur], h->f_velp[h->f_cur], h->f_orig[h->f_cur],
-            h->f_posr[fo], h->f_velp[fo], h->f_orig[fo], h->f_cell);
-        CK_LAUNCH();
-        h->launches += 2;
-        h->f_cur = fo;
+    add_launch(pl, ab, L_ZERO, zi, zb);
+    add_launch(pl, ab, L_HASH, hi, hb);
+    add_launch(pl, ab, L_SCAN_REDUCE, si, sb);
+    add_launch(pl, ab, L_SCAN_PARTIALS, si, sp);
+    add_launch(pl, ab, L_SCAN_APPLY, si, sb);
+    add_launch(pl, ab, L_SCATTER, ci, cb);
+    std::vector<Item<GatherFluidArgs>> gf;
+    std::vector<Item<GatherSolidArgs>> gs;
+    std::vector<int> gfb, gsb;
+    for (fsim_sim *h : m) {
+        gf.push_back({h->P, GatherFluidArgs{h->f_tmp, h->f_key, h->f_start, h->nf, h->f_posr[pf], h->f_velp[pf],
+                                            h->f_orig[pf], h->f_posr[1 - pf], h->f_velp[1 - pf], h->f_orig[1 - pf],
+                                            h->f_cell}});
+        gfb.push_back(blocks_for(h->nf, kBlock));
+        gs.push_back({h->P, GatherSolidArgs{h->s_tmp, h->s_key, h->s_start, h->ns, h->s_pos[ps], h->s_vel[ps],
+                                            h->s_ref[ps], h->s_type[ps], h->s_orig[ps], h->s_pos[1 - ps],
+                                            h->s_vel[1 - ps], h->s_ref[1 - ps], h->s_type[1 - ps], h->s_orig[1 - ps],
+                                            h->s_cell}});
+        gsb.push_back(blocks_for(h->ns, kBlock));
     }
-    if (h->ns) {
-        k_scatter<<<blocks_for(h->ns, kBlock), kBlock, 0, h->stream>>>(h->s_key, h->s_slot, h->s_start, h->s_tmp,
-                                                                        h->ns);
-        CK_LAUNCH();
-        k_gather_solid<<<blocks_for(h->ns, kBlock), kBlock, 0, h->stream>>>(
-            h->s_tmp, h->s_key, h->s_start, h->ns, h->s_pos[h->s_cur], h->s_vel[h->s_cur], h->s_ref[h->s_cur],
-            h->s_type[h->s_cur], h->s_orig[h->s_cur], h->s_pos[so], h->s_vel[so], h->s_ref[so], h->s_type[so],
-            h->s_orig[so], h->s_cell);
-        CK_LAUNCH();
-        h->launches += 2;
-        h->s_cur = so;
+    add_launch(pl, ab, L_GATHER_F, gf, gfb);
+    add_launch(pl, ab, L_GATHER_S, gs, gsb);
+}
+
+void plan_couple(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
+{
+    std::vector<Item<CoupleArgs>> it;
+    std::vector<int> nb;
+    for (fsim_sim *h : m) {
+        it.push_back({h->P, CoupleArgs{h->s_pos[ps], h->s_cell, h->s_start, h->f_posr[pf], h->f_velp[pf], h->f_start,
+                                       h->s_np, h->ns}});
+        nb.push_back(h->nf && h->ns ? blocks_for(32ll * h->ns, kBlock) : 0);
     }
-    h->f_sorted = true;
-    h->s_sorted = true;
-    h->f_deriv_ok = false;
-    h->s_np_ok = false;
-    h->s_mech_ok = false;
-    return FSIM_OK;
+    add_launch(pl, ab, L_COUPLE, it, nb);
 }
 
-fsim_status enqueue_couple(fsim_sim *h)
+void plan_virt(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf)
 {
-    if (!h->nf || !h->ns) return FSIM_OK;
-    k_couple<<<blocks_for(32ll * h->ns, kBlock), kBlock, 0, h->stream>>>(h->P, h->s_pos[h->s_cur], h->s_cell, h->s_start,
-                                                                   h->f_posr[h->f_cur], h->f_velp[h->f_cur],
-                                                                   h->f_start, h->s_np, h->ns);
-    CK_LAUNCH();
-    h->launches++;
-    h->s_np_ok = true;
-    return FSIM_OK;
-}
-
-fsim_status enqueue_virt(fsim_sim *h)
-{
-    if (!h->nv) return FSIM_OK;
-    k_virt<<<blocks_for(h->nv, kBlock), kBlock, 0, h->stream>>>(h->P, h->v_posr, h->v_normal, h->v_cell,
-                                                                 h->f_posr[h->f_cur], h->f_velp[h->f_cur],
-                                                                 h->f_orig[h->f_cur], h->f_start, h->v_posr,
-                                                                 h->v_velp, h->nv);
-    CK_LAUNCH();
-    h->launches++;
-    return FSIM_OK;
-}
-
-fsim_status enqueue_fluid(fsim_sim *h)
-{
-    if (!h->nf) return FSIM_OK;
-    const int fo = h->f_cur ^ 1;
-    FluidSweepArgs A;
-    A.posr = h->f_posr[h->f_cur];
-    A.velp = h->f_velp[h->f_cur];
-    A.start_f = h->f_start;
-    A.cell_f = h->f_cell;
-    A.orig_in = h->f_orig[h->f_cur];
-    A.s_pos = h->s_pos[h->s_cur];
-    A.s_vel = h->s_vel[h->s_cur];
-    A.s_np = h->s_np;
-    A.start_s = h->s_start;
-    A.v_posr = h->v_posr;
-    A.v_velp = h->v_velp;
-    A.start_v = h->v_start;
-    A.posr_out = h->f_posr[fo];
-    A.velp_out = h->f_velp[fo];
-    A.orig_out = h->f_orig[fo];
-    A.drho_out = h->f_drho;
-    A.dudt_out = h->f_dudt;
-    A.n = h->nf;
-    const bool timed = h->instrument && (size_t)(2 * h->instr_step + 1) < h->sweep_events.size();
-    if (timed) CK(cudaEventRecord(h->sweep_events[2 * h->instr_step], h->stream));
-    const int gs = blocks_for(h->nf, kSweepWarps * 32);
-    using SweepFn = void (*)(const DevParams, const FluidSweepArgs);
-    static const SweepFn table[8] = {
-        k_fluid_sweep<false, false, false>, k_fluid_sweep<false, false, true>, k_fluid_sweep<false, true, false>,
-        k_fluid_sweep<false, true, true>,   k_fluid_sweep<true, false, false>,  k_fluid_sweep<true, false, true>,
-        k_fluid_sweep<true, true, false>,   k_fluid_sweep<true, true, true>};
-    table[(h->keep ? 4 : 0) + (h->check_z ? 2 : 0) + (h->P.viscid ? 1 : 0)]<<<gs, kSweepWarps * 32, 0, h->stream>>>(h->P, A);
-    CK_LAUNCH();
-    if (timed) CK(cudaEventRecord(h->sweep_events[2 * h->instr_step + 1], h->stream));
-    h->launches++;
-    h->f_cur = fo;
-    h->f_deriv_ok = h->keep;
-    return FSIM_OK;
-}
-
-SolidArgs solid_args(fsim_sim *h)
-{
-    SolidArgs S;
-    S.pos = h->s_pos[h->s_cur];
-    S.vel = h->s_vel[h->s_cur];
-    S.ref = h->s_ref[h->s_cur];
-    S.type = h->s_type[h->s_cur];
-    S.cell = h->s_cell;
-    S.start_s = h->s_start;
-    S.np = h->s_np;
-    S.F = h->s_F;
-    S.Pk = h->s_P;
-    S.L = h->s_L;
-    S.PL = h->s_PL;
-    S.AV = h->s_AV;
-    S.dudt = h->s_dudt;
-    S.couple = h->s_couple;
-    S.fposr = h->f_posr[h->f_cur];
-    S.fvelp = h->f_velp[h->f_cur];
-    S.start_f = h->f_start;
-    S.n = h->ns;
-    return S;
-}
-
-fsim_status enqueue_solid(fsim_sim *h)
-{
-    if (!h->ns) return FSIM_OK;
-    const SolidArgs S = solid_args(h);
-    const int g = blocks_for(h->ns, kBlock);
-    const int gw = blocks_for(32ll * h->ns, kBlock); // one warp per solid particle
-    for (int k = 0; k < h->cfg.solid_sub_step; ++k) {
-        k_solid_deform<<<gw, kBlock, 0, h->stream>>>(h->P, S);
-        CK_LAUNCH();
-        k_solid_force<<<gw, kBlock, 0, h->stream>>>(h->P, S);
-        CK_LAUNCH();
-        k_solid_update<<<g, kBlock, 0, h->stream>>>(h->P, S);
-        CK_LAUNCH();
-        h->launches += 3;
+    std::vector<Item<VirtArgs>> it;
+    std::vector<int> nb;
+    for (fsim_sim *h : m) {
+        it.push_back({h->P, VirtArgs{h->v_posr, h->v_normal, h->v_cell, h->f_posr[pf], h->f_velp[pf], h->f_orig[pf],
+                                     h->f_start, h->v_posr, h->v_velp, h->nv}});
+        nb.push_back(blocks_for(h->nv, kBlock));
     }
-    h->s_mech_ok = true;
+    add_launch(pl, ab, L_VIRT, it, nb);
+}
+
+// fluid sweep + update (parity pf -> 1-pf)
+void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
+{
+    std::vector<Item<FluidSweepArgs>> it;
+    std::vector<int> nb;
+    bool any_check = false;
+    int nvisc = 0;
+    for (fsim_sim *h : m) {
+        FluidSweepArgs A;
+        A.posr = h->f_posr[pf];
+        A.velp = h->f_velp[pf];
+        A.start_f = h->f_start;
+        A.cell_f = h->f_cell;
+        A.orig_in = h->f_orig[pf];
+        A.s_pos = h->s_pos[ps];
+        A.s_vel = h->s_vel[ps];
+        A.s_np = h->s_np;
+        A.start_s = h->s_start;
+        A.v_posr = h->v_posr;
+        A.v_velp = h->v_velp;
+        A.start_v = h->v_start;
+        A.posr_out = h->f_posr[1 - pf];
+        A.velp_out = h->f_velp[1 - pf];
+        A.orig_out = h->f_orig[1 - pf];
+        A.drho_out = h->f_drho;
+        A.dudt_out = h->f_dudt;
+        A.n = h->nf;
+        A.keep = h->keep ? 1 : 0;
+        it.push_back({h->P, A});
+        nb.push_back(blocks_for(h->nf, kSweepWarps * 32));
+        if (h->nf) {
+            any_check = any_check || h->check_z;
+            nvisc += h->P.viscid ? 1 : 0;
+        }
+    }
+    const int n_active = (int)std::count_if(m.begin(), m.end(), [](fsim_sim *h) { return h->nf > 0; });
+    const int visc_mode = nvisc == 0 ? 0 : nvisc == n_active ? 1 : 2;
+    const size_t before = pl.launches.size();
+    add_launch(pl, ab, L_SWEEP, it, nb, (any_check ? 3 : 0) + visc_mode);
+    if (pl.launches.size() > before) pl.sweep_index = (int)before;
+}
+
+// solid sub-steps (in place on parity ps; the fluid is read at parity pf)
+void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
+{
+    int max_sub = 0;
+    for (fsim_sim *h : m)
+        if (h->ns) max_sub = std::max(max_sub, h->cfg.solid_sub_step);
+    for (int k = 0; k < max_sub; ++k) {
+        std::vector<Item<SolidArgs>> it;
+        std::vector<int> wb, tb;
+        for (fsim_sim *h : m) {
+            SolidArgs S;
+            S.pos = h->s_pos[ps];
+            S.vel = h->s_vel[ps];
+            S.ref = h->s_ref[ps];
+            S.type = h->s_type[ps];
+            S.cell = h->s_cell;
+            S.start_s = h->s_start;
+            S.np = h->s_np;
+            S.F = h->s_F;
+            S.Pk = h->s_P;
+            S.L = h->s_L;
+            S.PL = h->s_PL;
+            S.AV = h->s_AV;
+            S.dudt = h->s_dudt;
+            S.couple = h->s_couple;
+            S.fposr = h->f_posr[pf];
+            S.fvelp = h->f_velp[pf];
+            S.start_f = h->f_start;
+            S.n = h->ns;
+            it.push_back({h->P, S});
+            const bool active = h->ns && k < h->cfg.solid_sub_step;
+            wb.push_back(active ? blocks_for(32ll * h->ns, kBlock) : 0);
+            tb.push_back(active ? blocks_for(h->ns, kBlock) : 0);
+        }
+        add_launch(pl, ab, L_DEFORM, it, wb);
+        add_launch(pl, ab, L_FORCE, it, wb);
+        add_launch(pl, ab, L_UPDATE, it, tb);
+    }
+}
+
+// phases: bit k = FSIM_PHASE k
+fsim_status build_plan(const std::vector<fsim_sim *> &m, unsigned phases, int pf, int ps, Plan **out)
+{
+    *out = nullptr;
+    auto *pl = new (std::nothrow) Plan;
+    if (!pl) return FSIM_ENOMEM;
+    pl->device = m.empty() ? 0 : m[0]->device;
+    pl->pf = pf;
+    pl->ps = ps;
+    ArenaBuilder ab;
+    if (phases & (1u << FSIM_PHASE_CELL)) {
+        plan_cell(*pl, ab, m, pf, ps);
+        pf ^= 1;
+        ps ^= 1;
+    }
+    if (phases & (1u << FSIM_PHASE_COUPLE)) plan_couple(*pl, ab, m, pf, ps);
+    if (phases & (1u << FSIM_PHASE_VIRT)) plan_virt(*pl, ab, m, pf);
+    if (phases & (1u << FSIM_PHASE_FLUID)) {
+        plan_fluid(*pl, ab, m, pf, ps);
+        pf ^= 1;
+    }
+    if (phases & (1u << FSIM_PHASE_SOLID)) plan_solid(*pl, ab, m, pf, ps);
+    pl->pf_after = pf;
+    pl->ps_after = ps;
+    pl->host = ab.bytes;
+    if (!ab.bytes.empty()) {
+        cudaError_t e = cudaMalloc((void **)&pl->arena, ab.bytes.size());
+        if (e == cudaSuccess) e = cudaMemcpy(pl->arena, ab.bytes.data(), ab.bytes.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            fsim_set_error("plan upload failed: %s", cudaGetErrorString(e));
+            free_plan(pl);
+            return FSIM_ENOMEM;
+        }
+    }
+    *out = pl;
     return FSIM_OK;
 }
 
-// DeviceCalculation::calculation loop body (src/calculation.cu:23-33)
-fsim_status enqueue_step(fsim_sim *h)
+template <class Args>
+const Item<Args> *items_of(const Plan &pl, const Launch &L)
 {
-    fsim_status st;
-    if ((st = enqueue_cell_phase(h))) return st;
-    if ((st = enqueue_couple(h))) return st;
-    if ((st = enqueue_virt(h))) return st;
-    if ((st = enqueue_fluid(h))) return st;
-    if ((st = enqueue_solid(h))) return st;
+    return reinterpret_cast<const Item<Args> *>(pl.arena + L.items_off);
+}
+template <class Args>
+const Item<Args> &host_item(const Plan &pl, const Launch &L)
+{
+    return *reinterpret_cast<const Item<Args> *>(pl.host.data() + L.items_off);
+}
+
+#define FSIM_LAUNCH(KB, ARGS, THREADS) KB<<<g, THREADS, 0, st>>>(items_of<ARGS>(pl, L), tb, n)
+
+// Enqueue a plan's launches; optional events around the fluid sweep.
+fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, cudaEvent_t sweep0 = nullptr, cudaEvent_t sweep1 = nullptr)
+{
+    using SweepFn = void (*)(const Item<FluidSweepArgs> *, const int *, int);
+    using Sweep1Fn = void (*)(const DevParams, const FluidSweepArgs);
+    static const SweepFn sweeps[6] = {kb_fluid_sweep<false, 0>, kb_fluid_sweep<false, 1>, kb_fluid_sweep<false, 2>,
+                                      kb_fluid_sweep<true, 0>,  kb_fluid_sweep<true, 1>,  kb_fluid_sweep<true, 2>};
+    static const Sweep1Fn sweeps1[6] = {kb_fluid_sweep_1<false, 0>, kb_fluid_sweep_1<false, 1>,
+                                        kb_fluid_sweep_1<false, 2>, kb_fluid_sweep_1<true, 0>,
+                                        kb_fluid_sweep_1<true, 1>,  kb_fluid_sweep_1<true, 2>};
+    for (size_t k = 0; k < pl.launches.size(); ++k) {
+        const Launch &L = pl.launches[k];
+        const int *tb = reinterpret_cast<const int *>(pl.arena + L.table_off);
+        const int g = L.blocks, n = L.ninst;
+        switch (L.kind) {
+        case L_ZERO: FSIM_LAUNCH(kb_zero, ZeroArgs, kBlock); break;
+        case L_HASH: FSIM_LAUNCH(kb_hash, HashArgs, kBlock); break;
+        case L_SCAN_REDUCE: FSIM_LAUNCH(kb_scan_reduce, ScanArgs, kScanThreads); break;
+        case L_SCAN_PARTIALS: FSIM_LAUNCH(kb_scan_partials, ScanArgs, kScanThreads); break;
+        case L_SCAN_APPLY: FSIM_LAUNCH(kb_scan_apply, ScanArgs, kScanThreads); break;
+        case L_SCATTER: FSIM_LAUNCH(kb_scatter, ScatterArgs, kBlock); break;
+        case L_GATHER_F: FSIM_LAUNCH(kb_gather_fluid, GatherFluidArgs, kBlock); break;
+        case L_GATHER_S: FSIM_LAUNCH(kb_gather_solid, GatherSolidArgs, kBlock); break;
+        case L_COUPLE: FSIM_LAUNCH(kb_couple, CoupleArgs, kBlock); break;
+        case L_VIRT: FSIM_LAUNCH(kb_virt, VirtArgs, kBlock); break;
+        case L_SWEEP:
+            if (sweep0) CK(cudaEventRecord(sweep0, st));
+            if (n == 1) {
+                const Item<FluidSweepArgs> &it = host_item<FluidSweepArgs>(pl, L);
+                sweeps1[L.variant]<<<g, kSweepWarps * 32, 0, st>>>(it.P, it.A);
+            } else {
+                sweeps[L.variant]<<<g, kSweepWarps * 32, 0, st>>>(items_of<FluidSweepArgs>(pl, L), tb, n);
+            }
+            CK_LAUNCH();
+            if (sweep1) CK(cudaEventRecord(sweep1, st));
+            break;
+        case L_DEFORM: FSIM_LAUNCH(kb_solid_deform, SolidArgs, kBlock); break;
+        case L_FORCE: FSIM_LAUNCH(kb_solid_force, SolidArgs, kBlock); break;
+        case L_UPDATE: FSIM_LAUNCH(kb_solid_update, SolidArgs, kBlock); break;
+        default: fsim_set_error("unknown launch kind"); return FSIM_EINVAL;
+        }
+        CK_LAUNCH();
+    }
+    return FSIM_OK;
+}
+
+fsim_status capture_plan(Plan &pl, cudaStream_t st)
+{
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    fsim_status s = enqueue_plan(pl, st);
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (s) {
+        if (graph) cudaGraphDestroy(graph);
+        return s;
+    }
+    if (e != cudaSuccess) {
+        fsim_set_error("stream capture failed: %s", cudaGetErrorString(e));
+        return FSIM_ECUDA;
+    }
+    e = cudaGraphInstantiate(&pl.graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        pl.graph = nullptr;
+        fsim_set_error("graph instantiate failed: %s", cudaGetErrorString(e));
+        return FSIM_ECUDA;
+    }
+    return FSIM_OK;
+}
+
+// Validity bookkeeping after a plan ran on an instance.
+void after_plan(fsim_sim *h, unsigned phases, const Plan &pl)
+{
+    h->f_cur = pl.pf_after;
+    h->s_cur = pl.ps_after;
+    if (phases & (1u << FSIM_PHASE_CELL)) {
+        h->f_sorted = h->s_sorted = true;
+        h->f_deriv_ok = h->s_np_ok = h->s_mech_ok = false;
+    }
+    if ((phases & (1u << FSIM_PHASE_COUPLE)) && h->nf && h->ns) h->s_np_ok = true;
+    if (phases & (1u << FSIM_PHASE_FLUID)) h->f_deriv_ok = h->keep && h->nf > 0;
+    if ((phases & (1u << FSIM_PHASE_SOLID)) && h->ns) h->s_mech_ok = true;
+}
+
+constexpr unsigned kAllPhases = 0x1fu;
+
+fsim_status handle_step_plan(fsim_sim *h, Plan **out)
+{
+    Plan *&pl = h->step_plans[h->f_cur][h->s_cur];
+    if (!pl) {
+        fsim_status st = build_plan({h}, kAllPhases, h->f_cur, h->s_cur, &pl);
+        if (st) return st;
+    }
+    *out = pl;
     return FSIM_OK;
 }
 
 fsim_status run_step_graph(fsim_sim *h)
 {
-    GraphEntry &g = h->graphs[h->f_cur][h->s_cur];
-    if (!g.exec) {
-        const int f0 = h->f_cur, s0 = h->s_cur;
-        cudaGraph_t graph = nullptr;
-        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        h->launches = 0;
-        fsim_status st = enqueue_step(h);
-        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
-        if (st) {
-            if (graph) cudaGraphDestroy(graph);
-            h->f_cur = f0;
-            h->s_cur = s0;
-            return st;
-        }
-        if (e != cudaSuccess) {
-            fsim_set_error("stream capture failed: %s", cudaGetErrorString(e));
-            h->f_cur = f0;
-            h->s_cur = s0;
-            return FSIM_ECUDA;
-        }
-        e = cudaGraphInstantiate(&g.exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) {
-            g.exec = nullptr;
-            fsim_set_error("graph instantiate failed: %s", cudaGetErrorString(e));
-            h->f_cur = f0;
-            h->s_cur = s0;
-            return FSIM_ECUDA;
-        }
-        g.f_after = h->f_cur;
-        g.s_after = h->s_cur;
-        h->f_cur = f0;
-        h->s_cur = s0;
-    }
-    CK(cudaGraphLaunch(g.exec, h->stream));
-    h->f_cur = g.f_after;
-    h->s_cur = g.s_after;
-    h->f_sorted = h->s_sorted = true;
-    h->f_deriv_ok = h->keep && h->nf > 0;
-    h->s_np_ok = h->ns > 0 && h->nf > 0;
-    h->s_mech_ok = h->ns > 0;
+    Plan *pl = nullptr;
+    fsim_status st = handle_step_plan(h, &pl);
+    if (st) return st;
+    if (!pl->graph && (st = capture_plan(*pl, h->stream))) return st;
+    CK(cudaGraphLaunch(pl->graph, h->stream));
+    after_plan(h, kAllPhases, *pl);
     return FSIM_OK;
 }
 
@@ -1381,6 +1630,8 @@ fsim_status check_flags(fsim_sim *h)
     return FSIM_OK;
 }
 
+void batch_wait(fsim_sim *h);
+
 struct DeviceGuard {
     int prev = -1;
     explicit DeviceGuard(int dev)
@@ -1394,7 +1645,8 @@ struct DeviceGuard {
     }
 };
 
-// counting-sort the virtual particles once (walls are static)
+// counting-sort the virtual particles once (walls are static), with the same
+// batched sort kernels run as a one-instance plan over temporary arrays
 fsim_status sort_virtual(fsim_sim *h, const float *vpos_host)
 {
     const int n = h->nv;
@@ -1409,20 +1661,42 @@ fsim_status sort_virtual(fsim_sim *h, const float *vpos_host)
     CK(cudaMemcpyAsync(d_xyz, vpos_host, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, h->stream));
     k_pack_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(d_xyz, nullptr, n, h->P.rho0, tmp_pos);
     k_iota<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(orig0, n);
-    CK(cudaMemsetAsync(cnt, 0, sizeof(int) * h->ncell, h->stream));
-    k_hash<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(h->P, tmp_pos, n, key, slot, cnt, h->d_flags);
     CK_LAUNCH();
-    if ((st = enqueue_scan(h, cnt, h->v_start, nullptr, nullptr))) return st;
-    k_scatter<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(key, slot, h->v_start, tmp, n);
-    // reuse the fluid gather (posr) with a dummy velocity stream
-    k_gather_fluid<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(tmp, key, h->v_start, n, tmp_pos, tmp_pos, orig0,
-                                                                     h->v_posr, h->v_velp, h->v_orig, h->v_cell);
-    CK_LAUNCH();
-    CK(cudaMemsetAsync(h->v_velp, 0, sizeof(float4) * n, h->stream));
-    k_virt_normal<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(h->P, h->v_posr, h->v_cell, h->v_start,
-                                                                    h->v_normal, n);
-    CK_LAUNCH();
-    CK(cudaStreamSynchronize(h->stream));
+    Plan pl;
+    ArenaBuilder ab;
+    add_launch(pl, ab, L_ZERO, std::vector<Item<ZeroArgs>>{{h->P, ZeroArgs{cnt, h->ncell}}},
+               {blocks_for(h->ncell, kBlock)});
+    add_launch(pl, ab, L_HASH, std::vector<Item<HashArgs>>{{h->P, HashArgs{tmp_pos, n, key, slot, cnt, h->d_flags}}},
+               {blocks_for(n, kBlock)});
+    const std::vector<Item<ScanArgs>> sc{{h->P, ScanArgs{cnt, h->v_start, h->ncell, h->scan_partials}}};
+    add_launch(pl, ab, L_SCAN_REDUCE, sc, {blocks_for(h->ncell, kScanTile)});
+    add_launch(pl, ab, L_SCAN_PARTIALS, sc, {1});
+    add_launch(pl, ab, L_SCAN_APPLY, sc, {blocks_for(h->ncell, kScanTile)});
+    add_launch(pl, ab, L_SCATTER, std::vector<Item<ScatterArgs>>{{h->P, ScatterArgs{key, slot, h->v_start, tmp, n}}},
+               {blocks_for(n, kBlock)});
+    // the fluid gather with a dummy velocity stream
+    add_launch(pl, ab, L_GATHER_F,
+               std::vector<Item<GatherFluidArgs>>{{h->P, GatherFluidArgs{tmp, key, h->v_start, n, tmp_pos, tmp_pos,
+                                                                         orig0, h->v_posr, h->v_velp, h->v_orig,
+                                                                         h->v_cell}}},
+               {blocks_for(n, kBlock)});
+    pl.host = ab.bytes;
+    CK(cudaMalloc((void **)&pl.arena, ab.bytes.size()));
+    cudaError_t e = cudaMemcpy(pl.arena, ab.bytes.data(), ab.bytes.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && (st = enqueue_plan(pl, h->stream)) == FSIM_OK) {
+        e = cudaMemsetAsync(h->v_velp, 0, sizeof(float4) * n, h->stream);
+        k_virt_normal<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(h->P, h->v_posr, h->v_cell, h->v_start,
+                                                                        h->v_normal, n);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    }
+    cudaFree(pl.arena);
+    pl.arena = nullptr;
+    if (e != cudaSuccess) {
+        fsim_set_error("sorting the wall particles failed: %s", cudaGetErrorString(e));
+        return FSIM_ECUDA;
+    }
+    if (st) return st;
     // temporaries are released now
     void *tmps[] = {d_xyz, tmp_pos, key, slot, tmp, cnt, orig0};
     for (void *p : tmps) {
@@ -1601,6 +1875,10 @@ extern "C" fsim_status fsim_create(const fsim_config *cfg, const fsim_particles 
 extern "C" fsim_status fsim_destroy(fsim_handle h)
 {
     if (!h) return FSIM_OK;
+    if (h->batch) {
+        fsim_set_error("destroy the batch before its members");
+        return FSIM_EINVAL;
+    }
     DeviceGuard guard(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_all(h);
@@ -1611,6 +1889,10 @@ extern "C" fsim_status fsim_destroy(fsim_handle h)
 extern "C" fsim_status fsim_step(fsim_handle h, int nsteps)
 {
     if (!h || nsteps < 0) return FSIM_EINVAL;
+    if (h->batch) {
+        fsim_set_error("the handle belongs to a batch; step it through the batch");
+        return FSIM_EINVAL;
+    }
     DeviceGuard guard(h->device);
     for (int k = 0; k < nsteps; ++k) {
         fsim_status st = run_step_graph(h);
@@ -1622,6 +1904,7 @@ extern "C" fsim_status fsim_step(fsim_handle h, int nsteps)
 extern "C" fsim_status fsim_sync(fsim_handle h)
 {
     if (!h) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
     DeviceGuard guard(h->device);
     CK(cudaStreamSynchronize(h->stream));
     return check_flags(h);
@@ -1630,24 +1913,28 @@ extern "C" fsim_status fsim_sync(fsim_handle h)
 extern "C" fsim_status fsim_run_phase(fsim_handle h, int phase)
 {
     if (!h) return FSIM_EINVAL;
-    DeviceGuard guard(h->device);
-    h->launches = 0;
-    switch (phase) {
-    case FSIM_PHASE_CELL: return enqueue_cell_phase(h);
-    case FSIM_PHASE_COUPLE:
-    case FSIM_PHASE_VIRT:
-    case FSIM_PHASE_FLUID:
-    case FSIM_PHASE_SOLID:
-        if (!h->f_sorted || !h->s_sorted) {
-            fsim_set_error("run FSIM_PHASE_CELL first");
-            return FSIM_EINVAL;
-        }
-        if (phase == FSIM_PHASE_COUPLE) return enqueue_couple(h);
-        if (phase == FSIM_PHASE_VIRT) return enqueue_virt(h);
-        if (phase == FSIM_PHASE_FLUID) return enqueue_fluid(h);
-        return enqueue_solid(h);
-    default: fsim_set_error("unknown phase %d", phase); return FSIM_EINVAL;
+    if (phase < FSIM_PHASE_CELL || phase > FSIM_PHASE_SOLID) {
+        fsim_set_error("unknown phase %d", phase);
+        return FSIM_EINVAL;
     }
+    if (phase != FSIM_PHASE_CELL && (!h->f_sorted || !h->s_sorted)) {
+        fsim_set_error("run FSIM_PHASE_CELL first");
+        return FSIM_EINVAL;
+    }
+    if (h->batch) {
+        fsim_set_error("the handle belongs to a batch; step it through the batch");
+        return FSIM_EINVAL;
+    }
+    DeviceGuard guard(h->device);
+    Plan *&pl = h->phase_plans[phase][h->f_cur][h->s_cur];
+    if (!pl) {
+        fsim_status st = build_plan({h}, 1u << phase, h->f_cur, h->s_cur, &pl);
+        if (st) return st;
+    }
+    fsim_status st = enqueue_plan(*pl, h->stream);
+    if (st) return st;
+    after_plan(h, 1u << phase, *pl);
+    return FSIM_OK;
 }
 
 extern "C" int fsim_field_width(int field)
@@ -1678,6 +1965,7 @@ static int field_count(fsim_sim *h, int field)
 extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_t bytes)
 {
     if (!h || (!dst && bytes)) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
     const int width = fsim_field_width(field);
     if (!width) {
         fsim_set_error("unknown field %d", field);
@@ -1777,6 +2065,7 @@ extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_
 extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src, size_t bytes)
 {
     if (!h || (!src && bytes)) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
     const int width = fsim_field_width(field);
     const int n = field_count(h, field);
     float4 *dst = nullptr;
@@ -1802,6 +2091,7 @@ extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src,
     k_permute_in_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(dst, orig, n, comp, width,
                                                                       (const float *)h->staging);
     CK_LAUNCH();
+    if (h->batch) CK(cudaStreamSynchronize(h->stream)); // the batch stream must see it
     // positions changed: derived per-step products are stale until the next phases
     return FSIM_OK;
 }
@@ -1809,6 +2099,7 @@ extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src,
 extern "C" fsim_status fsim_neighbor_counts(fsim_handle h, int *out, size_t bytes)
 {
     if (!h || (!out && bytes)) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
     if (bytes != (size_t)h->nf * 3 * 4) {
         fsim_set_error("neighbor counts need %zu bytes", (size_t)h->nf * 12);
         return FSIM_EINVAL;
@@ -1839,6 +2130,7 @@ extern "C" fsim_status fsim_get_cells(fsim_handle h, int species, int *cell_star
                                       size_t ids_bytes)
 {
     if (!h || species < 0 || species > 2) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
     const int n = species == 0 ? h->nf : species == 1 ? h->ns : h->nv;
     if (start_bytes != (size_t)(h->ncell + 1) * 4 || ids_bytes != (size_t)n * 4 || !cell_start || (n && !ids)) {
         fsim_set_error("fsim_get_cells: wrong buffer sizes");
@@ -1901,6 +2193,10 @@ extern "C" fsim_status fsim_write_vtk(fsim_handle h, const char *out_dir, int fi
 extern "C" fsim_status fsim_time_steps(fsim_handle h, int nsteps, float *ms)
 {
     if (!h || nsteps < 0 || !ms) return FSIM_EINVAL;
+    if (h->batch) {
+        fsim_set_error("the handle belongs to a batch; time the batch");
+        return FSIM_EINVAL;
+    }
     DeviceGuard guard(h->device);
     // capture outside the timed region
     fsim_status st;
@@ -1916,6 +2212,10 @@ extern "C" fsim_status fsim_time_steps(fsim_handle h, int nsteps, float *ms)
 extern "C" fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_ms, float *sweep_ms)
 {
     if (!h || nsteps < 0 || !total_ms || !sweep_ms) return FSIM_EINVAL;
+    if (h->batch) {
+        fsim_set_error("the handle belongs to a batch; time the batch");
+        return FSIM_EINVAL;
+    }
     DeviceGuard guard(h->device);
     while ((int)h->sweep_events.size() < 2 * nsteps) {
         cudaEvent_t e;
@@ -1924,14 +2224,12 @@ extern "C" fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_m
     }
     fsim_status st = FSIM_OK;
     CK(cudaEventRecord(h->ev0, h->stream));
-    h->instrument = true;
-    for (int k = 0; k < nsteps && !st; ++k) {
-        h->instr_step = k;
-        h->launches = 0;
-        st = enqueue_step(h);
+    for (int k = 0; k < nsteps; ++k) {
+        Plan *pl = nullptr;
+        if ((st = handle_step_plan(h, &pl))) return st;
+        if ((st = enqueue_plan(*pl, h->stream, h->sweep_events[2 * k], h->sweep_events[2 * k + 1]))) return st;
+        after_plan(h, kAllPhases, *pl);
     }
-    h->instrument = false;
-    if (st) return st;
     CK(cudaEventRecord(h->ev1, h->stream));
     CK(cudaEventSynchronize(h->ev1));
     CK(cudaEventElapsedTime(total_ms, h->ev0, h->ev1));
@@ -1950,16 +2248,11 @@ extern "C" fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_m
 extern "C" fsim_status fsim_launches_per_step(fsim_handle h, int *n)
 {
     if (!h || !n) return FSIM_EINVAL;
-    // count by enqueuing nothing: the formula mirrors enqueue_step
-    int c = 0;
-    if (h->nf) c += 1 + 2;                  // hash, scatter, gather
-    if (h->ns) c += 1 + 2;
-    if (h->nf || h->ns) c += 3;             // scan
-    if (h->nf && h->ns) c += 1;             // couple
-    if (h->nv) c += 1;                      // virtual
-    if (h->nf) c += 1;                      // fluid sweep
-    if (h->ns) c += 3 * h->cfg.solid_sub_step;
-    *n = c;
+    DeviceGuard guard(h->device);
+    Plan *pl = nullptr;
+    fsim_status st = handle_step_plan(h, &pl);
+    if (st) return st;
+    *n = (int)pl->launches.size();
     return FSIM_OK;
 }
 
@@ -1995,5 +2288,187 @@ extern "C" fsim_status fsim_host_alloc(size_t bytes, void **out)
 extern "C" fsim_status fsim_host_free(void *p)
 {
     if (p) cudaFreeHost(p);
+    return FSIM_OK;
+}
+
+// =================================================================== batches
+struct fsim_batch;
+namespace {
+} // namespace
+struct fsim_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<fsim_sim *> members;
+    Plan *plans[2][2] = {}; // by (fluid, solid) parity of the members
+};
+
+namespace {
+
+void batch_wait(fsim_sim *h) { cudaStreamSynchronize(h->batch->stream); }
+
+// Bring a member to buffer parities (pf, ps) by copying its current state
+// into the other buffers (same order, so cell structures stay valid).
+fsim_status set_parity(fsim_sim *h, int pf, int ps)
+{
+    if (h->f_cur != pf && h->nf) {
+        const int a = h->f_cur, b = pf;
+        CK(cudaMemcpyAsync(h->f_posr[b], h->f_posr[a], sizeof(float4) * h->nf, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->f_velp[b], h->f_velp[a], sizeof(float4) * h->nf, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->f_orig[b], h->f_orig[a], sizeof(int) * h->nf, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    h->f_cur = pf;
+    if (h->s_cur != ps && h->ns) {
+        const int a = h->s_cur, b = ps;
+        CK(cudaMemcpyAsync(h->s_pos[b], h->s_pos[a], sizeof(float4) * h->ns, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->s_vel[b], h->s_vel[a], sizeof(float4) * h->ns, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->s_ref[b], h->s_ref[a], sizeof(float4) * h->ns, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->s_type[b], h->s_type[a], sizeof(int) * h->ns, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->s_orig[b], h->s_orig[a], sizeof(int) * h->ns, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    h->s_cur = ps;
+    CK(cudaStreamSynchronize(h->stream));
+    return FSIM_OK;
+}
+
+void free_batch(fsim_batch *b)
+{
+    for (auto &row : b->plans)
+        for (Plan *&pl : row) {
+            free_plan(pl);
+            pl = nullptr;
+        }
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+fsim_status batch_step_once(fsim_batch *b)
+{
+    const int pf = b->members[0]->f_cur, ps = b->members[0]->s_cur;
+    Plan *&pl = b->plans[pf][ps];
+    if (!pl) {
+        fsim_status st = build_plan(b->members, kAllPhases, pf, ps, &pl);
+        if (st) return st;
+    }
+    if (!pl->graph) {
+        fsim_status st = capture_plan(*pl, b->stream);
+        if (st) return st;
+    }
+    CK(cudaGraphLaunch(pl->graph, b->stream));
+    for (fsim_sim *h : b->members) after_plan(h, kAllPhases, *pl);
+    return FSIM_OK;
+}
+
+fsim_status batch_check_flags(fsim_batch *b)
+{
+    CK(cudaStreamSynchronize(b->stream));
+    fsim_status worst = FSIM_OK;
+    for (fsim_sim *h : b->members) {
+        fsim_status st = check_flags(h);
+        if (st && !worst) worst = st;
+    }
+    return worst;
+}
+
+} // namespace
+
+extern "C" fsim_status fsim_batch_create(fsim_handle *members, int n, fsim_batch_t *out)
+{
+    if (!members || n < 1 || !out) return FSIM_EINVAL;
+    *out = nullptr;
+    for (int k = 0; k < n; ++k) {
+        if (!members[k] || members[k]->batch || members[k]->device != members[0]->device) {
+            fsim_set_error("batch members must be distinct standalone handles on one device");
+            return FSIM_EINVAL;
+        }
+        for (int j = 0; j < k; ++j)
+            if (members[j] == members[k]) {
+                fsim_set_error("a handle appears twice in the batch");
+                return FSIM_EINVAL;
+            }
+    }
+    auto *b = new (std::nothrow) fsim_batch;
+    if (!b) return FSIM_ENOMEM;
+    b->device = members[0]->device;
+    DeviceGuard guard(b->device);
+    fsim_status st = FSIM_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+    if (e != cudaSuccess) {
+        fsim_set_error("batch stream/event creation failed: %s", cudaGetErrorString(e));
+        free_batch(b);
+        delete b;
+        return FSIM_ECUDA;
+    }
+    const int ps = members[0]->s_cur;
+    for (int k = 0; k < n && !st; ++k) st = set_parity(members[k], 0, ps);
+    if (st) {
+        free_batch(b);
+        delete b;
+        return st;
+    }
+    b->members.assign(members, members + n);
+    for (fsim_sim *h : b->members) h->batch = b;
+    *out = b;
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_batch_step(fsim_batch_t b, int nsteps)
+{
+    if (!b || nsteps < 0) return FSIM_EINVAL;
+    DeviceGuard guard(b->device);
+    for (int k = 0; k < nsteps; ++k) {
+        fsim_status st = batch_step_once(b);
+        if (st) return st;
+    }
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_batch_sync(fsim_batch_t b)
+{
+    if (!b) return FSIM_EINVAL;
+    DeviceGuard guard(b->device);
+    return batch_check_flags(b);
+}
+
+extern "C" fsim_status fsim_batch_time_steps(fsim_batch_t b, int nsteps, float *ms)
+{
+    if (!b || nsteps < 0 || !ms) return FSIM_EINVAL;
+    DeviceGuard guard(b->device);
+    CK(cudaEventRecord(b->ev0, b->stream));
+    for (int k = 0; k < nsteps; ++k) {
+        fsim_status st = batch_step_once(b);
+        if (st) return st;
+    }
+    CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaEventSynchronize(b->ev1));
+    CK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+    return batch_check_flags(b);
+}
+
+extern "C" fsim_status fsim_batch_launches_per_step(fsim_batch_t b, int *n)
+{
+    if (!b || !n) return FSIM_EINVAL;
+    DeviceGuard guard(b->device);
+    const int pf = b->members[0]->f_cur, ps = b->members[0]->s_cur;
+    Plan *&pl = b->plans[pf][ps];
+    if (!pl) {
+        fsim_status st = build_plan(b->members, kAllPhases, pf, ps, &pl);
+        if (st) return st;
+    }
+    *n = (int)pl->launches.size();
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_batch_destroy(fsim_batch_t b)
+{
+    if (!b) return FSIM_OK;
+    DeviceGuard guard(b->device);
+    cudaStreamSynchronize(b->stream);
+    for (fsim_sim *h : b->members) h->batch = nullptr;
+    free_batch(b);
+    delete b;
     return FSIM_OK;
 }

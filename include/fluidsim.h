@@ -239,6 +239,28 @@ fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_ms, float *s
 /* Kernel launches one fsim_step(h, 1) issues (for launch accounting). */
 fsim_status fsim_launches_per_step(fsim_handle h, int *n);
 
+/* -------------------------------------------------------------- batching */
+/* A batch advances several independent instances (handles created with
+ * fsim_create on the same device, of any sizes and parameters) in lockstep:
+ * every kernel of a step is launched once for the whole batch, and a batched
+ * step is one CUDA graph.  The reference runs one instance per process
+ * (src/main.cu:17-30); this has no reference counterpart and exists for
+ * ensembles of small and medium instances, whose one-by-one steps would
+ * leave most of the GPU idle.  While a handle belongs to a batch it is stepped
+ * only through the batch; its field getters and setters wait for the batch.
+ * Each member's results equal its standalone results bit for bit. */
+typedef struct fsim_batch *fsim_batch_t;
+fsim_status fsim_batch_create(fsim_handle *members, int n, fsim_batch_t *out);
+/* Enqueue nsteps batched steps on the batch's stream. */
+fsim_status fsim_batch_step(fsim_batch_t b, int nsteps);
+fsim_status fsim_batch_sync(fsim_batch_t b);
+/* Device time of nsteps batched steps (CUDA events on the batch's stream). */
+fsim_status fsim_batch_time_steps(fsim_batch_t b, int nsteps, float *ms);
+/* Kernel launches of one batched step. */
+fsim_status fsim_batch_launches_per_step(fsim_batch_t b, int *n);
+/* Dissolve the batch; the members continue as standalone handles. */
+fsim_status fsim_batch_destroy(fsim_batch_t b);
+
 /* Pinned (page-locked) host memory for fast host<->device field copies. */
 fsim_status fsim_host_alloc(size_t bytes, void **out);
 fsim_status fsim_host_free(void *p);

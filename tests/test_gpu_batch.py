@@ -1,0 +1,90 @@
+"""Batched instances (fsim_batch_*): every member's result equals its
+standalone result bit for bit, whatever else is in the batch."""
+import numpy as np
+import pytest
+
+from fluidsim_gb300 import api, cases
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("fluid_pos", "fluid_vel", "fluid_rho", "fluid_p", "solid_pos", "solid_vel", "solid_PK1", "virt_p",
+          "solid_normal")
+
+
+def _members():
+    """Instances that differ in size, viscosity, solid and sub-steps."""
+    specs = [
+        cases.tiny_box(jitter=0.01, seed=1),
+        cases.tiny_box(jitter=0.02, seed=2, with_solid=False, viscid=False, fluid=(8, 6, 9)),
+        cases.tiny_box(jitter=0.01, seed=3, fluid=(14, 12, 10), tank=(30, 18, 16)),
+    ]
+    specs[2][0].solid_sub_step = 6
+    specs[2][0].youngs_modulus = 3e5
+    return [cases.make(s) for s in specs]
+
+
+def _fields(sim):
+    out = {}
+    for f in FIELDS:
+        if f.startswith("solid") and sim.n["solid"] == 0:
+            continue
+        out[f] = sim.get(f)
+    return out
+
+
+@pytest.mark.parametrize("steps", [1, 7])
+def test_batch_members_equal_standalone(steps):
+    members = _members()
+    alone = []
+    for cfg, pa in members:
+        with api.Simulation(cfg, pa, device=0) as s:
+            s.step(steps)
+            s.sync()
+            alone.append(_fields(s))
+    sims = [api.Simulation(cfg, pa, device=0) for cfg, pa in members]
+    with api.Batch(sims) as b:
+        b.step(steps)
+        b.sync()
+        assert b.launches_per_step() <= 14 + 3 * 6
+        batched = [_fields(s) for s in sims]
+    for k, (a, c) in enumerate(zip(alone, batched)):
+        for f in a:
+            assert np.array_equal(a[f], c[f]), (k, f)
+    # dissolved: the members continue standalone
+    for s in sims:
+        s.step(1)
+        s.sync()
+        s.close()
+
+
+def test_batch_rejects_misuse():
+    (cfg, pa), = _members()[:1]
+    s = api.Simulation(cfg, pa, device=0)
+    with api.Batch([s]) as b:
+        with pytest.raises(api.FsimError):
+            s.step(1)  # members are stepped through the batch
+        with pytest.raises(api.FsimError):
+            api.Batch([s])  # already in a batch
+        b.step(2)
+        assert np.isfinite(s.get("fluid_pos")).all()  # getters wait for the batch
+    s.close()
+
+
+def test_batch_after_phase_calls_normalises_parity():
+    """A member whose buffers were left at the other parity by phase calls
+    joins the batch and still matches its standalone continuation."""
+    (cfg, pa), = _members()[:1]
+    ref = api.Simulation(cfg, pa, device=0)
+    s = api.Simulation(cfg, pa, device=0)
+    # a lone cell phase leaves both fluid and solid at the other buffer
+    ref.phase(api.PHASE_CELL)
+    s.phase(api.PHASE_CELL)
+    ref.step(3)
+    ref.sync()
+    with api.Batch([s]) as b:
+        b.step(3)
+        b.sync()
+    for f in ("fluid_pos", "fluid_vel", "solid_pos"):
+        assert np.array_equal(ref.get(f), s.get(f)), f
+    ref.close()
+    s.close()
