@@ -273,7 +273,7 @@ def run_gb300(args, dist):
     # ---- the batched form on the ensemble workload
     forms = None
     if not args.no_forms:
-        forms = {"ensemble64": run_ensemble(dev, max(10, min(args.steps, 50)))}
+        forms = {"ensemble64": run_ensemble(dev, max(10, min(args.steps, 50))), "served": run_served(dev)}
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
@@ -338,6 +338,26 @@ def run_ensemble(dev, steps):
         "unit": "particle-updates/s",
         "batched_launches_per_step": launches,
     }
+
+
+def run_served(dev):
+    """BASELINE config 4, shortened: a seeded Poisson stream (20 requests/s) of
+    config-3-style scenarios served with continuous batching under a 150 GB
+    budget, and the same stream served one request at a time."""
+    from fluidsim_gb300 import serve
+
+    spec = dict(n=40, rate=20.0, seed=7, fluid_range=(10_000, 300_000), solid_range=(1_000, 27_000),
+                steps_range=(100, 400))
+    batched = serve.Server(budget_bytes=150 * 2 ** 30, backend=serve.GpuBackend(dev), quantum=10).run(
+        serve.poisson_stream(**spec))
+    plain = serve.serve_one_by_one(serve.poisson_stream(**spec), device=dev)
+    return {"workload": "Poisson stream, %d requests at %g/s (seed 7), fluid %d-%d log-uniform, solid %d-%d, "
+                        "steps %d-%d uniform, dx=0.01; shortened from 2000 requests of 10k-1M fluid and "
+                        "200-2000 steps" % (spec["n"], spec["rate"], spec["fluid_range"][0], spec["fluid_range"][1],
+                                            spec["solid_range"][0], spec["solid_range"][1], spec["steps_range"][0],
+                                            spec["steps_range"][1]),
+            "served": batched, "one_by_one": plain,
+            "throughput_ratio": batched["throughput"] / plain["throughput"]}
 
 
 def run_profile(args):

@@ -150,6 +150,7 @@ def load():
         "fsim_batch_time_steps": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
         "fsim_batch_launches_per_step": (C.c_int, [P, C.POINTER(C.c_int)]),
         "fsim_batch_destroy": (C.c_int, [P]),
+        "fsim_estimate_bytes": (C.c_int, [C.POINTER(Config), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_size_t)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -167,7 +168,7 @@ EXPORTED = [
     "fsim_neighbor_counts", "fsim_get_cells", "fsim_write_vtk", "fsim_time_steps", "fsim_time_sweep",
     "fsim_launches_per_step", "fsim_host_alloc", "fsim_host_free", "fsim_counts", "fsim_get_derived",
     "fsim_cell_sort_noalloc", "fsim_batch_create", "fsim_batch_step", "fsim_batch_sync", "fsim_batch_time_steps",
-    "fsim_batch_launches_per_step", "fsim_batch_destroy",
+    "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes",
 ]
 
 
@@ -199,6 +200,12 @@ def config_from_ini(path):
     cfg = Config()
     check(load().fsim_config_from_ini(os.fsencode(path), C.byref(cfg)))
     return cfg
+
+
+def estimate_bytes(cfg, n_fluid, n_solid, n_virt):
+    out = C.c_size_t()
+    check(load().fsim_estimate_bytes(C.byref(cfg), n_fluid, n_solid, n_virt, C.byref(out)))
+    return out.value
 
 
 def derive(cfg):

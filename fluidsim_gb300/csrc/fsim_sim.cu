@@ -2472,3 +2472,28 @@ extern "C" fsim_status fsim_batch_destroy(fsim_batch_t b)
     delete b;
     return FSIM_OK;
 }
+
+extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, int n_solid, int n_virt,
+                                           size_t *out)
+{
+    if (!cfg || !out || n_fluid < 0 || n_solid < 0 || n_virt < 0) return FSIM_EINVAL;
+    fsim_derived d;
+    fsim_status st = fsim_derive(cfg, &d);
+    if (st) return st;
+    const size_t nf = n_fluid, ns = n_solid, nv = n_virt, nc = d.cell_number_total;
+    size_t b = 0;
+    b += nf * (2 * 2 * sizeof(float4) + 2 * sizeof(int) + 4 * sizeof(int)); // state x2, orig x2, cell/key/slot/tmp
+    if (cfg->keep_derivatives) b += nf * (sizeof(float) + sizeof(float4));
+    b += ns * (2 * 3 * sizeof(float4) + 2 * 2 * sizeof(int) + 4 * sizeof(int)); // state x2, cell/key/slot/tmp
+    b += ns * (3 * sizeof(float4) + 5 * 9 * sizeof(float));                     // per-step products
+    b += nv * (3 * sizeof(float4) + 2 * sizeof(int));
+    b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 3; // counts, starts
+    b += 2 * kMaxScanTiles * sizeof(int) + sizeof(unsigned);
+    size_t words = 3 * nf;
+    if (9 * ns > words) words = 9 * ns;
+    if (3 * nv > words) words = 3 * nv;
+    b += 4 * (words ? words : 1);
+    b += 64 * 1024; // plans and allocation granularity
+    *out = b;
+    return FSIM_OK;
+}

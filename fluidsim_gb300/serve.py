@@ -1,0 +1,200 @@
+"""Served stream of FSI requests with continuous batching.
+
+A request is one dam-break scenario (a config + case) and a number of steps.
+Requests arrive on a schedule; the server keeps the admitted ones resident on
+the GPU and advances all of them together with batched launches
+(fsim_batch_*).  At every step-quantum boundary it retires finished requests
+(their results are read back) and admits waiting ones first-come first-served
+while their estimated device memory (fsim_estimate_bytes) fits the budget, so
+requests that arrive while others run join the running batch.  The reference
+runs one scenario per process; this loop has no reference counterpart.
+
+`serve_one_by_one` processes the same stream with one standalone instance at a
+time (the plain form), for comparison.
+"""
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import api, cases
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float           # seconds after the start of the stream
+    cfg: object
+    case: object
+    steps: int
+    particles: int = 0       # fluid + solid, set when generated
+    done_at: float = float("nan")
+    result: dict = field(default_factory=dict)
+
+
+def poisson_stream(n, rate, seed=7, fluid_range=(10_000, 1_000_000), solid_range=(1_000, 27_000),
+                   steps_range=(200, 2000), dx=0.01):
+    """Seeded request stream: Poisson arrivals at `rate` per second; fluid count
+    log-uniform in fluid_range; a solid plate (or block) of solid_range
+    particles; steps uniform in steps_range."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for rid in range(n):
+        t += rng.exponential(1.0 / rate)
+        cfg, case = cases.ensemble_member(rng, dx=dx, n_range=fluid_range)
+        # solid block: 4 cells thick, height and width sized to the drawn count
+        ns = int(math.exp(rng.uniform(math.log(solid_range[0]), math.log(solid_range[1]))))
+        sz = max(4, min(case.tank_n[2], int(round(math.sqrt(ns / 4.0)))))
+        sy = max(2, min(case.tank_n[1] - 1, ns // (4 * sz)))
+        case.solid_n[0], case.solid_n[1], case.solid_n[2] = 4, sy, sz
+        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        cfg.iend = steps
+        out.append(Request(rid, t, cfg, case, steps))
+    return out
+
+
+def _result_fields(sim):
+    out = {"fluid_pos": sim.get("fluid_pos"), "fluid_vel": sim.get("fluid_vel"), "fluid_rho": sim.get("fluid_rho")}
+    if sim.n["solid"]:
+        out["solid_pos"] = sim.get("solid_pos")
+    return out
+
+
+def _percentile(xs, q):
+    return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if xs else float("nan")
+
+
+class GpuBackend:
+    """Instances are fsim handles; a batch is an fsim_batch over them."""
+
+    def __init__(self, device=0):
+        self.device = device
+
+    def prepare(self, r):
+        """Generate the request's particles; returns (particles, device bytes)."""
+        cfg, pa = cases.make((r.cfg, r.case))
+        return (cfg, pa), api.estimate_bytes(cfg, pa.n_fluid, pa.n_solid, pa.n_virt), pa.n_fluid + pa.n_solid
+
+    def create(self, prepared):
+        cfg, pa = prepared
+        return api.Simulation(cfg, pa, device=self.device)
+
+    def batch(self, instances):
+        return api.Batch(instances)
+
+    def result(self, inst):
+        return _result_fields(inst)
+
+    def destroy(self, inst):
+        inst.close()
+
+
+class Server:
+    """Continuous-batching server over one GPU.
+
+    Every loop turn: release requests whose arrival time has passed into the
+    waiting queue; admit from its head while the estimated device memory of
+    the admitted requests stays within the budget (a request larger than the
+    budget is admitted alone when nothing else runs); rebuild the batch when
+    its membership changed; advance the batch by `quantum` steps (fewer if a
+    member needs fewer); retire members whose steps are done."""
+
+    def __init__(self, budget_bytes, backend=None, quantum=10, keep_results=False):
+        self.budget = budget_bytes
+        self.backend = backend or GpuBackend()
+        self.quantum = quantum
+        self.keep_results = keep_results
+        self.log = []  # (event, request id, time)
+
+    def run(self, requests, clock=time.perf_counter, sleep=time.sleep):
+        be = self.backend
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        waiting, active = [], []  # active entries: [request, instance, steps left, bytes]
+        prepared = {}
+        nxt, used, batch = 0, 0, None
+        t0 = clock()
+        completed, work, rebuilds = 0, 0, 0
+        while completed < len(reqs):
+            now = clock() - t0
+            while nxt < len(reqs) and reqs[nxt].arrival <= now:
+                waiting.append(reqs[nxt])
+                nxt += 1
+            changed = False
+            while waiting:
+                r = waiting[0]
+                if r.rid not in prepared:
+                    prepared[r.rid] = be.prepare(r)
+                data, need, npart = prepared[r.rid]
+                if active and used + need > self.budget:
+                    break
+                waiting.pop(0)
+                del prepared[r.rid]
+                r.particles = npart
+                active.append([r, be.create(data), r.steps, need])
+                used += need
+                changed = True
+                self.log.append(("admit", r.rid, clock() - t0))
+            if not active:
+                if nxt < len(reqs):
+                    sleep(max(0.0, min(0.05, reqs[nxt].arrival - (clock() - t0))))
+                continue
+            if changed or batch is None:
+                if batch is not None:
+                    batch.close()
+                batch = be.batch([a[1] for a in active])
+                rebuilds += 1
+            k = min(self.quantum, min(a[2] for a in active))
+            batch.step(k)
+            batch.sync()
+            now = clock() - t0
+            finished = []
+            for a in active:
+                a[2] -= k
+                work += a[0].particles * k
+                if a[2] == 0:
+                    a[0].done_at = now
+                    finished.append(a)
+            if finished:
+                batch.close()
+                batch = None
+                for a in finished:
+                    if self.keep_results:
+                        a[0].result = be.result(a[1])
+                    be.destroy(a[1])
+                    used -= a[3]
+                    completed += 1
+                    self.log.append(("done", a[0].rid, now))
+                active = [a for a in active if a[2] > 0]
+        if batch is not None:
+            batch.close()
+        makespan = clock() - t0
+        lat = [r.done_at - r.arrival for r in reqs]
+        return {"requests": len(reqs), "makespan_s": makespan, "particle_updates": work,
+                "throughput": work / makespan, "p50_latency_s": _percentile(lat, 50),
+                "p99_latency_s": _percentile(lat, 99), "batch_rebuilds": rebuilds}
+
+
+def serve_one_by_one(requests, device=0, clock=time.perf_counter, keep_results=False):
+    """The plain form: one standalone instance at a time, first-come first-served."""
+    reqs = sorted(requests, key=lambda r: r.arrival)
+    t0 = clock()
+    work = 0
+    for r in reqs:
+        wait = r.arrival - (clock() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        cfg, pa = cases.make((r.cfg, r.case))
+        r.particles = pa.n_fluid + pa.n_solid
+        with api.Simulation(cfg, pa, device=device) as sim:
+            sim.step(r.steps)
+            sim.sync()
+            r.done_at = clock() - t0
+            if keep_results:
+                r.result = _result_fields(sim)
+        work += r.particles * r.steps
+    makespan = clock() - t0
+    lat = [r.done_at - r.arrival for r in reqs]
+    return {"requests": len(reqs), "makespan_s": makespan, "particle_updates": work, "throughput": work / makespan,
+            "p50_latency_s": _percentile(lat, 50), "p99_latency_s": _percentile(lat, 99)}

@@ -287,6 +287,10 @@ fsim_status fsim_host_free(void *p);
 fsim_status fsim_cell_sort_noalloc(const fsim_derived *grid, const float *d_pos, int n,
                                    int *d_cell_start, int *d_ids, void *stream);
 
+/* Device memory an instance of this configuration and these particle
+ * counts allocates (an upper estimate, for admission control). */
+fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, int n_solid, int n_virt, size_t *out);
+
 /* Sizes of the instance. */
 fsim_status fsim_counts(fsim_handle h, int *n_fluid, int *n_solid, int *n_virt);
 fsim_status fsim_get_derived(fsim_handle h, fsim_derived *out);

@@ -1,0 +1,34 @@
+"""Served form on the GPU: requests admitted while others run produce the
+same results as when each runs alone (bit for bit: a member of a batch runs
+the same kernels on its own data)."""
+import numpy as np
+import pytest
+
+from fluidsim_gb300 import serve
+
+pytestmark = pytest.mark.gpu
+
+
+def _stream():
+    return serve.poisson_stream(5, rate=400.0, seed=11, fluid_range=(2000, 9000), solid_range=(200, 900),
+                                steps_range=(8, 30))
+
+
+def test_served_results_equal_solo():
+    mixed = _stream()
+    out = serve.Server(budget_bytes=2 ** 36, quantum=3, keep_results=True).run(mixed)
+    assert out["requests"] == 5 and out["batch_rebuilds"] >= 2
+    solo = _stream()
+    serve.serve_one_by_one(solo, keep_results=True)
+    for a, b in zip(mixed, solo):
+        assert a.result.keys() == b.result.keys()
+        for k in a.result:
+            assert np.array_equal(a.result[k], b.result[k]), (a.rid, k)
+
+
+def test_budget_admits_one_at_a_time():
+    reqs = _stream()[:3]
+    srv = serve.Server(budget_bytes=1, quantum=4)  # every request alone
+    out = srv.run(reqs)
+    assert out["requests"] == 3
+    assert out["batch_rebuilds"] == 3
