@@ -323,8 +323,24 @@ struct GatherSolidArgs {
     const int *type_in, *orig_in;
     float4 *pos_out, *vel_out, *ref_out;
     int *type_out, *orig_out, *cell_out;
+    int *inv_out;       // sorted position of every input id
+    unsigned *cxyz_out; // cell coordinates packed x | y << 11 | z << 21
 };
-__device__ __forceinline__ void gather_solid_body(const DevParams &, const GatherSolidArgs &A, int blk)
+__device__ __forceinline__ unsigned pack_cell(const DevParams &P, int c)
+{
+    const int cx = c / (P.ny * P.nz), rem = c - cx * P.ny * P.nz;
+    const int cy = rem / P.nz, cz = rem - cy * P.nz;
+    return (unsigned)cx | ((unsigned)cy << 11) | ((unsigned)cz << 21);
+}
+// neighbouring cells (each coordinate within one), from packed coordinates
+__device__ __forceinline__ bool cells_adjacent(unsigned a, unsigned b)
+{
+    const int dx = (int)(a & 0x7ffu) - (int)(b & 0x7ffu);
+    const int dy = (int)((a >> 11) & 0x3ffu) - (int)((b >> 11) & 0x3ffu);
+    const int dz = (int)(a >> 21) - (int)(b >> 21);
+    return abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1;
+}
+__device__ __forceinline__ void gather_solid_body(const DevParams &P, const GatherSolidArgs &A, int blk)
 {
     const int d = blk * blockDim.x + threadIdx.x;
     if (d >= A.n) return;
@@ -334,8 +350,11 @@ __device__ __forceinline__ void gather_solid_body(const DevParams &, const Gathe
     A.vel_out[dst] = A.vel_in[src];
     A.ref_out[dst] = A.ref_in[src];
     A.type_out[dst] = A.type_in[src];
-    A.orig_out[dst] = A.orig_in[src];
+    const int o = A.orig_in[src];
+    A.orig_out[dst] = o;
     A.cell_out[dst] = cell;
+    A.inv_out[o] = dst;
+    A.cxyz_out[dst] = pack_cell(P, cell);
 }
 FSIM_BATCHED_KERNEL(kb_gather_solid, GatherSolidArgs, gather_solid_body, kBlock)
 
@@ -771,6 +790,10 @@ struct SolidArgs {
     const float4 *fposr, *fvelp;
     const int *start_f;
     int n;
+    // static reference-configuration neighbours (CSR over input ids)
+    const int *orig, *inv, *nbr_off, *nbr_orig;
+    const float4 *nbr_dXw; // (X_j - X_i, kernel weight)
+    const unsigned *cxyz;
 };
 
 struct M3 {
@@ -801,50 +824,62 @@ __device__ __forceinline__ M3 cofactor(const M3 &a)
     return c;
 }
 
+// Solid sub-step sweeps over the static reference-configuration neighbour
+// lists: the reference takes the solid candidates from the 27 cells of the
+// current cells and keeps those with |X_j - X_i| < 2h (src/solid.cu:53-69,
+// 195-203).  The list holds every j with |X_j - X_i| < 2h (built once); a
+// sub-step keeps the entries whose current cell is adjacent to i's, which is
+// exactly that set.  kSolidGroup lanes share one particle and combine their
+// sums with shuffles (a fixed pairing: deterministic).
+constexpr int kSolidGroup = 4;
+
+__device__ __forceinline__ float group_sum(float v)
+{
+#pragma unroll
+    for (int o = 1; o < kSolidGroup; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
 // solidDeformationCalculate (src/solid.cu:10-79): F and L over the
 // reference-configuration neighbours, L^-1 (identity when singular),
 // F <- F L^-1, Green strain, St-Venant-Kirchhoff 2nd Piola, P = F S.
 // Also stores P L^-1 and cof(F) L^-1 (= det(F) F^-T L^-1) for the force sweep.
-// One warp per solid particle.
 __device__ __forceinline__ void solid_deform_body(const DevParams &P, const SolidArgs &S, int blk)
 {
-    const int i = (blk * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= S.n) return; // whole warp
-    const float4 Xi = S.ref[i], xi = S.pos[i];
-    Rows rows;
-    neighbor_rows(P, S.cell[i], rows);
+    const int t = blk * blockDim.x + threadIdx.x;
+    const int i = t / kSolidGroup, g = t % kSolidGroup;
+    const bool valid = i < S.n;
     M3 F, L;
 #pragma unroll
     for (int k = 0; k < 9; ++k) F.m[k] = L.m[k] = 0.0f;
-    for (int r = 0; r < rows.count; ++r) {
-        for (int j = S.start_s[rows.base[r] + rows.z0] + lane, je = S.start_s[rows.base[r] + rows.z1]; j < je;
-             j += 32) {
-            const float4 Xj = S.ref[j];
-            const float dX[3] = {Xj.x - Xi.x, Xj.y - Xi.y, Xj.z - Xi.z};
-            const float r2 = dist2(dX[0], dX[1], dX[2]);
-            if (r2 < P.R2) {
-                const float4 xj = S.pos[j];
-                const float dx[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
-                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+    if (valid) {
+        const float4 xi = S.pos[i];
+        const unsigned ci = S.cxyz[i];
+        const int o = S.orig[i];
+        for (int e = S.nbr_off[o] + g, ee = S.nbr_off[o + 1]; e < ee; e += kSolidGroup) {
+            const int j = S.inv[S.nbr_orig[e]];
+            if (!cells_adjacent(ci, S.cxyz[j])) continue;
+            const float4 dXw = S.nbr_dXw[e];
+            const float4 xj = S.pos[j];
+            const float dx[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
+            const float dX[3] = {dXw.x, dXw.y, dXw.z};
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const float ra = dx[a] * w, la = dX[a] * w;
+            for (int a = 0; a < 3; ++a) {
+                const float ra = dx[a] * dXw.w, la = dX[a] * dXw.w;
 #pragma unroll
-                    for (int b = 0; b < 3; ++b) {
-                        F.m[3 * a + b] += ra * dX[b];
-                        L.m[3 * a + b] += la * dX[b];
-                    }
+                for (int c = 0; c < 3; ++c) {
+                    F.m[3 * a + c] += ra * dX[c];
+                    L.m[3 * a + c] += la * dX[c];
                 }
             }
         }
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-        F.m[k] = warp_sum(F.m[k]);
-        L.m[k] = warp_sum(L.m[k]);
+        F.m[k] = group_sum(F.m[k]);
+        L.m[k] = group_sum(L.m[k]);
     }
-    if (lane) return;
+    if (!valid || g) return;
     const M3 cl = cofactor(L);
     const float det = L.m[0] * cl.m[0] + L.m[1] * cl.m[1] + L.m[2] * cl.m[2];
     M3 Linv;
@@ -853,7 +888,7 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) Linv.m[3 * a + b] = cl.m[3 * b + a] * id;
+            for (int c = 0; c < 3; ++c) Linv.m[3 * a + c] = cl.m[3 * c + a] * id;
     } else {
 #pragma unroll
         for (int k = 0; k < 9; ++k) Linv.m[k] = (k % 4 == 0) ? 1.0f : 0.0f;
@@ -864,9 +899,9 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b = 0; b < 3; ++b)
-            E.m[3 * a + b] =
-                0.5f * (F.m[a] * F.m[b] + F.m[3 + a] * F.m[3 + b] + F.m[6 + a] * F.m[6 + b] - (a == b ? 1.0f : 0.0f));
+        for (int c = 0; c < 3; ++c)
+            E.m[3 * a + c] =
+                0.5f * (F.m[a] * F.m[c] + F.m[3 + a] * F.m[3 + c] + F.m[6 + a] * F.m[6 + c] - (a == c ? 1.0f : 0.0f));
     const float tr = E.m[0] + E.m[4] + E.m[8];
     M3 Sm;
 #pragma unroll
@@ -885,81 +920,94 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
 }
 FSIM_BATCHED_KERNEL(kb_solid_deform, SolidArgs, solid_deform_body, kBlock)
 
-// solidForceCalculate (src/solid.cu:81-207): stress divergence + artificial
-// viscosity over solid neighbours (reference configuration), fluid traction
-// over fluid neighbours (current configuration, fluid already advanced).
-// One warp per solid particle.
+// solidForceCalculate (src/solid.cu:81-207): fluid traction over the fluid
+// neighbours (current configuration, fluid already advanced; candidates from
+// the 27 cells of the step-start cell) plus stress divergence and artificial
+// viscosity over the reference-configuration solid neighbours.
 __device__ __forceinline__ void solid_force_body(const DevParams &P, const SolidArgs &S, int blk)
 {
-    const int i = (blk * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= S.n) return; // whole warp
-    const float4 xi = S.pos[i], Xi = S.ref[i], vi = S.vel[i], ni = S.np[i];
-    Rows rows;
-    neighbor_rows(P, S.cell[i], rows);
-    float PLi[9], AVi[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        PLi[k] = S.PL[9 * i + k];
-        AVi[k] = S.AV[9 * i + k];
-    }
+    const int t = blk * blockDim.x + threadIdx.x;
+    const int i = t / kSolidGroup, g = t % kSolidGroup;
+    const bool valid = i < S.n;
     float cx = 0.0f, cy = 0.0f, cz = 0.0f, ax = 0.0f, ay = 0.0f, az = 0.0f;
-    for (int r = 0; r < rows.count; ++r) {
-        const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+    if (valid) {
+        const float4 xi = S.pos[i], vi = S.vel[i], ni = S.np[i];
+        Rows rows;
+        neighbor_rows(P, S.cell[i], rows);
         // solidFluidCouple (src/solid.cu:81-117)
-        for (int j = S.start_f[c0] + lane, je = S.start_f[c1]; j < je; j += 32) {
-            const float4 q = S.fposr[j];
-            const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
-            const float r2 = dist2(dx, dy, dz);
-            if (r2 < P.R2) {
-                const float4 u = S.fvelp[j];
-                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
-                const float k2 = 2.0f * ((u.x - vi.x) * ni.x + (u.y - vi.y) * ni.y + (u.z - vi.z) * ni.z);
-                // u_i - u_j = -k2 n ; du = (u_i - u_j).e
-                const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
-                const float du = -k2 * (ni.x * dx + ni.y * dy + ni.z * dz) * inv_r;
-                float ps = 0.5f * (ni.w + u.w);
-                if (du >= 0.0f) ps += 0.5f * q.w * du * P.c0;
-                const float f = -2.0f * ps * P.rho_s_inv * w;
-                cx += f * dx;
-                cy += f * dy;
-                cz += f * dz;
+        for (int r = 0; r < rows.count; ++r) {
+            const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+            for (int j = S.start_f[c0] + g, je = S.start_f[c1]; j < je; j += kSolidGroup) {
+                const float4 q = S.fposr[j];
+                const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 < P.R2) {
+                    const float4 u = S.fvelp[j];
+                    const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+                    const float k2 = 2.0f * ((u.x - vi.x) * ni.x + (u.y - vi.y) * ni.y + (u.z - vi.z) * ni.z);
+                    // u_i - u_j = -k2 n ; du = (u_i - u_j).e
+                    const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+                    const float du = -k2 * (ni.x * dx + ni.y * dy + ni.z * dz) * inv_r;
+                    float ps = 0.5f * (ni.w + u.w);
+                    if (du >= 0.0f) ps += 0.5f * q.w * du * P.c0;
+                    const float f = -2.0f * ps * P.rho_s_inv * w;
+                    cx += f * dx;
+                    cy += f * dy;
+                    cz += f * dz;
+                }
             }
         }
         // solidSolidForce (src/solid.cu:119-157)
-        for (int j = S.start_s[c0] + lane, je = S.start_s[c1]; j < je; j += 32) {
-            const float4 Xj = S.ref[j];
-            const float dX = Xj.x - Xi.x, dY = Xj.y - Xi.y, dZ = Xj.z - Xi.z;
-            const float r2 = dist2(dX, dY, dZ);
-            if (r2 < P.R2) {
-                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
-                const float *PLj = S.PL + 9 * j;
-                const float ws = w * P.rho_s_inv;
-                ax += ((PLj[0] + PLi[0]) * dX + (PLj[1] + PLi[1]) * dY + (PLj[2] + PLi[2]) * dZ) * ws;
-                ay += ((PLj[3] + PLi[3]) * dX + (PLj[4] + PLi[4]) * dY + (PLj[5] + PLi[5]) * dZ) * ws;
-                az += ((PLj[6] + PLi[6]) * dX + (PLj[7] + PLi[7]) * dY + (PLj[8] + PLi[8]) * dZ) * ws;
-                const float4 xj = S.pos[j], vj = S.vel[j];
-                const float ddx = xj.x - xi.x, ddy = xj.y - xi.y, ddz = xj.z - xi.z;
-                const float dvdx = (vj.x - vi.x) * ddx + (vj.y - vi.y) * ddy + (vj.z - vi.z) * ddz;
-                const float nu = P.h * dvdx / (ddx * ddx + ddy * ddy + ddz * ddz + P.eps_h2);
-                const float visc = (P.alpha * nu * P.cs_s - P.beta * nu * nu) * w;
-                ax += (AVi[0] * dX + AVi[1] * dY + AVi[2] * dZ) * visc;
-                ay += (AVi[3] * dX + AVi[4] * dY + AVi[5] * dZ) * visc;
-                az += (AVi[6] * dX + AVi[7] * dY + AVi[8] * dZ) * visc;
-            }
+        float PLi[9], AVi[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            PLi[k] = S.PL[9 * i + k];
+            AVi[k] = S.AV[9 * i + k];
+        }
+        const unsigned ci = S.cxyz[i];
+        const int o = S.orig[i];
+        for (int e = S.nbr_off[o] + g, ee = S.nbr_off[o + 1]; e < ee; e += kSolidGroup) {
+            const int j = S.inv[S.nbr_orig[e]];
+            if (!cells_adjacent(ci, S.cxyz[j])) continue;
+            const float4 dXw = S.nbr_dXw[e];
+            const float dX = dXw.x, dY = dXw.y, dZ = dXw.z, w = dXw.w;
+            const float *PLj = S.PL + 9 * j;
+            const float ws = w * P.rho_s_inv;
+            ax += ((PLj[0] + PLi[0]) * dX + (PLj[1] + PLi[1]) * dY + (PLj[2] + PLi[2]) * dZ) * ws;
+            ay += ((PLj[3] + PLi[3]) * dX + (PLj[4] + PLi[4]) * dY + (PLj[5] + PLi[5]) * dZ) * ws;
+            az += ((PLj[6] + PLi[6]) * dX + (PLj[7] + PLi[7]) * dY + (PLj[8] + PLi[8]) * dZ) * ws;
+            const float4 xj = S.pos[j], vj = S.vel[j];
+            const float ddx = xj.x - xi.x, ddy = xj.y - xi.y, ddz = xj.z - xi.z;
+            const float dvdx = (vj.x - vi.x) * ddx + (vj.y - vi.y) * ddy + (vj.z - vi.z) * ddz;
+            const float nu = P.h * dvdx / (ddx * ddx + ddy * ddy + ddz * ddz + P.eps_h2);
+            const float visc = (P.alpha * nu * P.cs_s - P.beta * nu * nu) * w;
+            ax += (AVi[0] * dX + AVi[1] * dY + AVi[2] * dZ) * visc;
+            ay += (AVi[3] * dX + AVi[4] * dY + AVi[5] * dZ) * visc;
+            az += (AVi[6] * dX + AVi[7] * dY + AVi[8] * dZ) * visc;
         }
     }
-    cx = warp_sum(cx);
-    cy = warp_sum(cy);
-    cz = warp_sum(cz);
-    ax = warp_sum(ax);
-    ay = warp_sum(ay);
-    az = warp_sum(az);
-    if (lane) return;
+    cx = group_sum(cx);
+    cy = group_sum(cy);
+    cz = group_sum(cz);
+    ax = group_sum(ax);
+    ay = group_sum(ay);
+    az = group_sum(az);
+    if (!valid || g) return;
     S.couple[i] = make_float4(cx, cy, cz, 0.0f);
     S.dudt[i] = make_float4(ax + cx, ay + cy, az + cz, 0.0f);
 }
 FSIM_BATCHED_KERNEL(kb_solid_force, SolidArgs, solid_force_body, kBlock)
+
+// Kernel weight of every static solid neighbour pair (once, at creation).
+__global__ void k_solid_pair_weights(const DevParams P, float4 *__restrict__ dXw, int n)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    float4 v = dXw[e];
+    const float r2 = dist2(v.x, v.y, v.z);
+    v.w = __expf(-r2 * P.h_inv2) * P.kdiff;
+    dXw[e] = v;
+}
 
 // solidUpdate (src/solid.cu:209-239)
 __device__ __forceinline__ void solid_update_body(const DevParams &P, const SolidArgs &S, int blk)
@@ -1104,6 +1152,10 @@ struct fsim_sim {
     int *s_cnt = nullptr, *s_start = nullptr;
     float4 *s_np = nullptr, *s_dudt = nullptr, *s_couple = nullptr;
     float *s_F = nullptr, *s_P = nullptr, *s_L = nullptr, *s_PL = nullptr, *s_AV = nullptr;
+    int *s_inv = nullptr;         // sorted position of every input id (written by the gather)
+    unsigned *s_cxyz = nullptr;   // packed cell coordinates, sorted order
+    int *s_nbr_off = nullptr, *s_nbr_orig = nullptr; // static reference neighbours (CSR, input ids)
+    float4 *s_nbr_dXw = nullptr;  // (X_j - X_i, kernel weight) per list entry
     int s_cur = 0;
     bool s_sorted = false;
     bool s_np_ok = false;    // normal + pressure are in the order of s_cur
@@ -1344,7 +1396,7 @@ void plan_cell(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
         gs.push_back({h->P, GatherSolidArgs{h->s_tmp, h->s_key, h->s_start, h->ns, h->s_pos[ps], h->s_vel[ps],
                                             h->s_ref[ps], h->s_type[ps], h->s_orig[ps], h->s_pos[1 - ps],
                                             h->s_vel[1 - ps], h->s_ref[1 - ps], h->s_type[1 - ps], h->s_orig[1 - ps],
-                                            h->s_cell}});
+                                            h->s_cell, h->s_inv, h->s_cxyz}});
         gsb.push_back(blocks_for(h->ns, kBlock));
     }
     add_launch(pl, ab, L_GATHER_F, gf, gfb);
@@ -1446,9 +1498,15 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
             S.fvelp = h->f_velp[pf];
             S.start_f = h->f_start;
             S.n = h->ns;
+            S.orig = h->s_orig[ps];
+            S.inv = h->s_inv;
+            S.nbr_off = h->s_nbr_off;
+            S.nbr_orig = h->s_nbr_orig;
+            S.nbr_dXw = h->s_nbr_dXw;
+            S.cxyz = h->s_cxyz;
             it.push_back({h->P, S});
             const bool active = h->ns && k < h->cfg.solid_sub_step;
-            wb.push_back(active ? blocks_for(32ll * h->ns, kBlock) : 0);
+            wb.push_back(active ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
             tb.push_back(active ? blocks_for(h->ns, kBlock) : 0);
         }
         add_launch(pl, ab, L_DEFORM, it, wb);
@@ -1710,6 +1768,79 @@ fsim_status sort_virtual(fsim_sim *h, const float *vpos_host)
     return FSIM_OK;
 }
 
+// Static reference-configuration neighbour lists of the solid: for every
+// input id i, the ids j != i with |X_j - X_i|^2 < (2h)^2, the squared distance
+// formed as the device forms it (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) in FP32).
+// Binned on a host grid of cell size >= 2h; list entries are in increasing j.
+fsim_status build_solid_neighbors(fsim_sim *h, const float *ref)
+{
+    const int ns = h->ns;
+    const float R2 = h->P.R2;
+    const double cs = std::sqrt((double)R2) * 1.0001 + 1e-12;
+    float lo[3] = {ref[0], ref[1], ref[2]}, hi[3] = {ref[0], ref[1], ref[2]};
+    for (int i = 0; i < ns; ++i)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], ref[3 * i + a]);
+            hi[a] = std::max(hi[a], ref[3 * i + a]);
+        }
+    int nb[3];
+    for (int a = 0; a < 3; ++a) nb[a] = std::max(1, std::min(1024, (int)((hi[a] - lo[a]) / cs) + 1));
+    auto bin = [&](int i, int a) {
+        const int b = (int)((ref[3 * i + a] - lo[a]) / cs);
+        return std::min(nb[a] - 1, std::max(0, b));
+    };
+    const size_t nbins = (size_t)nb[0] * nb[1] * nb[2];
+    std::vector<int> bstart(nbins + 1, 0), order(ns);
+    std::vector<int> key(ns);
+    for (int i = 0; i < ns; ++i) {
+        key[i] = (bin(i, 0) * nb[1] + bin(i, 1)) * nb[2] + bin(i, 2);
+        ++bstart[key[i] + 1];
+    }
+    for (size_t b = 0; b < nbins; ++b) bstart[b + 1] += bstart[b];
+    {
+        std::vector<int> fill(bstart.begin(), bstart.end() - 1);
+        for (int i = 0; i < ns; ++i) order[fill[key[i]]++] = i; // increasing i within a bin
+    }
+    std::vector<int> off(ns + 1, 0), nbr;
+    std::vector<float4> dXw;
+    std::vector<int> cand;
+    for (int i = 0; i < ns; ++i) {
+        const int bx = bin(i, 0), by = bin(i, 1), bz = bin(i, 2);
+        cand.clear();
+        for (int x = std::max(0, bx - 1); x <= std::min(nb[0] - 1, bx + 1); ++x)
+            for (int y = std::max(0, by - 1); y <= std::min(nb[1] - 1, by + 1); ++y)
+                for (int z = std::max(0, bz - 1); z <= std::min(nb[2] - 1, bz + 1); ++z) {
+                    const int b = (x * nb[1] + y) * nb[2] + z;
+                    for (int k = bstart[b]; k < bstart[b + 1]; ++k) cand.push_back(order[k]);
+                }
+        std::sort(cand.begin(), cand.end());
+        for (int j : cand) {
+            if (j == i) continue;
+            const float dx = ref[3 * j] - ref[3 * i], dy = ref[3 * j + 1] - ref[3 * i + 1],
+                        dz = ref[3 * j + 2] - ref[3 * i + 2];
+            const float r2 = std::fmaf(dz, dz, std::fmaf(dy, dy, dx * dx));
+            if (r2 < R2) {
+                nbr.push_back(j);
+                dXw.push_back(make_float4(dx, dy, dz, 0.0f));
+            }
+        }
+        off[i + 1] = (int)nbr.size();
+    }
+    const size_t ne = nbr.size();
+    fsim_status st;
+    if ((st = dalloc(h, &h->s_nbr_off, (size_t)ns + 1)) || (st = dalloc(h, &h->s_nbr_orig, ne)) ||
+        (st = dalloc(h, &h->s_nbr_dXw, ne)))
+        return st;
+    CK(cudaMemcpy(h->s_nbr_off, off.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+    if (ne) {
+        CK(cudaMemcpy(h->s_nbr_orig, nbr.data(), sizeof(int) * ne, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->s_nbr_dXw, dXw.data(), sizeof(float4) * ne, cudaMemcpyHostToDevice));
+        k_solid_pair_weights<<<blocks_for((long long)ne, kBlock), kBlock, 0, h->stream>>>(h->P, h->s_nbr_dXw, (int)ne);
+        CK_LAUNCH();
+    }
+    return FSIM_OK;
+}
+
 fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
 {
     const int nf = p->n_fluid, ns = p->n_solid, nv = p->n_virt, nc = h->ncell;
@@ -1742,7 +1873,8 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
         (st = dalloc(h, &h->s_np, ns)) || (st = dalloc(h, &h->s_dudt, ns)) || (st = dalloc(h, &h->s_couple, ns)) ||
         (st = dalloc(h, &h->s_F, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_P, 9 * (size_t)ns)) ||
         (st = dalloc(h, &h->s_L, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_PL, 9 * (size_t)ns)) ||
-        (st = dalloc(h, &h->s_AV, 9 * (size_t)ns)))
+        (st = dalloc(h, &h->s_AV, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_inv, ns)) ||
+        (st = dalloc(h, &h->s_cxyz, ns)))
         return st;
     // virtual
     if ((st = dalloc(h, &h->v_posr, nv)) || (st = dalloc(h, &h->v_velp, nv)) || (st = dalloc(h, &h->v_normal, nv)) ||
@@ -1801,6 +1933,7 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
         CK(cudaMemset(h->s_couple, 0, sizeof(float4) * ns));
         h->s_mech_ok = true; // initial values, in input order (= s_orig[0])
         h->s_np_ok = true;
+        if ((st = build_solid_neighbors(h, p->solid_ref_pos))) return st;
     }
     if (nv && (st = sort_virtual(h, p->virt_pos))) return st;
     CK(cudaStreamSynchronize(h->stream));
@@ -1854,6 +1987,12 @@ extern "C" fsim_status fsim_create(const fsim_config *cfg, const fsim_particles 
     h->nv = p->n_virt;
     h->ncell = h->der.cell_number_total;
     h->keep = cfg->keep_derivatives != 0;
+    if (h->ns && (h->P.nx >= 2048 || h->P.ny >= 1024 || h->P.nz >= 2048)) {
+        fsim_set_error("cell grid %d x %d x %d too large for a solid (limit 2047 x 1023 x 2047)", h->P.nx, h->P.ny,
+                       h->P.nz);
+        delete h;
+        return FSIM_EINVAL;
+    }
     // The union-of-rows sweep needs no z-cell check when the z spacing exceeds
     // the impact distance by more than FP32 rounding of the cell coordinate
     // (about 2.4e-7 * nz cells, doubled here, plus slack) can eat; keep it otherwise.
@@ -2485,7 +2624,13 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
     b += nf * (2 * 2 * sizeof(float4) + 2 * sizeof(int) + 4 * sizeof(int)); // state x2, orig x2, cell/key/slot/tmp
     if (cfg->keep_derivatives) b += nf * (sizeof(float) + sizeof(float4));
     b += ns * (2 * 3 * sizeof(float4) + 2 * 2 * sizeof(int) + 4 * sizeof(int)); // state x2, cell/key/slot/tmp
-    b += ns * (3 * sizeof(float4) + 5 * 9 * sizeof(float));                     // per-step products
+    b += ns * (3 * sizeof(float4) + 5 * 9 * sizeof(float) + 2 * sizeof(int));  // per-step products, inv, cells
+    {
+        // static solid neighbour lists: lattice count within 2h, plus slack
+        const double r = std::sqrt((double)d.impact_distance_square) / (double)cfg->particle_diameter;
+        const size_t per = (size_t)(4.18879 * r * r * r * 1.25) + 8;
+        b += ns * per * (sizeof(int) + sizeof(float4)) + (ns + 1) * sizeof(int);
+    }
     b += nv * (3 * sizeof(float4) + 2 * sizeof(int));
     b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 3; // counts, starts
     b += 2 * kMaxScanTiles * sizeof(int) + sizeof(unsigned);
