@@ -273,7 +273,8 @@ def run_gb300(args, dist):
     # ---- the batched form on the ensemble workload
     forms = None
     if not args.no_forms:
-        forms = {"ensemble64": run_ensemble(dev, max(10, min(args.steps, 50))), "served": run_served(dev)}
+        forms = {"mixed": run_mixed(dev, max(10, min(args.steps, 100))),
+                 "ensemble64": run_ensemble(dev, max(10, min(args.steps, 50))), "served": run_served(dev)}
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
@@ -305,6 +306,29 @@ def run_gb300(args, dist):
         }
         print(json.dumps(line), flush=True)
     return 0
+
+
+def run_mixed(dev, steps):
+    """BASELINE config 2: the 4M FSI case with +-0.01 dx position jitter (seed
+    12345) in the plain FP32 form and in the mixed form, same input.  Device
+    time of `steps` graph steps each; the per-field error of both forms against
+    the FP64 oracle is measured separately (tests/accuracy_report.py)."""
+    from fluidsim_gb300 import api, cases
+
+    out = {}
+    for name, prec in (("plain", api.PRECISION_FP32), ("mixed", api.PRECISION_MIXED)):
+        cfg, pa = cases.make(cases.fsi_4m_jitter(precision=prec))
+        with api.Simulation(cfg, pa, device=dev) as sim:
+            sim.step(5)
+            sim.sync()
+            ms = sim.time_steps(steps)
+            tot, sweep = sim.time_sweep(steps)
+        out[name] = (pa.n_fluid + pa.n_solid) * steps / (ms * 1e-3)
+        out[name + "_ms_per_step"] = ms / steps
+        out[name + "_sweep_ms"] = sweep / steps
+    out.update({"workload": "fsi_4m with uniform +-0.01 dx jitter (seed 12345)", "steps": steps,
+                "unit": "particle-updates/s", "ratio_mixed_over_plain": out["mixed"] / out["plain"]})
+    return out
 
 
 def run_ensemble(dev, steps):

@@ -15,6 +15,9 @@ LIB_PATH = os.path.join(_PKG, "_build", "libfluidsim.so")
 # status codes
 OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENUMERIC, EIO = range(7)
 PRECISION_FP32, PRECISION_MIXED = 0, 1
+CONSERVATION_N = 10
+CONSERVATION_KEYS = ("fluid_mass", "solid_mass", "momentum_x", "momentum_y", "momentum_z", "kinetic_energy",
+                     "potential_energy", "fluid_elastic_energy", "fluid_density_excess", "solid_strain_energy")
 PHASE_CELL, PHASE_COUPLE, PHASE_VIRT, PHASE_FLUID, PHASE_SOLID = range(5)
 
 FIELDS = {
@@ -139,6 +142,7 @@ def load():
         "fsim_time_steps": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
         "fsim_time_sweep": (C.c_int, [P, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "fsim_launches_per_step": (C.c_int, [P, C.POINTER(C.c_int)]),
+        "fsim_conservation": (C.c_int, [P, C.POINTER(C.c_double), C.c_int]),
         "fsim_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
         "fsim_host_free": (C.c_int, [P]),
         "fsim_counts": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -168,7 +172,7 @@ EXPORTED = [
     "fsim_neighbor_counts", "fsim_get_cells", "fsim_write_vtk", "fsim_time_steps", "fsim_time_sweep",
     "fsim_launches_per_step", "fsim_host_alloc", "fsim_host_free", "fsim_counts", "fsim_get_derived",
     "fsim_cell_sort_noalloc", "fsim_batch_create", "fsim_batch_step", "fsim_batch_sync", "fsim_batch_time_steps",
-    "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes",
+    "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes", "fsim_conservation",
 ]
 
 
@@ -402,6 +406,12 @@ class Simulation:
         n = C.c_int()
         check(self.lib.fsim_launches_per_step(self.h, C.byref(n)))
         return n.value
+
+    def conservation(self):
+        """FP64 conservation totals (fsim_conservation) as a dict."""
+        out = (C.c_double * CONSERVATION_N)()
+        check(self.lib.fsim_conservation(self.h, out, CONSERVATION_N))
+        return dict(zip(CONSERVATION_KEYS, list(out)))
 
 
 class PinnedBuffer:

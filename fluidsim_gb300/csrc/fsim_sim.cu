@@ -22,6 +22,7 @@
 // output, no atomics on physics sums): results are deterministic.
 #include "fsim_internal.h"
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -47,6 +48,11 @@ struct DevParams {
     // domain
     float dmin[3], dmax[3], cmin[3], cinv[3];
     int nx, ny, nz, ncell;
+    // mixed form: cell size, domain bounds relative to the grid origin,
+    // density-deviation clamp, FP16 scales of the gathered deviations
+    float cdx[3], dlo_rel[3], dhi_rel[3];
+    float dlt_min, dlt_max, p_unit, p_unit_inv;
+    int mixed;
 };
 
 enum : unsigned { FLAG_OUT_OF_GRID = 1u };
@@ -378,6 +384,7 @@ __device__ __forceinline__ float tait_pressure(const DevParams &P, float rho)
 // reference's release build is compiled with -use_fast_math).
 struct PairAcc {
     float drho, ax, ay, az;
+    float drho_c; // compensation term of the density-rate sum (KAHAN)
 };
 
 __device__ __forceinline__ float ex2_approx(float x)
@@ -400,11 +407,40 @@ __device__ __forceinline__ float rcp_approx(float x)
 }
 
 // LIMITER: min(3 du, c0) (fluid, wall) or c0 (solid).  clamp_ps: P* >= 0 (wall).
-template <bool LIMITER, int VISCID>
+// KAHAN: the density-rate sum is Kahan-compensated (mixed form).
+template <bool LIMITER, int VISCID, bool KAHAN = false>
 __device__ __forceinline__ void riemann_pair(const DevParams &P, float dx, float dy, float dz, float r2, float uix,
                                              float uiy, float uiz, float rhoi, float pi, float ujx, float ujy,
                                              float ujz, float rhoj, float pj, bool clamp_ps, PairAcc &A)
 {
+    if (KAHAN) {
+        // The same terms with every rounding spelled out (no contraction
+        // freedom left to the compiler), so that every kernel inlining this
+        // rounds identically, and a Kahan-compensated density-rate sum.
+        const float w = __fmul_rn(ex2_approx(__fmul_rn(r2, P.exp2_scale)), P.kdiff);
+        const float inv_r = rsqrt_approx(fmaxf(r2, 1e-30f));
+        const float rs_inv = rcp_approx(__fadd_rn(rhoi, rhoj));
+        const float a = fmaf(__fsub_rn(uiz, ujz), dz, fmaf(__fsub_rn(uiy, ujy), dy, __fmul_rn(__fsub_rn(uix, ujx), dx)));
+        const float du = fmaxf(__fmul_rn(a, inv_r), 0.0f);
+        const float lim = LIMITER ? fminf(__fmul_rn(3.0f, du), P.c0) : P.c0;
+        float ps = __fmul_rn(fmaf(rhoi, pj, __fmul_rn(rhoj, pi)), rs_inv);
+        ps = fmaf(__fmul_rn(__fmul_rn(__fmul_rn(rhoi, rhoj), rs_inv), du), lim, ps);
+        if (clamp_ps) ps = fmaxf(ps, 0.0f);
+        const float r = __fmul_rn(r2, inv_r);
+        const float x = fmaf(rhoj, a, -__fmul_rn(__fmul_rn(__fsub_rn(pi, pj), r), P.c0_inv));
+        const float y = __fsub_rn(__fmul_rn(__fmul_rn(x, rs_inv), w), A.drho_c);
+        const float t = __fadd_rn(A.drho, y);
+        A.drho_c = __fsub_rn(__fsub_rn(t, A.drho), y);
+        A.drho = t;
+        float f = __fmul_rn(-2.0f, ps);
+        if (VISCID == 1 || (VISCID == 2 && P.viscid))
+            f = fmaf(__fmul_rn(P.mu10, -a), rcp_approx(__fadd_rn(r2, P.eps_h2)), f);
+        f = __fmul_rn(f, w);
+        A.ax = fmaf(f, dx, A.ax);
+        A.ay = fmaf(f, dy, A.ay);
+        A.az = fmaf(f, dz, A.az);
+        return;
+    }
     const float w = ex2_approx(r2 * P.exp2_scale) * P.kdiff;
     const float inv_r = rsqrt_approx(fmaxf(r2, 1e-30f)); // r2 = 0 (the particle itself) contributes 0
     const float rs_inv = rcp_approx(rhoi + rhoj);
@@ -438,6 +474,7 @@ struct FluidSweepArgs {
     float4 *dudt_out;
     int n;
     int keep; // write drho/dt and du/dt
+    const float2 *cm; // mixed form: per-cell (density deviation, pressure) references
 };
 
 // fluidUpdate (src/fluid.cu:234-269) applied to the sums of one particle: NaN
@@ -496,7 +533,7 @@ constexpr int kChunk = 16;    // candidates between capacity checks
 
 enum Species { kFluid = 0, kVirt = 1, kSolid = 2 };
 
-template <int SP, int VISCID>
+template <int SP, int VISCID, bool KAHAN = false>
 __device__ __forceinline__ void flush_list(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
                                            int &cnt, float4 pr, float4 vp, PairAcc &acc)
 {
@@ -508,15 +545,24 @@ __device__ __forceinline__ void flush_list(const DevParams &P, const FluidSweepA
                 const float4 q = A.s_pos[j], np = A.s_np[j], sv = A.s_vel[j];
                 const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
                 const float r2 = dist2(dx, dy, dz);
-                const float k2 = 2.0f * ((vp.x - sv.x) * np.x + (vp.y - sv.y) * np.y + (vp.z - sv.z) * np.z);
-                riemann_pair<false, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, vp.x - k2 * np.x,
-                                           vp.y - k2 * np.y, vp.z - k2 * np.z, pr.w, np.w, false, acc);
+                if (KAHAN) {
+                    const float k2 = __fmul_rn(2.0f, fmaf(__fsub_rn(vp.z, sv.z), np.z,
+                                                          fmaf(__fsub_rn(vp.y, sv.y), np.y,
+                                                               __fmul_rn(__fsub_rn(vp.x, sv.x), np.x))));
+                    riemann_pair<false, VISCID, true>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w,
+                                                      fmaf(-k2, np.x, vp.x), fmaf(-k2, np.y, vp.y),
+                                                      fmaf(-k2, np.z, vp.z), pr.w, np.w, false, acc);
+                } else {
+                    const float k2 = 2.0f * ((vp.x - sv.x) * np.x + (vp.y - sv.y) * np.y + (vp.z - sv.z) * np.z);
+                    riemann_pair<false, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, vp.x - k2 * np.x,
+                                                vp.y - k2 * np.y, vp.z - k2 * np.z, pr.w, np.w, false, acc);
+                }
             } else {
                 const float4 q = SP == kFluid ? A.posr[j] : A.v_posr[j];
                 const float4 u = SP == kFluid ? A.velp[j] : A.v_velp[j];
                 const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
                 const float r2 = dist2(dx, dy, dz);
-                riemann_pair<true, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q.w,
+                riemann_pair<true, VISCID, KAHAN>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q.w,
                                                 u.w, SP == kVirt, acc);
             }
         }
@@ -524,7 +570,7 @@ __device__ __forceinline__ void flush_list(const DevParams &P, const FluidSweepA
     cnt = 0;
 }
 
-template <int SP, bool CHECK_Z, int VISCID>
+template <int SP, bool CHECK_Z, int VISCID, bool KAHAN = false>
 __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
                                                int &cnt, bool in, int cz, int cx, int cy, int z0, int z1, float4 pr,
                                                float4 vp, PairAcc &acc)
@@ -542,7 +588,7 @@ __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSw
             const int je = start[base + z1];
             while (j < je) {
                 if (__reduce_max_sync(kFull, cnt) > kListCap - kChunk)
-                    flush_list<SP, VISCID>(P, A, lst, lane, cnt, pr, vp, acc);
+                    flush_list<SP, VISCID, KAHAN>(P, A, lst, lane, cnt, pr, vp, acc);
                 const int jend = min(j + kChunk, je);
 #pragma unroll 4
                 for (; j < jend; ++j) {
@@ -558,7 +604,7 @@ __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSw
             }
         }
     }
-    flush_list<SP, VISCID>(P, A, lst, lane, cnt, pr, vp, acc);
+    flush_list<SP, VISCID, KAHAN>(P, A, lst, lane, cnt, pr, vp, acc);
 }
 
 template <bool CHECK_Z, int VISCID>
@@ -779,6 +825,467 @@ __device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs
 }
 FSIM_BATCHED_KERNEL(kb_couple, CoupleArgs, couple_body, kBlock)
 
+// =================================================================== mixed form
+// Fluid state of the mixed form (same 2 x 16 bytes per particle as the plain
+// form, different contents):
+//   posr = (offset from the particle's cell corner, x y z FP32;
+//           FP16 pair: density deviation and pressure, each relative to the
+//           per-cell FP32 reference cm[cell], for neighbour gathers)
+//   velp = (u, v, w, delta = rho/rho0 - 1 in FP32: the particle's own density)
+// The cell of sorted particle i is cell_f[i] (kept valid for the current
+// order at all times), so x = cell_min + cell * interval + offset.  Pair
+// distances are differences of offsets plus whole cells, exact to the FP32
+// resolution of a cell (~1e-9 m) instead of the domain (~2e-7 m at 2.5 m).
+// The pressure is the Tait EOS of delta (expm1/log1p, no cancellation).
+// Wall particles store offsets from their own (static) cells the same way;
+// the solid keeps absolute FP32 positions.
+constexpr int kCodeShift = 26;                   // neighbour-list entry = j | cell code << 26
+constexpr int kIndexMask = (1 << kCodeShift) - 1;
+constexpr float kDeltaScale = 1024.0f;           // FP16 density-deviation scale
+constexpr float kDeltaUnit = 1.0f / 1024.0f;
+
+__device__ __forceinline__ float eos_delta(const DevParams &P, float d)
+{
+    return fmaxf(__fmul_rn(P.rho2p, expm1f(__fmul_rn(P.gamma, log1pf(d)))), P.min_p);
+}
+__device__ __forceinline__ void cell_xyz(const DevParams &P, int c, int &cx, int &cy, int &cz)
+{
+    const int row = c / P.nz;
+    cz = c - row * P.nz;
+    cx = row / P.ny;
+    cy = row - cx * P.ny;
+}
+__device__ __forceinline__ unsigned half2_bits(float a, float b)
+{
+    const __half2 h = __floats2half2_rn(a, b);
+    unsigned u;
+    memcpy(&u, &h, sizeof u);
+    return u;
+}
+__device__ __forceinline__ float2 half2_floats(float bits)
+{
+    const unsigned u = __float_as_uint(bits);
+    __half2 h;
+    memcpy(&h, &u, sizeof h);
+    return __half22float2(h);
+}
+
+// Cell phase, fluid hash of the mixed form: move every particle to the cell
+// its offset now lies in (offset -= whole cells) and hash it there.
+__device__ __forceinline__ int rebin_axis(float &off, int c, float inv, float d, int n, bool &bad)
+{
+    int t = c + (int)floorf(off * inv);
+    if (t < 0 || t >= n) {
+        bad = true;
+        t = t < 0 ? 0 : n - 1;
+    }
+    if (t != c) off -= (float)(t - c) * d;
+    return t;
+}
+struct HashMixedArgs {
+    float4 *pos;
+    const int *cell_old;
+    int n;
+    int *key, *slot, *cnt;
+    unsigned *flags;
+};
+__device__ __forceinline__ void hash_mixed_body(const DevParams &P, const HashMixedArgs &A, int blk)
+{
+    const int s = blk * blockDim.x + threadIdx.x;
+    if (s >= A.n) return;
+    float4 p = A.pos[s];
+    int cx, cy, cz;
+    cell_xyz(P, A.cell_old[s], cx, cy, cz);
+    bool bad = false;
+    cx = rebin_axis(p.x, cx, P.cinv[0], P.cdx[0], P.nx, bad);
+    cy = rebin_axis(p.y, cy, P.cinv[1], P.cdx[1], P.ny, bad);
+    cz = rebin_axis(p.z, cz, P.cinv[2], P.cdx[2], P.nz, bad);
+    if (bad) atomicOr(A.flags, FLAG_OUT_OF_GRID);
+    const int c = (cx * P.ny + cy) * P.nz + cz;
+    A.pos[s] = p;
+    A.key[s] = c;
+    A.slot[s] = atomicAdd(&A.cnt[c], 1);
+}
+FSIM_BATCHED_KERNEL(kb_hash_mixed, HashMixedArgs, hash_mixed_body, kBlock)
+
+// Per-cell references and the FP16 gather pair (after the sort): cm[c] =
+// mean (delta, p) of the cell's particles; each particle stores its
+// deviations from them as FP16 in posr.w.  Deviations inside a 2h cell are
+// small, so FP16 keeps them to ~1e-3 relative, i.e. ~0.01 Pa for hydrostatic
+// water at dx = 5 mm, where an absolute FP16 pressure would be ~3 Pa.
+struct CellRefArgs {
+    float4 *posr;
+    const float4 *velp;
+    const int *start;
+    float2 *cm;
+    int ncell;
+};
+__device__ __forceinline__ void cell_ref_body(const DevParams &P, const CellRefArgs &A, int blk)
+{
+    const int c = blk * blockDim.x + threadIdx.x;
+    if (c >= A.ncell) return;
+    const int b = A.start[c], e = A.start[c + 1];
+    if (b == e) return; // never read: no particle refers to an empty cell
+    float sd = 0.0f, sp = 0.0f;
+    for (int j = b; j < e; ++j) {
+        const float d = A.velp[j].w;
+        sd += d;
+        sp += eos_delta(P, d);
+    }
+    const float inv_n = 1.0f / (float)(e - b);
+    const float dm = sd * inv_n, pm = sp * inv_n;
+    A.cm[c] = make_float2(dm, pm);
+    float *w = reinterpret_cast<float *>(A.posr);
+    for (int j = b; j < e; ++j) {
+        const float d = A.velp[j].w;
+        w[4 * (size_t)j + 3] = __uint_as_float(half2_bits((d - dm) * kDeltaScale, (eos_delta(P, d) - pm) * P.p_unit_inv));
+    }
+}
+FSIM_BATCHED_KERNEL(kb_cell_ref, CellRefArgs, cell_ref_body, kBlock)
+
+// Own particle of the mixed sweep.
+struct OwnMixed {
+    float bx, by, bz; // offset + one cell: the list's cell code b in {0,1,2} gives offset - (b - 1) cell
+    int cbase;        // linear cell of code (0, 0, 0)
+    float rho, p;
+};
+
+template <int SP, int VISCID>
+__device__ __forceinline__ void flush_list_m(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
+                                             int &cnt, const OwnMixed &o, float4 vp, PairAcc &acc)
+{
+    const int m = __reduce_max_sync(kFull, cnt);
+    const int nynz = P.ny * P.nz;
+    for (int k = 0; k < m; ++k) {
+        if (k < cnt) {
+            const unsigned e = (unsigned)lst[k][lane];
+            const int j = (int)(e & kIndexMask);
+            const int bx = (e >> kCodeShift) & 3u, by = (e >> (kCodeShift + 2)) & 3u, bz = e >> (kCodeShift + 4);
+            const float4 q = SP == kFluid ? A.posr[j] : A.v_posr[j];
+            const float4 u = SP == kFluid ? A.velp[j] : A.v_velp[j];
+            const float dx = q.x - fmaf(-(float)bx, P.cdx[0], o.bx);
+            const float dy = q.y - fmaf(-(float)by, P.cdx[1], o.by);
+            const float dz = q.z - fmaf(-(float)bz, P.cdx[2], o.bz);
+            const float r2 = dist2(dx, dy, dz);
+            float rhoj, pj;
+            if (SP == kFluid) {
+                const float2 ref = A.cm[o.cbase + bx * nynz + by * P.nz + bz];
+                const float2 dev = half2_floats(q.w);
+                rhoj = fmaf(P.rho0, fmaf(dev.x, kDeltaUnit, ref.x), P.rho0);
+                pj = fmaf(dev.y, P.p_unit, ref.y);
+            } else {
+                rhoj = q.w;
+                pj = u.w;
+            }
+            riemann_pair<true, VISCID, true>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, o.rho, o.p, u.x, u.y, u.z, rhoj,
+                                             pj, SP == kVirt, acc);
+        }
+    }
+    cnt = 0;
+}
+
+// Candidate stream of the mixed sweep: the union rows, cell by cell, so that
+// every candidate's cell (relative to the lane's own) is known; it travels
+// with the list entry as a 6-bit code.  Each lane only takes candidates from
+// its own 27 cells.
+template <int SP, int VISCID>
+__device__ __forceinline__ void gather_species_m(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
+                                                 int &cnt, bool in, int cz, int cx, int cy, int z0, int z1,
+                                                 float4 off, const OwnMixed &o, float4 vp, PairAcc &acc)
+{
+    const int *start = SP == kFluid ? A.start_f : A.start_v;
+    const float4 *pos = SP == kFluid ? A.posr : A.v_posr;
+    for (int ox = -1; ox <= 1; ++ox) {
+        const int x = cx + ox;
+        if (x < 0 || x >= P.nx) continue;
+        const float psx = fmaf(-(float)ox, P.cdx[0], off.x);
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int y = cy + oy;
+            if (y < 0 || y >= P.ny) continue;
+            const float psy = fmaf(-(float)oy, P.cdx[1], off.y);
+            const int rb = (x * P.ny + y) * P.nz;
+            const unsigned code_xy = (unsigned)(ox + 1) | ((unsigned)(oy + 1) << 2);
+            int j = start[rb + z0];
+            for (int z = z0; z < z1; ++z) {
+                const int je = start[rb + z + 1];
+                const int dzc = z - cz;
+                const bool inz = in && dzc >= -1 && dzc <= 1;
+                const float psz = fmaf(-(float)dzc, P.cdx[2], off.z);
+                const unsigned code = (code_xy | ((unsigned)(dzc + 1) << 4)) << kCodeShift;
+                while (j < je) {
+                    if (__reduce_max_sync(kFull, cnt) > kListCap - kChunk)
+                        flush_list_m<SP, VISCID>(P, A, lst, lane, cnt, o, vp, acc);
+                    const int jend = min(j + kChunk, je);
+#pragma unroll 4
+                    for (; j < jend; ++j) {
+                        const float4 q = pos[j]; // a broadcast
+                        const float r2 = dist2(q.x - psx, q.y - psy, q.z - psz);
+                        if (inz && r2 < P.R2) lst[cnt++][lane] = (int)(code | (unsigned)j);
+                    }
+                }
+            }
+        }
+    }
+    flush_list_m<SP, VISCID>(P, A, lst, lane, cnt, o, vp, acc);
+}
+
+// fluidUpdate (src/fluid.cu:234-269) in the mixed form: delta and offsets.
+__device__ __forceinline__ void fluid_update_store_m(const DevParams &P, const FluidSweepArgs &A, int i, float4 off,
+                                                     float4 vp, float rho, const PairAcc &acc, int cx, int cy, int cz)
+{
+    // explicit roundings throughout (see riemann_pair's KAHAN branch)
+    const float rho_inv = __fdividef(1.0f, rho);
+    float drho = __fmul_rn(__fmul_rn(2.0f, rho), acc.drho);
+    float ax = __fmul_rn(acc.ax, rho_inv), ay = __fmul_rn(acc.ay, rho_inv), az = __fmul_rn(acc.az, rho_inv);
+    if (!(drho == drho)) drho = 0.0f;
+    if (!(ax == ax && ay == ay && az == az)) ax = ay = az = 0.0f;
+    float x = fmaf(vp.x, P.dt, off.x), y = fmaf(vp.y, P.dt, off.y), z = fmaf(vp.z, P.dt, off.z);
+    float ux = fmaf(__fadd_rn(ax, P.gx), P.dt, vp.x), uy = fmaf(__fadd_rn(ay, P.gy), P.dt, vp.y),
+          uz = fmaf(__fadd_rn(az, P.gz), P.dt, vp.z);
+    float d = fmaf(__fmul_rn(drho, P.rho0_inv), P.dt, vp.w);
+    d = fminf(fmaxf(d, P.dlt_min), P.dlt_max);
+    x = fminf(fmaxf(x, fmaf(-(float)cx, P.cdx[0], P.dlo_rel[0])), fmaf(-(float)cx, P.cdx[0], P.dhi_rel[0]));
+    y = fminf(fmaxf(y, fmaf(-(float)cy, P.cdx[1], P.dlo_rel[1])), fmaf(-(float)cy, P.cdx[1], P.dhi_rel[1]));
+    z = fminf(fmaxf(z, fmaf(-(float)cz, P.cdx[2], P.dlo_rel[2])), fmaf(-(float)cz, P.cdx[2], P.dhi_rel[2]));
+    const float speed = __fsqrt_rn(fmaf(uz, uz, fmaf(uy, uy, __fmul_rn(ux, ux))));
+    if (speed > P.vmax) {
+        const float s = __fdiv_rn(P.vmax, speed);
+        ux = __fmul_rn(ux, s);
+        uy = __fmul_rn(uy, s);
+        uz = __fmul_rn(uz, s);
+    }
+    A.posr_out[i] = make_float4(x, y, z, 0.0f);
+    A.velp_out[i] = make_float4(ux, uy, uz, d);
+    A.orig_out[i] = A.orig_in[i];
+    if (A.keep) {
+        A.drho_out[i] = drho;
+        A.dudt_out[i] = make_float4(ax, ay, az, 0.0f);
+    }
+}
+
+template <int VISCID>
+__device__ __forceinline__ void fluid_sweep_mixed_body(const DevParams &P, const FluidSweepArgs &A, int blk)
+{
+    __shared__ int lists[kSweepWarps][kListCap][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = (blk * kSweepWarps + warp) * 32 + lane;
+    const bool valid = i < A.n;
+    int(*lst)[32] = lists[warp];
+    const float4 off = valid ? A.posr[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 vp = valid ? A.velp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const int cell = valid ? A.cell_f[i] : 0;
+    int cx, cy, cz;
+    cell_xyz(P, cell, cx, cy, cz);
+    const int row = cell / P.nz;
+    OwnMixed o;
+    o.bx = __fadd_rn(off.x, P.cdx[0]);
+    o.by = __fadd_rn(off.y, P.cdx[1]);
+    o.bz = __fadd_rn(off.z, P.cdx[2]);
+    o.cbase = cell - P.ny * P.nz - P.nz - 1;
+    o.rho = fmaf(P.rho0, vp.w, P.rho0);
+    o.p = eos_delta(P, vp.w);
+    // absolute position and (rho, p) for the solid pairs, in the plain layout
+    const float4 pa = make_float4(__fadd_rn(fmaf((float)cx, P.cdx[0], P.cmin[0]), off.x),
+                                  __fadd_rn(fmaf((float)cy, P.cdx[1], P.cmin[1]), off.y),
+                                  __fadd_rn(fmaf((float)cz, P.cdx[2], P.cmin[2]), off.z), o.rho);
+    const float4 va = make_float4(vp.x, vp.y, vp.z, o.p);
+    PairAcc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    int cnt = 0;
+    unsigned remaining = __ballot_sync(kFull, valid);
+    while (remaining) {
+        const int leader = __ffs(remaining) - 1;
+        const int grow = __shfl_sync(kFull, row, leader);
+        const unsigned grp = __ballot_sync(kFull, valid && row == grow);
+        remaining &= ~grp;
+        const bool in = (grp >> lane) & 1u;
+        const int zlo = __reduce_min_sync(kFull, in ? cz : INT_MAX);
+        const int zhi = __reduce_max_sync(kFull, in ? cz : INT_MIN);
+        const int z0 = max(zlo - 1, 0), z1 = min(zhi + 1, P.nz - 1) + 1;
+        const int gx = grow / P.ny, gy = grow - gx * P.ny;
+        gather_species_m<kFluid, VISCID>(P, A, lst, lane, cnt, in, cz, gx, gy, z0, z1, off, o, vp, acc);
+        gather_species_m<kVirt, VISCID>(P, A, lst, lane, cnt, in, cz, gx, gy, z0, z1, off, o, vp, acc);
+        gather_species<kSolid, false, VISCID, true>(P, A, lst, lane, cnt, in, cz, gx, gy, z0, z1, pa, va, acc);
+    }
+    if (valid) fluid_update_store_m(P, A, i, off, vp, o.rho, acc, cx, cy, cz);
+}
+
+template <int VISCID>
+__global__ void __launch_bounds__(kSweepWarps * 32) kb_fluid_sweep_m(const Item<FluidSweepArgs> *__restrict__ items,
+                                                                     const int *__restrict__ bstart, int ninst)
+{
+    const int inst = locate_instance(bstart, ninst, blockIdx.x);
+    const DevParams P = items[inst].P;
+    fluid_sweep_mixed_body<VISCID>(P, items[inst].A, (int)blockIdx.x - bstart[inst]);
+}
+template <int VISCID>
+__global__ void __launch_bounds__(kSweepWarps * 32) kb_fluid_sweep_m1(const DevParams P, const FluidSweepArgs A)
+{
+    fluid_sweep_mixed_body<VISCID>(P, A, (int)blockIdx.x);
+}
+
+// getVirtData (src/virt.cu:9-75) in the mixed form.
+__device__ __forceinline__ void virt_mixed_body(const DevParams &P, const VirtArgs &A, int blk)
+{
+    const int i = blk * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    const float4 xi = A.v_posr_in[i]; // offset from the wall particle's cell
+    int cx, cy, cz;
+    cell_xyz(P, A.v_cell[i], cx, cy, cz);
+    float best = FSIM_LARGE_FLOAT;
+    int best_j = -1, best_orig = INT_MAX;
+    float bsx = 0.0f, bsy = 0.0f, bsz = 0.0f;
+    const int z0 = max(cz - 1, 0), z1 = min(cz + 1, P.nz - 1) + 1;
+    for (int ox = -1; ox <= 1; ++ox) {
+        const int x = cx + ox;
+        if (x < 0 || x >= P.nx) continue;
+        const float psx = fmaf(-(float)ox, P.cdx[0], xi.x);
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int y = cy + oy;
+            if (y < 0 || y >= P.ny) continue;
+            const float psy = fmaf(-(float)oy, P.cdx[1], xi.y);
+            const int rb = (x * P.ny + y) * P.nz;
+            for (int z = z0; z < z1; ++z) {
+                const float psz = fmaf(-(float)(z - cz), P.cdx[2], xi.z);
+                for (int j = A.start_f[rb + z], je = A.start_f[rb + z + 1]; j < je; ++j) {
+                    const float4 q = A.fposr[j];
+                    const float d2 = dist2(q.x - psx, q.y - psy, q.z - psz);
+                    bool take = d2 < best;
+                    if (!take && d2 == best) take = A.forig[j] < best_orig;
+                    if (take) {
+                        best = d2;
+                        best_j = j;
+                        best_orig = A.forig[j];
+                        bsx = psx;
+                        bsy = psy;
+                        bsz = psz;
+                    }
+                }
+            }
+        }
+    }
+    float rho = P.rho0, p = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
+    if (best_j >= 0) {
+        const float4 q = A.fposr[best_j], u = A.fvelp[best_j];
+        rho = fmaf(P.rho0, u.w, P.rho0);
+        p = eos_delta(P, u.w) - rho * (P.gx * (q.x - bsx) + P.gy * (q.y - bsy) + P.gz * (q.z - bsz));
+        ux = u.x;
+        uy = u.y;
+        uz = u.z;
+    }
+    const float4 nrm = A.v_normal[i];
+    const float k2 = 2.0f * (ux * nrm.x + uy * nrm.y + uz * nrm.z);
+    A.v_posr[i] = make_float4(xi.x, xi.y, xi.z, rho);
+    A.v_velp[i] = make_float4(ux - k2 * nrm.x, uy - k2 * nrm.y, uz - k2 * nrm.z, p);
+}
+FSIM_BATCHED_KERNEL(kb_virt_mixed, VirtArgs, virt_mixed_body, kBlock)
+
+// A fluid candidate of a warp-per-solid-particle row walk in the mixed form:
+// its z cell from the row's cell boundaries, its position relative to the
+// solid particle from the offset.
+struct RowMixed {
+    int b1, b2, z0;  // start of the row's 2nd and 3rd cell, first cell
+    float sx, sy;    // solid offset minus the row's x/y cell shift
+};
+__device__ __forceinline__ void fluid_rel(const DevParams &P, const RowMixed &R, int j, float sz0, float4 q, float &dx,
+                                          float &dy, float &dz)
+{
+    const int k = (j >= R.b1) + (j >= R.b2);
+    dx = q.x - R.sx;
+    dy = q.y - R.sy;
+    dz = q.z - fmaf(-(float)k, P.cdx[2], sz0);
+}
+
+
+// The mixed-form row walk of a solid particle: calls f(j, q, dx, dy, dz) for
+// every fluid candidate of the 27 cells of solid cell `cell`, lanes of a group
+// of `G` taking every G-th candidate of a row.
+template <int G, class F>
+__device__ __forceinline__ void solid_fluid_walk_m(const DevParams &P, const int *__restrict__ start_f,
+                                                   const float4 *__restrict__ fposr, int cell, float4 xi, int g, F &&f)
+{
+    int cx, cy, cz;
+    cell_xyz(P, cell, cx, cy, cz);
+    const float sox = xi.x - fmaf((float)cx, P.cdx[0], P.cmin[0]);
+    const float soy = xi.y - fmaf((float)cy, P.cdx[1], P.cmin[1]);
+    const float soz = xi.z - fmaf((float)cz, P.cdx[2], P.cmin[2]);
+    const int z0 = max(cz - 1, 0), z1 = min(cz + 1, P.nz - 1) + 1;
+    const float sz0 = fmaf(-(float)(z0 - cz), P.cdx[2], soz);
+    for (int ox = -1; ox <= 1; ++ox) {
+        const int x = cx + ox;
+        if (x < 0 || x >= P.nx) continue;
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int y = cy + oy;
+            if (y < 0 || y >= P.ny) continue;
+            const int rb = (x * P.ny + y) * P.nz;
+            RowMixed R;
+            R.z0 = z0;
+            R.b1 = start_f[rb + min(z0 + 1, z1)];
+            R.b2 = start_f[rb + min(z0 + 2, z1)];
+            R.sx = fmaf(-(float)ox, P.cdx[0], sox);
+            R.sy = fmaf(-(float)oy, P.cdx[1], soy);
+            for (int j = start_f[rb + z0] + g, je = start_f[rb + z1]; j < je; j += G) {
+                const float4 q = fposr[j];
+                float dx, dy, dz;
+                fluid_rel(P, R, j, sz0, q, dx, dy, dz);
+                f(j, dx, dy, dz);
+            }
+        }
+    }
+}
+
+// solidCoupleUpdate (src/solid.cu:262-344) in the mixed form.
+__device__ __forceinline__ void couple_mixed_body(const DevParams &P, const CoupleArgs &A, int blk)
+{
+    const int i = (blk * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= A.n) return; // whole warp
+    const float4 xi = A.s_pos[i];
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f, psum = 0.0f, wsum = 0.0f;
+    solid_fluid_walk_m<32>(P, A.start_f, A.fposr, A.s_cell[i], xi, lane, [&](int j, float dx, float dy, float dz) {
+        const float r2 = dist2(dx, dy, dz);
+        if (r2 < P.R2) {
+            const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
+            wsum += w;
+            psum += eos_delta(P, A.fvelp[j].w) * w;
+        }
+    });
+    Rows rows;
+    neighbor_rows(P, A.s_cell[i], rows);
+    for (int r = 0; r < rows.count; ++r) {
+        const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+        for (int j = A.start_s[c0] + lane, je = A.start_s[c1]; j < je; j += 32) {
+            const float4 q = A.s_pos[j];
+            const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2) {
+                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+                nx -= dx * w;
+                ny -= dy * w;
+                nz -= dz * w;
+            }
+        }
+    }
+    nx = warp_sum(nx);
+    ny = warp_sum(ny);
+    nz = warp_sum(nz);
+    psum = warp_sum(psum);
+    wsum = warp_sum(wsum);
+    if (lane) return;
+    const float l2 = nx * nx + ny * ny + nz * nz;
+    if (l2 < FSIM_EPS_FOR_SUM) {
+        nx = ny = nz = 0.0f;
+    } else {
+        const float s = rsqrtf(l2);
+        nx *= s;
+        ny *= s;
+        nz *= s;
+    }
+    const float p = wsum > FSIM_EPS_FLOAT ? fmaxf(psum / wsum, P.min_p) : 0.0f;
+    A.s_np[i] = make_float4(nx, ny, nz, p);
+}
+FSIM_BATCHED_KERNEL(kb_couple_mixed, CoupleArgs, couple_mixed_body, kBlock)
+
+
 // ------------------------------------------------------------ solid
 struct SolidArgs {
     float4 *pos, *vel;
@@ -844,6 +1351,8 @@ __device__ __forceinline__ float group_sum(float v)
 // reference-configuration neighbours, L^-1 (identity when singular),
 // F <- F L^-1, Green strain, St-Venant-Kirchhoff 2nd Piola, P = F S.
 // Also stores P L^-1 and cof(F) L^-1 (= det(F) F^-T L^-1) for the force sweep.
+// MIXED: L^-1 is formed in FP64 (cofactors, determinant, division) and rounded.
+template <bool MIXED>
 __device__ __forceinline__ void solid_deform_body(const DevParams &P, const SolidArgs &S, int blk)
 {
     const int t = blk * blockDim.x + threadIdx.x;
@@ -880,9 +1389,27 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
         L.m[k] = group_sum(L.m[k]);
     }
     if (!valid || g) return;
+    M3 Linv;
+    if (MIXED) {
+        double l[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) l[k] = (double)L.m[k];
+        const double c0 = l[4] * l[8] - l[5] * l[7], c1 = l[5] * l[6] - l[3] * l[8], c2 = l[3] * l[7] - l[4] * l[6];
+        const double det = l[0] * c0 + l[1] * c1 + l[2] * c2;
+        if (det != 0.0) {
+            const double id = 1.0 / det;
+            const double inv[9] = {c0 * id, (l[2] * l[7] - l[1] * l[8]) * id, (l[1] * l[5] - l[2] * l[4]) * id,
+                                   c1 * id, (l[0] * l[8] - l[2] * l[6]) * id, (l[2] * l[3] - l[0] * l[5]) * id,
+                                   c2 * id, (l[1] * l[6] - l[0] * l[7]) * id, (l[0] * l[4] - l[1] * l[3]) * id};
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Linv.m[k] = (float)inv[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Linv.m[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+        }
+    } else {
     const M3 cl = cofactor(L);
     const float det = L.m[0] * cl.m[0] + L.m[1] * cl.m[1] + L.m[2] * cl.m[2];
-    M3 Linv;
     if (det != 0.0f) {
         const float id = 1.0f / det;
 #pragma unroll
@@ -892,6 +1419,7 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
     } else {
 #pragma unroll
         for (int k = 0; k < 9; ++k) Linv.m[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+    }
     }
     F = mmul(F, Linv);
     // E = (F^T F - I)/2, S = 2 mu E + lambda tr(E) I, P = F S
@@ -918,12 +1446,15 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
         S.AV[9 * i + k] = AV.m[k];
     }
 }
-FSIM_BATCHED_KERNEL(kb_solid_deform, SolidArgs, solid_deform_body, kBlock)
+FSIM_BATCHED_KERNEL(kb_solid_deform, SolidArgs, solid_deform_body<false>, kBlock)
+FSIM_BATCHED_KERNEL(kb_solid_deform_mixed, SolidArgs, solid_deform_body<true>, kBlock)
 
 // solidForceCalculate (src/solid.cu:81-207): fluid traction over the fluid
 // neighbours (current configuration, fluid already advanced; candidates from
 // the 27 cells of the step-start cell) plus stress divergence and artificial
 // viscosity over the reference-configuration solid neighbours.
+// MIXED: fluid positions are cell offsets, fluid (rho, p) come from delta.
+template <bool MIXED>
 __device__ __forceinline__ void solid_force_body(const DevParams &P, const SolidArgs &S, int blk)
 {
     const int t = blk * blockDim.x + threadIdx.x;
@@ -932,9 +1463,33 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
     float cx = 0.0f, cy = 0.0f, cz = 0.0f, ax = 0.0f, ay = 0.0f, az = 0.0f;
     if (valid) {
         const float4 xi = S.pos[i], vi = S.vel[i], ni = S.np[i];
+        // solidFluidCouple (src/solid.cu:81-117)
+        auto traction = [&](float dx, float dy, float dz, float r2, float4 u, float rhoj, float pj) {
+            const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+            const float k2 = 2.0f * ((u.x - vi.x) * ni.x + (u.y - vi.y) * ni.y + (u.z - vi.z) * ni.z);
+            const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+            const float du = -k2 * (ni.x * dx + ni.y * dy + ni.z * dz) * inv_r;
+            float ps = 0.5f * (ni.w + pj);
+            if (du >= 0.0f) ps += 0.5f * rhoj * du * P.c0;
+            const float f = -2.0f * ps * P.rho_s_inv * w;
+            cx += f * dx;
+            cy += f * dy;
+            cz += f * dz;
+        };
+        if (MIXED) {
+            solid_fluid_walk_m<kSolidGroup>(P, S.start_f, S.fposr, S.cell[i], xi, g,
+                                            [&](int j, float dx, float dy, float dz) {
+                                                const float r2 = dist2(dx, dy, dz);
+                                                if (r2 < P.R2) {
+                                                    const float4 u = S.fvelp[j];
+                                                    traction(dx, dy, dz, r2, u, fmaf(P.rho0, u.w, P.rho0),
+                                                             eos_delta(P, u.w));
+                                                }
+                                            });
+        }
         Rows rows;
         neighbor_rows(P, S.cell[i], rows);
-        // solidFluidCouple (src/solid.cu:81-117)
+        if (MIXED) rows.count = 0;
         for (int r = 0; r < rows.count; ++r) {
             const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
             for (int j = S.start_f[c0] + g, je = S.start_f[c1]; j < je; j += kSolidGroup) {
@@ -996,7 +1551,8 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
     S.couple[i] = make_float4(cx, cy, cz, 0.0f);
     S.dudt[i] = make_float4(ax + cx, ay + cy, az + cz, 0.0f);
 }
-FSIM_BATCHED_KERNEL(kb_solid_force, SolidArgs, solid_force_body, kBlock)
+FSIM_BATCHED_KERNEL(kb_solid_force, SolidArgs, solid_force_body<false>, kBlock)
+FSIM_BATCHED_KERNEL(kb_solid_force_mixed, SolidArgs, solid_force_body<true>, kBlock)
 
 // Kernel weight of every static solid neighbour pair (once, at creation).
 __global__ void k_solid_pair_weights(const DevParams P, float4 *__restrict__ dXw, int n)
@@ -1031,6 +1587,7 @@ __device__ __forceinline__ void solid_update_body(const DevParams &P, const Soli
     }
 }
 FSIM_BATCHED_KERNEL(kb_solid_update, SolidArgs, solid_update_body, kBlock)
+
 
 // ------------------------------------------------------- neighbour counts
 __global__ void k_neighbor_counts(const DevParams P, const float4 *__restrict__ fposr, const int *__restrict__ cell_f,
@@ -1118,6 +1675,183 @@ __global__ void k_pack_f4(const float *__restrict__ xyz, const float *__restrict
     out[s] = make_float4(xyz[3 * s], xyz[3 * s + 1], xyz[3 * s + 2], w ? w[s] : wconst);
 }
 
+// Mixed form conversions (FP64 arithmetic, once per particle).
+__device__ __forceinline__ double cell_corner(const DevParams &P, int axis, int c)
+{
+    return (double)P.cmin[axis] + (double)c * (double)P.cdx[axis];
+}
+// plain (x, y, z, rho) / (u, v, w, p) -> mixed offsets / delta; the cell of
+// every particle from the FP32 cell index of its position
+__global__ void k_fluid_to_mixed(const DevParams P, float4 *__restrict__ posr, float4 *__restrict__ velp,
+                                 int *__restrict__ cell, int n, unsigned *flags)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const float4 p = posr[s];
+    const int c = cell_index(P, p.x, p.y, p.z, flags);
+    int cx, cy, cz;
+    cell_xyz(P, c, cx, cy, cz);
+    posr[s] = make_float4((float)((double)p.x - cell_corner(P, 0, cx)), (float)((double)p.y - cell_corner(P, 1, cy)),
+                          (float)((double)p.z - cell_corner(P, 2, cz)), 0.0f);
+    velp[s].w = (float)((double)p.w / (double)P.rho0 - 1.0);
+    cell[s] = c;
+}
+// absolute positions -> offsets from the given cells (wall particles)
+__global__ void k_offsets_in_cells(const DevParams P, float4 *__restrict__ pos, const int *__restrict__ cell, int n)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    float4 p = pos[s];
+    int cx, cy, cz;
+    cell_xyz(P, cell[s], cx, cy, cz);
+    p.x = (float)((double)p.x - cell_corner(P, 0, cx));
+    p.y = (float)((double)p.y - cell_corner(P, 1, cy));
+    p.z = (float)((double)p.z - cell_corner(P, 2, cz));
+    pos[s] = p;
+}
+enum MixedField { MF_POS = 0, MF_RHO = 1, MF_P = 2 };
+// out[orig[s]] = absolute position / density / pressure of a mixed-form particle
+__global__ void k_unpermute_mixed(const DevParams P, const float4 *__restrict__ pos, const float4 *__restrict__ velp,
+                                  const int *__restrict__ cell, const int *__restrict__ orig, int n, int what,
+                                  float *__restrict__ out)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int o = orig[s];
+    if (what == MF_POS) {
+        const float4 p = pos[s];
+        int cx, cy, cz;
+        cell_xyz(P, cell[s], cx, cy, cz);
+        out[3 * o] = (float)(cell_corner(P, 0, cx) + (double)p.x);
+        out[3 * o + 1] = (float)(cell_corner(P, 1, cy) + (double)p.y);
+        out[3 * o + 2] = (float)(cell_corner(P, 2, cz) + (double)p.z);
+    } else {
+        const double d = (double)velp[s].w;
+        if (what == MF_RHO) {
+            out[o] = (float)((double)P.rho0 * (1.0 + d));
+        } else {
+            const double pr = (double)P.rho2p * expm1((double)P.gamma * log1p(d));
+            out[o] = (float)fmax(pr, (double)P.min_p);
+        }
+    }
+}
+// set a mixed-form position (offset from the particle's current cell) or density
+__global__ void k_permute_in_mixed(const DevParams P, float4 *__restrict__ pos, float4 *__restrict__ velp,
+                                   const int *__restrict__ cell, const int *__restrict__ orig, int n, int what,
+                                   const float *__restrict__ in)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int o = orig[s];
+    if (what == MF_POS) {
+        float4 p = pos[s];
+        int cx, cy, cz;
+        cell_xyz(P, cell[s], cx, cy, cz);
+        p.x = (float)((double)in[3 * o] - cell_corner(P, 0, cx));
+        p.y = (float)((double)in[3 * o + 1] - cell_corner(P, 1, cy));
+        p.z = (float)((double)in[3 * o + 2] - cell_corner(P, 2, cz));
+        pos[s] = p;
+    } else {
+        velp[s].w = (float)((double)in[o] / (double)P.rho0 - 1.0);
+    }
+}
+
+
+// ------------------------------------------------- conservation (FP64)
+// Per-particle terms in FP64, block sums in a fixed tree order; the host adds
+// the block sums in order.  Layout of a block's terms: FSIM_CONSERVATION_N.
+__device__ __forceinline__ double block_sum_d(double v, double *sh)
+{
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+// specific elastic energy of the Tait EOS, integral_rho0^rho p / rho'^2, in delta
+__device__ __forceinline__ double tait_energy(const DevParams &P, double d)
+{
+    const double g1 = (double)P.gamma - 1.0;
+    const double l = log1p(d);
+    const double a = g1 != 0.0 ? expm1(g1 * l) / g1 : l;
+    return (double)P.rho2p / (double)P.rho0 * (a - d / (1.0 + d));
+}
+__global__ void __launch_bounds__(kBlock) k_conservation_fluid(const DevParams P, const float4 *__restrict__ posr,
+                                                               const float4 *__restrict__ velp,
+                                                               const int *__restrict__ cell, int n, double vol,
+                                                               double *__restrict__ partials)
+{
+    __shared__ double sh[kBlock];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double t[FSIM_CONSERVATION_N] = {};
+    if (s < n) {
+        const float4 p = posr[s], u = velp[s];
+        double x = p.x, y = p.y, z = p.z, d;
+        if (P.mixed) {
+            int cx, cy, cz;
+            cell_xyz(P, cell[s], cx, cy, cz);
+            x += cell_corner(P, 0, cx);
+            y += cell_corner(P, 1, cy);
+            z += cell_corner(P, 2, cz);
+            d = (double)u.w;
+        } else {
+            d = (double)p.w / (double)P.rho0 - 1.0;
+        }
+        const double m = (double)P.rho0 * vol;
+        const double ux = u.x, uy = u.y, uz = u.z;
+        t[0] = m;
+        t[2] = m * ux;
+        t[3] = m * uy;
+        t[4] = m * uz;
+        t[5] = 0.5 * m * (ux * ux + uy * uy + uz * uz);
+        t[6] = -m * ((double)P.gx * x + (double)P.gy * y + (double)P.gz * z);
+        t[7] = m * tait_energy(P, d);
+        t[8] = (double)P.rho0 * d * vol;
+    }
+#pragma unroll 1
+    for (int k = 0; k < FSIM_CONSERVATION_N; ++k) {
+        const double r = block_sum_d(t[k], sh);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * FSIM_CONSERVATION_N + k] = r;
+    }
+}
+__global__ void __launch_bounds__(kBlock) k_conservation_solid(const DevParams P, const float4 *__restrict__ pos,
+                                                               const float4 *__restrict__ vel,
+                                                               const float *__restrict__ F, int n, double rho_s,
+                                                               double vol, double *__restrict__ partials)
+{
+    __shared__ double sh[kBlock];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double t[FSIM_CONSERVATION_N] = {};
+    if (s < n) {
+        const float4 p = pos[s], u = vel[s];
+        const double m = rho_s * vol;
+        const double ux = u.x, uy = u.y, uz = u.z;
+        t[1] = m;
+        t[2] = m * ux;
+        t[3] = m * uy;
+        t[4] = m * uz;
+        t[5] = 0.5 * m * (ux * ux + uy * uy + uz * uz);
+        t[6] = -m * ((double)P.gx * p.x + (double)P.gy * p.y + (double)P.gz * p.z);
+        double f[9], E[9];
+        for (int k = 0; k < 9; ++k) f[k] = F[9 * (size_t)s + k];
+        for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c)
+                E[3 * a + c] = 0.5 * (f[a] * f[c] + f[3 + a] * f[3 + c] + f[6 + a] * f[6 + c] - (a == c ? 1.0 : 0.0));
+        double ee = 0.0;
+        for (int k = 0; k < 9; ++k) ee += E[k] * E[k];
+        const double tr = E[0] + E[4] + E[8];
+        t[9] = vol * ((double)P.mu_s * ee + 0.5 * (double)P.lambda * tr * tr);
+    }
+#pragma unroll 1
+    for (int k = 0; k < FSIM_CONSERVATION_N; ++k) {
+        const double r = block_sum_d(t[k], sh);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * FSIM_CONSERVATION_N + k] = r;
+    }
+}
 } // namespace
 
 // =================================================================== handle
@@ -1140,6 +1874,8 @@ struct fsim_sim {
     int *f_orig[2] = {};
     int *f_cell = nullptr, *f_key = nullptr, *f_slot = nullptr, *f_tmp = nullptr;
     int *f_cnt = nullptr, *f_start = nullptr;
+    float2 *f_cm = nullptr;  // mixed form: per-cell (delta, p) references of the FP16 gather
+    bool mixed = false;
     float *f_drho = nullptr;
     float4 *f_dudt = nullptr;
     int f_cur = 0;
@@ -1283,6 +2019,28 @@ void fill_params(fsim_sim *h)
     P.ny = d.cell_number[1];
     P.nz = d.cell_number[2];
     P.ncell = d.cell_number_total;
+    // mixed form
+    P.mixed = c.precision == FSIM_PRECISION_MIXED ? 1 : 0;
+    for (int k = 0; k < 3; ++k) {
+        P.cdx[k] = d.interval[k];
+        P.dlo_rel[k] = (float)((double)lo[k] - (double)d.cell_min[k]);
+        P.dhi_rel[k] = (float)((double)hi[k] - (double)d.cell_min[k]);
+    }
+    const double rho0 = c.fluid_density;
+    P.dlt_min = (float)((double)d.min_density / rho0 - 1.0);
+    P.dlt_max = (float)((double)d.max_density / rho0 - 1.0);
+    // FP16 unit of the gathered pressure deviation: a power of two such that
+    // the largest possible deviation (EOS at the density bounds, the pressure
+    // floor) stays below 2^15 units
+    {
+        const double g = c.gamma, b = d.coefficient_rho2p;
+        const double pmax = b * (std::pow(1.0 + P.dlt_max, g) - 1.0);
+        const double pmin = std::max((double)c.min_pressure, b * (std::pow(1.0 + P.dlt_min, g) - 1.0));
+        const double span = std::max(pmax - pmin, 1e-30);
+        const int e = (int)std::ceil(std::log2(span / 32768.0));
+        P.p_unit = (float)std::ldexp(1.0, e);
+        P.p_unit_inv = (float)std::ldexp(1.0, -e);
+    }
 }
 
 // ---------------------------------------------------------------- plans
@@ -1293,7 +2051,8 @@ void fill_params(fsim_sim *h)
 // captured once into a CUDA graph.
 enum LaunchKind {
     L_ZERO, L_HASH, L_SCAN_REDUCE, L_SCAN_PARTIALS, L_SCAN_APPLY, L_SCATTER, L_GATHER_F, L_GATHER_S,
-    L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE
+    L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE,
+    L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M
 };
 
 struct Launch {
@@ -1355,19 +2114,27 @@ void plan_cell(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
 {
     std::vector<Item<ZeroArgs>> zi;
     std::vector<Item<HashArgs>> hi;
+    std::vector<Item<HashMixedArgs>> hmi;
     std::vector<Item<ScanArgs>> si;
     std::vector<Item<ScatterArgs>> ci;
-    std::vector<int> zb, hb, sb, sp, cb;
+    std::vector<int> zb, hb, hmb, sb, sp, cb;
     for (fsim_sim *h : m) {
         for (int sp_ = 0; sp_ < 2; ++sp_) {
             const int n = sp_ ? h->ns : h->nf;
             Item<ZeroArgs> z{h->P, ZeroArgs{sp_ ? h->s_cnt : h->f_cnt, n ? h->ncell : 0}};
             zi.push_back(z);
             zb.push_back(blocks_for(z.A.n, kBlock));
-            Item<HashArgs> hh{h->P, sp_ ? HashArgs{h->s_pos[ps], h->ns, h->s_key, h->s_slot, h->s_cnt, h->d_flags}
-                                        : HashArgs{h->f_posr[pf], h->nf, h->f_key, h->f_slot, h->f_cnt, h->d_flags}};
-            hi.push_back(hh);
-            hb.push_back(blocks_for(n, kBlock));
+            if (!sp_ && h->mixed) {
+                hmi.push_back({h->P, HashMixedArgs{h->f_posr[pf], h->f_cell, h->nf, h->f_key, h->f_slot, h->f_cnt,
+                                                   h->d_flags}});
+                hmb.push_back(blocks_for(n, kBlock));
+            } else {
+                Item<HashArgs> hh{h->P, sp_ ? HashArgs{h->s_pos[ps], h->ns, h->s_key, h->s_slot, h->s_cnt, h->d_flags}
+                                            : HashArgs{h->f_posr[pf], h->nf, h->f_key, h->f_slot, h->f_cnt,
+                                                       h->d_flags}};
+                hi.push_back(hh);
+                hb.push_back(blocks_for(n, kBlock));
+            }
             Item<ScanArgs> sc{h->P, sp_ ? ScanArgs{h->s_cnt, h->s_start, h->ncell, h->scan_partials + kMaxScanTiles}
                                         : ScanArgs{h->f_cnt, h->f_start, h->ncell, h->scan_partials}};
             si.push_back(sc);
@@ -1381,6 +2148,7 @@ void plan_cell(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
     }
     add_launch(pl, ab, L_ZERO, zi, zb);
     add_launch(pl, ab, L_HASH, hi, hb);
+    add_launch(pl, ab, L_HASH_M, hmi, hmb);
     add_launch(pl, ab, L_SCAN_REDUCE, si, sb);
     add_launch(pl, ab, L_SCAN_PARTIALS, si, sp);
     add_launch(pl, ab, L_SCAN_APPLY, si, sb);
@@ -1401,6 +2169,14 @@ void plan_cell(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
     }
     add_launch(pl, ab, L_GATHER_F, gf, gfb);
     add_launch(pl, ab, L_GATHER_S, gs, gsb);
+    std::vector<Item<CellRefArgs>> cr;
+    std::vector<int> crb;
+    for (fsim_sim *h : m) {
+        if (!h->mixed) continue;
+        cr.push_back({h->P, CellRefArgs{h->f_posr[1 - pf], h->f_velp[1 - pf], h->f_start, h->f_cm, h->ncell}});
+        crb.push_back(h->nf ? blocks_for(h->ncell, kBlock) : 0);
+    }
+    add_launch(pl, ab, L_CELLREF, cr, crb);
 }
 
 void plan_couple(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
@@ -1412,7 +2188,7 @@ void plan_couple(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, i
                                        h->s_np, h->ns}});
         nb.push_back(h->nf && h->ns ? blocks_for(32ll * h->ns, kBlock) : 0);
     }
-    add_launch(pl, ab, L_COUPLE, it, nb);
+    add_launch(pl, ab, m.empty() || !m[0]->mixed ? L_COUPLE : L_COUPLE_M, it, nb);
 }
 
 void plan_virt(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf)
@@ -1424,7 +2200,7 @@ void plan_virt(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
                                      h->f_start, h->v_posr, h->v_velp, h->nv}});
         nb.push_back(blocks_for(h->nv, kBlock));
     }
-    add_launch(pl, ab, L_VIRT, it, nb);
+    add_launch(pl, ab, m.empty() || !m[0]->mixed ? L_VIRT : L_VIRT_M, it, nb);
 }
 
 // fluid sweep + update (parity pf -> 1-pf)
@@ -1455,6 +2231,7 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         A.dudt_out = h->f_dudt;
         A.n = h->nf;
         A.keep = h->keep ? 1 : 0;
+        A.cm = h->f_cm;
         it.push_back({h->P, A});
         nb.push_back(blocks_for(h->nf, kSweepWarps * 32));
         if (h->nf) {
@@ -1465,7 +2242,8 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
     const int n_active = (int)std::count_if(m.begin(), m.end(), [](fsim_sim *h) { return h->nf > 0; });
     const int visc_mode = nvisc == 0 ? 0 : nvisc == n_active ? 1 : 2;
     const size_t before = pl.launches.size();
-    add_launch(pl, ab, L_SWEEP, it, nb, (any_check ? 3 : 0) + visc_mode);
+    const bool mixed = !m.empty() && m[0]->mixed;
+    add_launch(pl, ab, L_SWEEP, it, nb, mixed ? 6 + visc_mode : (any_check ? 3 : 0) + visc_mode);
     if (pl.launches.size() > before) pl.sweep_index = (int)before;
 }
 
@@ -1509,8 +2287,9 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
             wb.push_back(active ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
             tb.push_back(active ? blocks_for(h->ns, kBlock) : 0);
         }
-        add_launch(pl, ab, L_DEFORM, it, wb);
-        add_launch(pl, ab, L_FORCE, it, wb);
+        const bool mixed = !m.empty() && m[0]->mixed;
+        add_launch(pl, ab, mixed ? L_DEFORM_M : L_DEFORM, it, wb);
+        add_launch(pl, ab, mixed ? L_FORCE_M : L_FORCE, it, wb);
         add_launch(pl, ab, L_UPDATE, it, tb);
     }
 }
@@ -1572,11 +2351,15 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, cudaEvent_t sweep0 = n
 {
     using SweepFn = void (*)(const Item<FluidSweepArgs> *, const int *, int);
     using Sweep1Fn = void (*)(const DevParams, const FluidSweepArgs);
-    static const SweepFn sweeps[6] = {kb_fluid_sweep<false, 0>, kb_fluid_sweep<false, 1>, kb_fluid_sweep<false, 2>,
-                                      kb_fluid_sweep<true, 0>,  kb_fluid_sweep<true, 1>,  kb_fluid_sweep<true, 2>};
-    static const Sweep1Fn sweeps1[6] = {kb_fluid_sweep_1<false, 0>, kb_fluid_sweep_1<false, 1>,
+    // variants 0-5: plain (CHECK_Z, VISCID); 6-8: mixed (VISCID)
+    static const SweepFn sweeps[9] = {kb_fluid_sweep<false, 0>, kb_fluid_sweep<false, 1>, kb_fluid_sweep<false, 2>,
+                                      kb_fluid_sweep<true, 0>,  kb_fluid_sweep<true, 1>,  kb_fluid_sweep<true, 2>,
+                                      kb_fluid_sweep_m<0>,      kb_fluid_sweep_m<1>,      kb_fluid_sweep_m<2>};
+    static const Sweep1Fn sweeps1[9] = {kb_fluid_sweep_1<false, 0>, kb_fluid_sweep_1<false, 1>,
                                         kb_fluid_sweep_1<false, 2>, kb_fluid_sweep_1<true, 0>,
-                                        kb_fluid_sweep_1<true, 1>,  kb_fluid_sweep_1<true, 2>};
+                                        kb_fluid_sweep_1<true, 1>,  kb_fluid_sweep_1<true, 2>,
+                                        kb_fluid_sweep_m1<0>,       kb_fluid_sweep_m1<1>,
+                                        kb_fluid_sweep_m1<2>};
     for (size_t k = 0; k < pl.launches.size(); ++k) {
         const Launch &L = pl.launches[k];
         const int *tb = reinterpret_cast<const int *>(pl.arena + L.table_off);
@@ -1606,6 +2389,12 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, cudaEvent_t sweep0 = n
         case L_DEFORM: FSIM_LAUNCH(kb_solid_deform, SolidArgs, kBlock); break;
         case L_FORCE: FSIM_LAUNCH(kb_solid_force, SolidArgs, kBlock); break;
         case L_UPDATE: FSIM_LAUNCH(kb_solid_update, SolidArgs, kBlock); break;
+        case L_HASH_M: FSIM_LAUNCH(kb_hash_mixed, HashMixedArgs, kBlock); break;
+        case L_CELLREF: FSIM_LAUNCH(kb_cell_ref, CellRefArgs, kBlock); break;
+        case L_COUPLE_M: FSIM_LAUNCH(kb_couple_mixed, CoupleArgs, kBlock); break;
+        case L_VIRT_M: FSIM_LAUNCH(kb_virt_mixed, VirtArgs, kBlock); break;
+        case L_DEFORM_M: FSIM_LAUNCH(kb_solid_deform_mixed, SolidArgs, kBlock); break;
+        case L_FORCE_M: FSIM_LAUNCH(kb_solid_force_mixed, SolidArgs, kBlock); break;
         default: fsim_set_error("unknown launch kind"); return FSIM_EINVAL;
         }
         CK_LAUNCH();
@@ -1861,6 +2650,7 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
         (st = dalloc(h, &h->f_tmp, nf)) || (st = dalloc(h, &h->f_cnt, nc)) || (st = dalloc(h, &h->f_start, nc + 1)))
         return st;
     if (h->keep && ((st = dalloc(h, &h->f_drho, nf)) || (st = dalloc(h, &h->f_dudt, nf)))) return st;
+    if (h->mixed && (st = dalloc(h, &h->f_cm, nc))) return st;
     // solid
     for (int b = 0; b < 2; ++b) {
         if ((st = dalloc(h, &h->s_pos[b], ns)) || (st = dalloc(h, &h->s_vel[b], ns)) ||
@@ -1905,6 +2695,9 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
         CK(cudaMemcpyAsync(stg, p->fluid_vel, sizeof(float) * 3 * nf, cudaMemcpyHostToDevice, h->stream));
         k_pack_f4<<<blocks_for(nf, kBlock), kBlock, 0, h->stream>>>(stg, d_rho, nf, 0.0f, h->f_velp[0]);
         k_iota<<<blocks_for(nf, kBlock), kBlock, 0, h->stream>>>(h->f_orig[0], nf);
+        if (h->mixed)
+            k_fluid_to_mixed<<<blocks_for(nf, kBlock), kBlock, 0, h->stream>>>(h->P, h->f_posr[0], h->f_velp[0],
+                                                                               h->f_cell, nf, h->d_flags);
         CK_LAUNCH();
         CK(cudaStreamSynchronize(h->stream));
         cudaFree(d_rho);
@@ -1936,6 +2729,10 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
         if ((st = build_solid_neighbors(h, p->solid_ref_pos))) return st;
     }
     if (nv && (st = sort_virtual(h, p->virt_pos))) return st;
+    if (nv && h->mixed) {
+        k_offsets_in_cells<<<blocks_for(nv, kBlock), kBlock, 0, h->stream>>>(h->P, h->v_posr, h->v_cell, nv);
+        CK_LAUNCH();
+    }
     CK(cudaStreamSynchronize(h->stream));
     return check_flags(h);
 }
@@ -1987,6 +2784,12 @@ extern "C" fsim_status fsim_create(const fsim_config *cfg, const fsim_particles 
     h->nv = p->n_virt;
     h->ncell = h->der.cell_number_total;
     h->keep = cfg->keep_derivatives != 0;
+    h->mixed = h->P.mixed != 0;
+    if (h->mixed && (h->nf > kIndexMask || h->nv > kIndexMask)) {
+        fsim_set_error("the mixed form takes at most %d fluid and %d wall particles", kIndexMask, kIndexMask);
+        delete h;
+        return FSIM_EINVAL;
+    }
     if (h->ns && (h->P.nx >= 2048 || h->P.ny >= 1024 || h->P.nz >= 2048)) {
         fsim_set_error("cell grid %d x %d x %d too large for a solid (limit 2047 x 1023 x 2047)", h->P.nx, h->P.ny,
                        h->P.nz);
@@ -2121,6 +2924,23 @@ extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_
     float *stg = (float *)h->staging;
     const int *forig = h->f_orig[h->f_cur];
     const int *sorig = h->s_orig[h->s_cur];
+    if (h->mixed && (field == FSIM_FLUID_POS || field == FSIM_FLUID_RHO || field == FSIM_FLUID_P ||
+                     field == FSIM_VIRT_POS)) {
+        if (field == FSIM_VIRT_POS)
+            k_unpermute_mixed<<<g, kBlock, 0, h->stream>>>(h->P, h->v_posr, h->v_velp, h->v_cell, h->v_orig, n, MF_POS,
+                                                            stg);
+        else
+            k_unpermute_mixed<<<g, kBlock, 0, h->stream>>>(h->P, h->f_posr[h->f_cur], h->f_velp[h->f_cur], h->f_cell,
+                                                            forig, n,
+                                                            field == FSIM_FLUID_POS   ? MF_POS
+                                                            : field == FSIM_FLUID_RHO ? MF_RHO
+                                                                                      : MF_P,
+                                                            stg);
+        CK_LAUNCH();
+        CK(cudaMemcpyAsync(dst, stg, bytes, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return FSIM_OK;
+    }
     switch (field) {
     case FSIM_FLUID_POS: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->f_posr[h->f_cur], forig, n, 0, 3, stg); break;
     case FSIM_FLUID_RHO: k_unpermute_f4<<<g, kBlock, 0, h->stream>>>(h->f_posr[h->f_cur], forig, n, 3, 1, stg); break;
@@ -2220,6 +3040,10 @@ extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src,
     default: fsim_set_error("field %d is not settable", field); return FSIM_EINVAL;
     }
     orig = field < 10 ? h->f_orig[h->f_cur] : h->s_orig[h->s_cur];
+    if (h->mixed && field == FSIM_FLUID_P) {
+        fsim_set_error("in the mixed form the fluid pressure is the EOS of the density; set FSIM_FLUID_RHO");
+        return FSIM_EINVAL;
+    }
     if (bytes != (size_t)n * width * 4) {
         fsim_set_error("field %d needs %zu bytes, got %zu", field, (size_t)n * width * 4, bytes);
         return FSIM_EINVAL;
@@ -2227,8 +3051,13 @@ extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src,
     if (n == 0) return FSIM_OK;
     DeviceGuard guard(h->device);
     CK(cudaMemcpyAsync(h->staging, src, bytes, cudaMemcpyHostToDevice, h->stream));
-    k_permute_in_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(dst, orig, n, comp, width,
-                                                                      (const float *)h->staging);
+    if (h->mixed && (field == FSIM_FLUID_POS || field == FSIM_FLUID_RHO))
+        k_permute_in_mixed<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(
+            h->P, h->f_posr[h->f_cur], h->f_velp[h->f_cur], h->f_cell, orig, n,
+            field == FSIM_FLUID_POS ? MF_POS : MF_RHO, (const float *)h->staging);
+    else
+        k_permute_in_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(dst, orig, n, comp, width,
+                                                                          (const float *)h->staging);
     CK_LAUNCH();
     if (h->batch) CK(cudaStreamSynchronize(h->stream)); // the batch stream must see it
     // positions changed: derived per-step products are stale until the next phases
@@ -2245,6 +3074,10 @@ extern "C" fsim_status fsim_neighbor_counts(fsim_handle h, int *out, size_t byte
     }
     if (!h->f_sorted) {
         fsim_set_error("run FSIM_PHASE_CELL first");
+        return FSIM_EINVAL;
+    }
+    if (h->mixed) {
+        fsim_set_error("neighbour counts are a check of the plain form's FP32 pair set");
         return FSIM_EINVAL;
     }
     if (!h->nf) return FSIM_OK;
@@ -2395,6 +3228,42 @@ extern "C" fsim_status fsim_launches_per_step(fsim_handle h, int *n)
     return FSIM_OK;
 }
 
+extern "C" fsim_status fsim_conservation(fsim_handle h, double *out, int n_out)
+{
+    if (!h || !out || n_out < 1) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
+    DeviceGuard guard(h->device);
+    const int bf = blocks_for(h->nf, kBlock), bs = blocks_for(h->ns, kBlock);
+    const size_t words = (size_t)(bf + bs) * FSIM_CONSERVATION_N;
+    double *d_part = nullptr;
+    CK(cudaMalloc((void **)&d_part, sizeof(double) * (words ? words : 1)));
+    const double vol = (double)h->der.particle_volume;
+    cudaError_t e = cudaSuccess;
+    if (bf)
+        k_conservation_fluid<<<bf, kBlock, 0, h->stream>>>(h->P, h->f_posr[h->f_cur], h->f_velp[h->f_cur], h->f_cell,
+                                                            h->nf, vol, d_part);
+    if (bs)
+        k_conservation_solid<<<bs, kBlock, 0, h->stream>>>(h->P, h->s_pos[h->s_cur], h->s_vel[h->s_cur], h->s_F, h->ns,
+                                                            (double)h->cfg.solid_density, vol,
+                                                            d_part + (size_t)bf * FSIM_CONSERVATION_N);
+    e = cudaGetLastError();
+    std::vector<double> part(words);
+    if (e == cudaSuccess && words)
+        e = cudaMemcpyAsync(part.data(), d_part, sizeof(double) * words, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d_part);
+    if (e != cudaSuccess) {
+        fsim_set_error("conservation sums failed: %s", cudaGetErrorString(e));
+        return FSIM_ECUDA;
+    }
+    double tot[FSIM_CONSERVATION_N] = {};
+    for (int b = 0; b < bf + bs; ++b)
+        for (int k = 0; k < FSIM_CONSERVATION_N; ++k) tot[k] += part[(size_t)b * FSIM_CONSERVATION_N + k];
+    for (int k = 0; k < n_out && k < FSIM_CONSERVATION_N; ++k) out[k] = tot[k];
+    for (int k = FSIM_CONSERVATION_N; k < n_out; ++k) out[k] = 0.0;
+    return FSIM_OK;
+}
+
 extern "C" fsim_status fsim_counts(fsim_handle h, int *nf, int *ns, int *nv)
 {
     if (!h) return FSIM_EINVAL;
@@ -2521,6 +3390,10 @@ extern "C" fsim_status fsim_batch_create(fsim_handle *members, int n, fsim_batch
             fsim_set_error("batch members must be distinct standalone handles on one device");
             return FSIM_EINVAL;
         }
+        if (members[k]->mixed != members[0]->mixed) {
+            fsim_set_error("batch members must share the precision form");
+            return FSIM_EINVAL;
+        }
         for (int j = 0; j < k; ++j)
             if (members[j] == members[k]) {
                 fsim_set_error("a handle appears twice in the batch");
@@ -2633,6 +3506,7 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
     }
     b += nv * (3 * sizeof(float4) + 2 * sizeof(int));
     b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 3; // counts, starts
+    if (cfg->precision == FSIM_PRECISION_MIXED) b += nc * sizeof(float2); // per-cell references
     b += 2 * kMaxScanTiles * sizeof(int) + sizeof(unsigned);
     size_t words = 3 * nf;
     if (9 * ns > words) words = 9 * ns;

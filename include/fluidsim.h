@@ -53,7 +53,16 @@ const char *fsim_status_string(fsim_status s);
 const char *fsim_last_error(void);
 
 /* ------------------------------------------------------------------ config */
-/* Precision forms (an extension; the reference is FP32 only). */
+/* Precision forms (an extension; the reference is FP32 only).
+ * FP32: the reference's arithmetic and storage (absolute FP32 positions,
+ *   density and pressure), cell ids and pair sets bit-exact with it.
+ * MIXED: FP32 arithmetic with fluid positions stored as an integer cell plus
+ *   an FP32 offset inside it, density stored as delta = rho/rho0 - 1 with the
+ *   pressure its Tait EOS, neighbour-gathered density/pressure packed as FP16
+ *   deviations from per-cell FP32 references, a Kahan-compensated density
+ *   rate, and the solid's kernel-correction inverse L^-1 in FP64.  Fields are
+ *   read and written in the same units as the FP32 form; FSIM_FLUID_P is
+ *   read-only (it follows from the density). */
 enum { FSIM_PRECISION_FP32 = 0, FSIM_PRECISION_MIXED = 1 };
 
 /* Every key the reference reads from input.ini, with the same meaning.
@@ -238,6 +247,22 @@ fsim_status fsim_time_steps(fsim_handle h, int nsteps, float *ms);
 fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_ms, float *sweep_ms);
 /* Kernel launches one fsim_step(h, 1) issues (for launch accounting). */
 fsim_status fsim_launches_per_step(fsim_handle h, int *n);
+
+/* Conservation totals of the current state, accumulated in FP64 on the device
+ * (per-particle terms in FP64, fixed-order block sums; deterministic).  No
+ * counterpart in the reference.  Particle mass m = density * particle_volume
+ * (rho0 for fluid, solid_density for solid); g = gravity vector.
+ *   out[0] fluid mass            out[1] solid mass
+ *   out[2..4] momentum sum m u (fluid + solid)
+ *   out[5] kinetic energy sum m |u|^2 / 2 (fluid + solid)
+ *   out[6] potential energy sum -m g.x (fluid + solid)
+ *   out[7] fluid elastic energy: sum m * integral_rho0^rho p/rho'^2 drho' of
+ *          the Tait EOS (pressure floor ignored)
+ *   out[8] fluid density excess sum (rho - rho0) * particle_volume
+ *   out[9] solid strain energy sum V (mu E:E + lambda/2 tr(E)^2), E the Green
+ *          strain of the last solid phase's F (0 before the first one) */
+#define FSIM_CONSERVATION_N 10
+fsim_status fsim_conservation(fsim_handle h, double *out, int n_out);
 
 /* -------------------------------------------------------------- batching */
 /* A batch advances several independent instances (handles created with
