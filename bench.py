@@ -236,6 +236,7 @@ def run_gb300(args, dist):
     achieved = alg_bytes / t_launch / 1e9
     step_bytes = (ALG_BYTES_FLUID * pa.n_fluid + pa.n_solid * (ALG_BYTES_SOLID * cfg.solid_sub_step +
                                                                ALG_BYTES_SOLID_STEP) + ALG_BYTES_VIRT * pa.n_virt)
+    fp32 = sweep_flop_roofline(api, sim, dev, t_launch)
     traffic = None
     prof = os.path.join(ROOT, "profiles", "fluid_sweep_traffic.json")
     if os.path.exists(prof):
@@ -298,6 +299,7 @@ def run_gb300(args, dist):
                          "alg_bytes_per_launch": alg_bytes, "launch_ms": t_launch * 1e3,
                          "step_alg_bytes": step_bytes,
                          "step_frac": step_bytes / (ms * 1e-3 / args.steps) / 1e9 / hbm_peak},
+            "roofline_fp32": fp32,
             "cpu_baseline": cpu,
             "clocks": clk,
             "forms": forms,
@@ -306,6 +308,37 @@ def run_gb300(args, dist):
         }
         print(json.dumps(line), flush=True)
     return 0
+
+
+def sweep_flop_roofline(api, sim, dev, t_launch):
+    """The sweep against the FP32 roofline (it is a gather bound by FP32/ALU
+    issue, not by HBM): algorithmic FLOPs of one launch = 10 per candidate
+    distance test over the reference's 27-cell candidates + 80 per in-range
+    pair (FMA = 2, exp/rsqrt/div = 1), counted on the current state; the peak
+    is the device's FP32 FMA throughput measured here by fsim_measure_fp32_peak."""
+    import numpy as np
+
+    d = sim.derived()
+    nx, ny, nz = d.cell_number[0], d.cell_number[1], d.cell_number[2]
+    occ = np.zeros((nx, ny, nz), np.int64)
+    for sp in (0, 1, 2):
+        start, _ = sim.cells(sp)
+        occ += np.diff(start.astype(np.int64)).reshape(nx, ny, nz)
+    pad = np.pad(occ, 1)
+    box = sum(pad[1 + a:1 + a + nx, 1 + b:1 + b + ny, 1 + c:1 + c + nz]
+              for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1))
+    fstart, _ = sim.cells(0)
+    nfc = np.diff(fstart.astype(np.int64)).reshape(nx, ny, nz)
+    cand = float((nfc * box).sum())
+    pairs = float(sim.neighbor_counts().astype(np.int64).sum())
+    flop = 10.0 * cand + 80.0 * pairs
+    peak = api.measure_fp32_peak(dev)
+    achieved = flop / t_launch / 1e12
+    nf = max(1, int(nfc.sum()))
+    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": "measured (fsim_measure_fp32_peak, FMA chains at full residency)",
+            "flop_per_launch": flop, "candidates_per_particle": cand / nf, "pairs_per_particle": pairs / nf,
+            "flop_model": "10 FLOP per 27-cell candidate test + 80 FLOP per in-range pair"}
 
 
 def run_mixed(dev, steps):

@@ -143,6 +143,7 @@ def load():
         "fsim_time_sweep": (C.c_int, [P, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "fsim_launches_per_step": (C.c_int, [P, C.POINTER(C.c_int)]),
         "fsim_conservation": (C.c_int, [P, C.POINTER(C.c_double), C.c_int]),
+        "fsim_measure_fp32_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
         "fsim_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
         "fsim_host_free": (C.c_int, [P]),
         "fsim_counts": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -173,6 +174,7 @@ EXPORTED = [
     "fsim_launches_per_step", "fsim_host_alloc", "fsim_host_free", "fsim_counts", "fsim_get_derived",
     "fsim_cell_sort_noalloc", "fsim_batch_create", "fsim_batch_step", "fsim_batch_sync", "fsim_batch_time_steps",
     "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes", "fsim_conservation",
+    "fsim_measure_fp32_peak",
 ]
 
 
@@ -209,6 +211,13 @@ def config_from_ini(path):
 def estimate_bytes(cfg, n_fluid, n_solid, n_virt):
     out = C.c_size_t()
     check(load().fsim_estimate_bytes(C.byref(cfg), n_fluid, n_solid, n_virt, C.byref(out)))
+    return out.value
+
+
+def measure_fp32_peak(device=0):
+    """FP32 FMA throughput of the device in TFLOP/s (fsim_measure_fp32_peak)."""
+    out = C.c_double()
+    check(load().fsim_measure_fp32_peak(device, C.byref(out)))
     return out.value
 
 

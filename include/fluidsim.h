@@ -264,6 +264,11 @@ fsim_status fsim_launches_per_step(fsim_handle h, int *n);
 #define FSIM_CONSERVATION_N 10
 fsim_status fsim_conservation(fsim_handle h, double *out, int n_out);
 
+/* Measurement utility (no counterpart in the reference): FP32 FMA throughput
+ * of `device` in TFLOP/s (an FMA counts 2), from a kernel of independent FMA
+ * chains at full residency timed with CUDA events (best of 3 launches). */
+fsim_status fsim_measure_fp32_peak(int device, double *tflops);
+
 /* -------------------------------------------------------------- batching */
 /* A batch advances several independent instances (handles created with
  * fsim_create on the same device, of any sizes and parameters) in lockstep:
