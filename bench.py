@@ -226,6 +226,10 @@ def run_gb300(args, dist):
     ms = dist.max(ms)
     value = nupd * args.steps * dist.ws / (ms * 1e-3)
 
+    chosen, tune_ms = sim.sweep_tuning()
+    tuning = {"chosen_shape": chosen, "shape": api.SWEEP_SHAPES[chosen] if chosen >= 0 else None,
+              "shapes": "(warps per block, list capacity)", "sweep_ms_per_shape": tune_ms}
+
     # ---- per-kernel timing of the dominant kernel (fluid sweep), CUDA events on the handle's stream
     tot_ms, sweep_ms = sim.time_sweep(args.steps)
     sweep_ms = dist.max(sweep_ms)
@@ -300,6 +304,7 @@ def run_gb300(args, dist):
                          "step_alg_bytes": step_bytes,
                          "step_frac": step_bytes / (ms * 1e-3 / args.steps) / 1e9 / hbm_peak},
             "roofline_fp32": fp32,
+            "autotuner": tuning,
             "cpu_baseline": cpu,
             "clocks": clk,
             "forms": forms,
@@ -383,6 +388,7 @@ def run_ensemble(dev, steps):
         b.sync()
         batched_ms = b.time_steps(steps)
         launches = b.launches_per_step()
+        chosen, tune_ms = b.sweep_tuning()
     for sm in sims:
         sm.close()
     return {
@@ -394,40 +400,64 @@ def run_ensemble(dev, steps):
         "ratio": one_by_one_ms / batched_ms,
         "unit": "particle-updates/s",
         "batched_launches_per_step": launches,
+        "autotuner": {"chosen_shape": chosen, "sweep_ms_per_shape": tune_ms},
     }
 
 
 def run_served(dev):
-    """BASELINE config 4, shortened: a seeded Poisson stream (20 requests/s) of
-    config-3-style scenarios served with continuous batching under a 150 GB
-    budget, and the same stream served one request at a time."""
+    """BASELINE config 4, shortened in request count only: a seeded Poisson
+    stream (20 requests/s) of config-3-style scenarios with the config's
+    distributions (fluid 10k-1M log-uniform, solid 1k-27k, 200-2000 steps),
+    served with continuous batching under a 150 GB budget, and the same stream
+    served one request at a time.  Request data is generated before the clock
+    starts.  24 requests keep the run to tens of seconds; at 20 requests/s the
+    stream saturates the GPU, as the 2000-request stream does."""
     from fluidsim_gb300 import serve
 
-    spec = dict(n=40, rate=20.0, seed=7, fluid_range=(10_000, 300_000), solid_range=(1_000, 27_000),
-                steps_range=(100, 400))
-    batched = serve.Server(budget_bytes=150 * 2 ** 30, backend=serve.GpuBackend(dev), quantum=10).run(
-        serve.poisson_stream(**spec))
-    plain = serve.serve_one_by_one(serve.poisson_stream(**spec), device=dev)
+    spec = dict(n=24, rate=20.0, seed=7, fluid_range=(10_000, 1_000_000), solid_range=(1_000, 27_000),
+                steps_range=(200, 2000))
+    reqs = serve.pregenerate(serve.poisson_stream(**spec))
+    batched = serve.Server(budget_bytes=150 * 10 ** 9, backend=serve.GpuBackend(dev), quantum=20,
+                           max_particles=6_000_000).run(reqs)
+    again = serve.poisson_stream(**spec)  # same stream, same data
+    for r, q in zip(reqs, again):
+        q.data, q.particles = r.data, r.particles
+    plain = serve.serve_one_by_one(again, device=dev)
     return {"workload": "Poisson stream, %d requests at %g/s (seed 7), fluid %d-%d log-uniform, solid %d-%d, "
-                        "steps %d-%d uniform, dx=0.01; shortened from 2000 requests of 10k-1M fluid and "
-                        "200-2000 steps" % (spec["n"], spec["rate"], spec["fluid_range"][0], spec["fluid_range"][1],
-                                            spec["solid_range"][0], spec["solid_range"][1], spec["steps_range"][0],
-                                            spec["steps_range"][1]),
+                        "steps %d-%d uniform, dx=0.01, 150 GB HBM budget and a 6M-particle work budget; the config's "
+                        "2000 requests shortened to %d"
+                        % (spec["n"], spec["rate"], spec["fluid_range"][0], spec["fluid_range"][1],
+                           spec["solid_range"][0], spec["solid_range"][1], spec["steps_range"][0],
+                           spec["steps_range"][1], spec["n"]),
             "served": batched, "one_by_one": plain,
             "throughput_ratio": batched["throughput"] / plain["throughput"]}
 
 
 def run_profile(args):
     """Fewest launches for an ncu capture: creation, then N graph-free steps
-    (the same kernels as the timed region)."""
-    from fluidsim_gb300 import api
+    (the same kernels as the timed region).  --profile-form picks the plain
+    4M case, the mixed form of the jittered 4M case, or the batched ensemble."""
+    from fluidsim_gb300 import api, cases
 
-    cfg, pa = workload(args)
+    if args.profile_form == "ensemble":
+        members = [cases.make(s) for s in cases.ensemble(64, 2024)]
+        sims = [api.Simulation(cfg, pa, device=0) for cfg, pa in members]
+        with api.Batch(sims) as b:
+            ms = b.time_steps(args.profile_steps)
+        for sm in sims:
+            sm.close()
+        print(json.dumps({"profile_steps": args.profile_steps, "form": "ensemble",
+                          "ms_per_step": ms / args.profile_steps}))
+        return 0
+    if args.profile_form == "mixed":
+        cfg, pa = cases.make(cases.fsi_4m_jitter(precision=api.PRECISION_MIXED))
+    else:
+        cfg, pa = workload(args)
     sim = api.Simulation(cfg, pa, device=0)
     tot, sweep = sim.time_sweep(args.profile_steps)
     sim.close()
-    print(json.dumps({"profile_steps": args.profile_steps, "ms_per_step": tot / args.profile_steps,
-                      "sweep_ms": sweep / args.profile_steps}))
+    print(json.dumps({"profile_steps": args.profile_steps, "form": args.profile_form,
+                      "ms_per_step": tot / args.profile_steps, "sweep_ms": sweep / args.profile_steps}))
     return 0
 
 
@@ -440,6 +470,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--profile-form", choices=("plain", "mixed", "ensemble"), default="plain")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling run for ncu: create the workload, run this many steps, print nothing else")
     args = ap.parse_args()

@@ -144,6 +144,8 @@ def load():
         "fsim_launches_per_step": (C.c_int, [P, C.POINTER(C.c_int)]),
         "fsim_conservation": (C.c_int, [P, C.POINTER(C.c_double), C.c_int]),
         "fsim_measure_fp32_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+        "fsim_sweep_tuning": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
+        "fsim_batch_sweep_tuning": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
         "fsim_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
         "fsim_host_free": (C.c_int, [P]),
         "fsim_counts": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -174,8 +176,9 @@ EXPORTED = [
     "fsim_launches_per_step", "fsim_host_alloc", "fsim_host_free", "fsim_counts", "fsim_get_derived",
     "fsim_cell_sort_noalloc", "fsim_batch_create", "fsim_batch_step", "fsim_batch_sync", "fsim_batch_time_steps",
     "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes", "fsim_conservation",
-    "fsim_measure_fp32_peak",
+    "fsim_measure_fp32_peak", "fsim_sweep_tuning", "fsim_batch_sweep_tuning",
 ]
+SWEEP_SHAPES = ((4, 48), (4, 32), (8, 32))  # (warps per block, list capacity) per shape index
 
 
 class FsimError(RuntimeError):
@@ -212,6 +215,13 @@ def estimate_bytes(cfg, n_fluid, n_solid, n_virt):
     out = C.c_size_t()
     check(load().fsim_estimate_bytes(C.byref(cfg), n_fluid, n_solid, n_virt, C.byref(out)))
     return out.value
+
+
+def _tuning(fn, handle):
+    chosen = C.c_int()
+    ms = (C.c_float * len(SWEEP_SHAPES))()
+    check(fn(handle, C.byref(chosen), ms, len(SWEEP_SHAPES)))
+    return chosen.value, list(ms)
 
 
 def measure_fp32_peak(device=0):
@@ -416,6 +426,10 @@ class Simulation:
         check(self.lib.fsim_launches_per_step(self.h, C.byref(n)))
         return n.value
 
+    def sweep_tuning(self):
+        """(chosen shape or -1, [ms per shape]) of the sweep autotuner."""
+        return _tuning(self.lib.fsim_sweep_tuning, self.h)
+
     def conservation(self):
         """FP64 conservation totals (fsim_conservation) as a dict."""
         out = (C.c_double * CONSERVATION_N)()
@@ -472,6 +486,10 @@ class Batch:
         n = C.c_int()
         check(self.lib.fsim_batch_launches_per_step(self.b, C.byref(n)))
         return n.value
+
+    def sweep_tuning(self):
+        """(chosen shape or -1, [ms per shape]) of the batch's sweep autotuner."""
+        return _tuning(self.lib.fsim_batch_sweep_tuning, self.b)
 
     def close(self):
         if self.b:

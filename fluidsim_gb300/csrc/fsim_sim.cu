@@ -527,9 +527,22 @@ __device__ __forceinline__ void fluid_update_store(const DevParams &P, const Flu
 // distance, so the pair set is exactly the reference's; CHECK_Z re-checks the
 // z cell when the grid spacing is too close to the impact distance for that
 // argument to survive FP32 rounding.
-constexpr int kSweepWarps = 4;
-constexpr int kListCap = 48;  // per-lane neighbour list entries in shared memory
-constexpr int kChunk = 16;    // candidates between capacity checks
+//
+// Launch shape: warps per block, per-lane list capacity (shared memory) and
+// candidates between capacity checks.  None of them changes what a lane sums or
+// in which order (a warp owns the same 32 particles and walks the same stream
+// whatever the block size; flushes evaluate a lane's hits in stream order), so
+// results are bit-identical across shapes and the autotuner may pick any.
+// Smaller lists leave more of the SM's 256 KB L1 as cache for the gathers.
+template <int W, int CAP, int CHUNK>
+struct SweepShape {
+    static constexpr int warps = W, cap = CAP, chunk = CHUNK;
+};
+using Shape0 = SweepShape<4, 48, 16>; // 24 KB of lists per 128-thread block
+using Shape1 = SweepShape<4, 32, 8>;  // 16 KB per 128-thread block
+using Shape2 = SweepShape<8, 32, 8>;  // 32 KB per 256-thread block
+constexpr int kSweepShapes = 3;
+constexpr int kShapeWarps[kSweepShapes] = {Shape0::warps, Shape1::warps, Shape2::warps};
 
 enum Species { kFluid = 0, kVirt = 1, kSolid = 2 };
 
@@ -570,7 +583,7 @@ __device__ __forceinline__ void flush_list(const DevParams &P, const FluidSweepA
     cnt = 0;
 }
 
-template <int SP, bool CHECK_Z, int VISCID, bool KAHAN = false>
+template <int SP, bool CHECK_Z, int VISCID, class SH, bool KAHAN = false>
 __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
                                                int &cnt, bool in, int cz, int cx, int cy, int z0, int z1, float4 pr,
                                                float4 vp, PairAcc &acc)
@@ -587,9 +600,9 @@ __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSw
             int j = start[base + z0];
             const int je = start[base + z1];
             while (j < je) {
-                if (__reduce_max_sync(kFull, cnt) > kListCap - kChunk)
+                if (__reduce_max_sync(kFull, cnt) > SH::cap - SH::chunk)
                     flush_list<SP, VISCID, KAHAN>(P, A, lst, lane, cnt, pr, vp, acc);
-                const int jend = min(j + kChunk, je);
+                const int jend = min(j + SH::chunk, je);
 #pragma unroll 4
                 for (; j < jend; ++j) {
                     const float4 q = pos[j]; // same address in every lane: a broadcast
@@ -607,12 +620,12 @@ __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSw
     flush_list<SP, VISCID, KAHAN>(P, A, lst, lane, cnt, pr, vp, acc);
 }
 
-template <bool CHECK_Z, int VISCID>
+template <bool CHECK_Z, int VISCID, class SH>
 __device__ __forceinline__ void fluid_sweep_body(const DevParams &P, const FluidSweepArgs &A, int blk)
 {
-    __shared__ int lists[kSweepWarps][kListCap][32];
+    __shared__ int lists[SH::warps][SH::cap][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = (blk * kSweepWarps + warp) * 32 + lane;
+    const int i = (blk * SH::warps + warp) * 32 + lane;
     const bool valid = i < A.n;
     int(*lst)[32] = lists[warp];
     const float4 pr = valid ? A.posr[i] : make_float4(0.0f, 0.0f, 0.0f, 1.0f);
@@ -632,28 +645,28 @@ __device__ __forceinline__ void fluid_sweep_body(const DevParams &P, const Fluid
         const int zhi = __reduce_max_sync(kFull, in ? cz : INT_MIN);
         const int z0 = max(zlo - 1, 0), z1 = min(zhi + 1, P.nz - 1) + 1;
         const int cx = grow / P.ny, cy = grow - cx * P.ny;
-        gather_species<kFluid, CHECK_Z, VISCID>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
-        gather_species<kVirt, CHECK_Z, VISCID>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
-        gather_species<kSolid, CHECK_Z, VISCID>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
+        gather_species<kFluid, CHECK_Z, VISCID, SH>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
+        gather_species<kVirt, CHECK_Z, VISCID, SH>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
+        gather_species<kSolid, CHECK_Z, VISCID, SH>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
     }
     if (valid) fluid_update_store(P, A, i, pr, vp, acc);
 }
 
-template <bool CHECK_Z, int VISCID>
-__global__ void __launch_bounds__(kSweepWarps * 32) kb_fluid_sweep(const Item<FluidSweepArgs> *__restrict__ items,
-                                                                   const int *__restrict__ bstart, int ninst)
+template <bool CHECK_Z, int VISCID, class SH>
+__global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep(const Item<FluidSweepArgs> *__restrict__ items,
+                                                                 const int *__restrict__ bstart, int ninst)
 {
     const int inst = locate_instance(bstart, ninst, blockIdx.x);
     const DevParams P = items[inst].P;
-    fluid_sweep_body<CHECK_Z, VISCID>(P, items[inst].A, (int)blockIdx.x - bstart[inst]);
+    fluid_sweep_body<CHECK_Z, VISCID, SH>(P, items[inst].A, (int)blockIdx.x - bstart[inst]);
 }
 
 // The one-instance sweep takes {params, args} by value: kernel parameters live
 // in the constant bank, where its hot loops read them without extra loads.
-template <bool CHECK_Z, int VISCID>
-__global__ void __launch_bounds__(kSweepWarps * 32) kb_fluid_sweep_1(const DevParams P, const FluidSweepArgs A)
+template <bool CHECK_Z, int VISCID, class SH>
+__global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep_1(const DevParams P, const FluidSweepArgs A)
 {
-    fluid_sweep_body<CHECK_Z, VISCID>(P, A, (int)blockIdx.x);
+    fluid_sweep_body<CHECK_Z, VISCID, SH>(P, A, (int)blockIdx.x);
 }
 
 // ------------------------------------------------------- virtual particles
@@ -760,10 +773,21 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
+// kSolidGroup lanes share one solid particle: they split its candidates and
+// combine their sums with shuffles (a fixed pairing: deterministic).
+constexpr int kSolidGroup = 4;
+
+__device__ __forceinline__ float group_sum(float v)
+{
+#pragma unroll
+    for (int o = 1; o < kSolidGroup; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
 // ------------------------------------------------------- fluid-solid coupling
 // solidCoupleUpdate (src/solid.cu:262-344): solid normal from the solid
 // neighbours' kernel gradients, solid pressure as the Shepard average of the
-// fluid pressure.  One warp per solid particle.
+// fluid pressure.  kSolidGroup lanes per solid particle.
 struct CoupleArgs {
     const float4 *s_pos;
     const int *s_cell, *start_s;
@@ -774,43 +798,45 @@ struct CoupleArgs {
 };
 __device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs &A, int blk)
 {
-    const int i = (blk * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= A.n) return; // whole warp
-    const float4 xi = A.s_pos[i];
-    Rows rows;
-    neighbor_rows(P, A.s_cell[i], rows);
+    const int t = blk * blockDim.x + threadIdx.x;
+    const int i = t / kSolidGroup, g = t % kSolidGroup;
+    const bool valid = i < A.n;
     float nx = 0.0f, ny = 0.0f, nz = 0.0f, psum = 0.0f, wsum = 0.0f;
-    for (int r = 0; r < rows.count; ++r) {
-        const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-        for (int j = A.start_f[c0] + lane, je = A.start_f[c1]; j < je; j += 32) {
-            const float4 q = A.fposr[j];
-            const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
-            const float r2 = dist2(dx, dy, dz);
-            if (r2 < P.R2) {
-                const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
-                wsum += w;
-                psum += A.fvelp[j].w * w;
+    if (valid) {
+        const float4 xi = A.s_pos[i];
+        Rows rows;
+        neighbor_rows(P, A.s_cell[i], rows);
+        for (int r = 0; r < rows.count; ++r) {
+            const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+            for (int j = A.start_f[c0] + g, je = A.start_f[c1]; j < je; j += kSolidGroup) {
+                const float4 q = A.fposr[j];
+                const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 < P.R2) {
+                    const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
+                    wsum += w;
+                    psum += A.fvelp[j].w * w;
+                }
             }
-        }
-        for (int j = A.start_s[c0] + lane, je = A.start_s[c1]; j < je; j += 32) {
-            const float4 q = A.s_pos[j];
-            const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
-            const float r2 = dist2(dx, dy, dz);
-            if (r2 < P.R2) {
-                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
-                nx -= dx * w;
-                ny -= dy * w;
-                nz -= dz * w;
+            for (int j = A.start_s[c0] + g, je = A.start_s[c1]; j < je; j += kSolidGroup) {
+                const float4 q = A.s_pos[j];
+                const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 < P.R2) {
+                    const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+                    nx -= dx * w;
+                    ny -= dy * w;
+                    nz -= dz * w;
+                }
             }
         }
     }
-    nx = warp_sum(nx);
-    ny = warp_sum(ny);
-    nz = warp_sum(nz);
-    psum = warp_sum(psum);
-    wsum = warp_sum(wsum);
-    if (lane) return;
+    nx = group_sum(nx);
+    ny = group_sum(ny);
+    nz = group_sum(nz);
+    psum = group_sum(psum);
+    wsum = group_sum(wsum);
+    if (!valid || g) return;
     const float l2 = nx * nx + ny * ny + nz * nz;
     if (l2 < FSIM_EPS_FOR_SUM) {
         nx = ny = nz = 0.0f;
@@ -988,7 +1014,7 @@ __device__ __forceinline__ void flush_list_m(const DevParams &P, const FluidSwee
 // every candidate's cell (relative to the lane's own) is known; it travels
 // with the list entry as a 6-bit code.  Each lane only takes candidates from
 // its own 27 cells.
-template <int SP, int VISCID>
+template <int SP, int VISCID, class SH>
 __device__ __forceinline__ void gather_species_m(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
                                                  int &cnt, bool in, int cz, int cx, int cy, int z0, int z1,
                                                  float4 off, const OwnMixed &o, float4 vp, PairAcc &acc)
@@ -1013,9 +1039,9 @@ __device__ __forceinline__ void gather_species_m(const DevParams &P, const Fluid
                 const float psz = fmaf(-(float)dzc, P.cdx[2], off.z);
                 const unsigned code = (code_xy | ((unsigned)(dzc + 1) << 4)) << kCodeShift;
                 while (j < je) {
-                    if (__reduce_max_sync(kFull, cnt) > kListCap - kChunk)
+                    if (__reduce_max_sync(kFull, cnt) > SH::cap - SH::chunk)
                         flush_list_m<SP, VISCID>(P, A, lst, lane, cnt, o, vp, acc);
-                    const int jend = min(j + kChunk, je);
+                    const int jend = min(j + SH::chunk, je);
 #pragma unroll 4
                     for (; j < jend; ++j) {
                         const float4 q = pos[j]; // a broadcast
@@ -1063,12 +1089,12 @@ __device__ __forceinline__ void fluid_update_store_m(const DevParams &P, const F
     }
 }
 
-template <int VISCID>
+template <int VISCID, class SH>
 __device__ __forceinline__ void fluid_sweep_mixed_body(const DevParams &P, const FluidSweepArgs &A, int blk)
 {
-    __shared__ int lists[kSweepWarps][kListCap][32];
+    __shared__ int lists[SH::warps][SH::cap][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = (blk * kSweepWarps + warp) * 32 + lane;
+    const int i = (blk * SH::warps + warp) * 32 + lane;
     const bool valid = i < A.n;
     int(*lst)[32] = lists[warp];
     const float4 off = valid ? A.posr[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -1102,25 +1128,25 @@ __device__ __forceinline__ void fluid_sweep_mixed_body(const DevParams &P, const
         const int zhi = __reduce_max_sync(kFull, in ? cz : INT_MIN);
         const int z0 = max(zlo - 1, 0), z1 = min(zhi + 1, P.nz - 1) + 1;
         const int gx = grow / P.ny, gy = grow - gx * P.ny;
-        gather_species_m<kFluid, VISCID>(P, A, lst, lane, cnt, in, cz, gx, gy, z0, z1, off, o, vp, acc);
-        gather_species_m<kVirt, VISCID>(P, A, lst, lane, cnt, in, cz, gx, gy, z0, z1, off, o, vp, acc);
-        gather_species<kSolid, false, VISCID, true>(P, A, lst, lane, cnt, in, cz, gx, gy, z0, z1, pa, va, acc);
+        gather_species_m<kFluid, VISCID, SH>(P, A, lst, lane, cnt, in, cz, gx, gy, z0, z1, off, o, vp, acc);
+        gather_species_m<kVirt, VISCID, SH>(P, A, lst, lane, cnt, in, cz, gx, gy, z0, z1, off, o, vp, acc);
+        gather_species<kSolid, false, VISCID, SH, true>(P, A, lst, lane, cnt, in, cz, gx, gy, z0, z1, pa, va, acc);
     }
     if (valid) fluid_update_store_m(P, A, i, off, vp, o.rho, acc, cx, cy, cz);
 }
 
-template <int VISCID>
-__global__ void __launch_bounds__(kSweepWarps * 32) kb_fluid_sweep_m(const Item<FluidSweepArgs> *__restrict__ items,
-                                                                     const int *__restrict__ bstart, int ninst)
+template <int VISCID, class SH>
+__global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep_m(const Item<FluidSweepArgs> *__restrict__ items,
+                                                                   const int *__restrict__ bstart, int ninst)
 {
     const int inst = locate_instance(bstart, ninst, blockIdx.x);
     const DevParams P = items[inst].P;
-    fluid_sweep_mixed_body<VISCID>(P, items[inst].A, (int)blockIdx.x - bstart[inst]);
+    fluid_sweep_mixed_body<VISCID, SH>(P, items[inst].A, (int)blockIdx.x - bstart[inst]);
 }
-template <int VISCID>
-__global__ void __launch_bounds__(kSweepWarps * 32) kb_fluid_sweep_m1(const DevParams P, const FluidSweepArgs A)
+template <int VISCID, class SH>
+__global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep_m1(const DevParams P, const FluidSweepArgs A)
 {
-    fluid_sweep_mixed_body<VISCID>(P, A, (int)blockIdx.x);
+    fluid_sweep_mixed_body<VISCID, SH>(P, A, (int)blockIdx.x);
 }
 
 // getVirtData (src/virt.cu:9-75) in the mixed form.
@@ -1236,41 +1262,44 @@ __device__ __forceinline__ void solid_fluid_walk_m(const DevParams &P, const int
 // solidCoupleUpdate (src/solid.cu:262-344) in the mixed form.
 __device__ __forceinline__ void couple_mixed_body(const DevParams &P, const CoupleArgs &A, int blk)
 {
-    const int i = (blk * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= A.n) return; // whole warp
-    const float4 xi = A.s_pos[i];
+    const int t = blk * blockDim.x + threadIdx.x;
+    const int i = t / kSolidGroup, g = t % kSolidGroup;
+    const bool valid = i < A.n;
     float nx = 0.0f, ny = 0.0f, nz = 0.0f, psum = 0.0f, wsum = 0.0f;
-    solid_fluid_walk_m<32>(P, A.start_f, A.fposr, A.s_cell[i], xi, lane, [&](int j, float dx, float dy, float dz) {
-        const float r2 = dist2(dx, dy, dz);
-        if (r2 < P.R2) {
-            const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
-            wsum += w;
-            psum += eos_delta(P, A.fvelp[j].w) * w;
-        }
-    });
-    Rows rows;
-    neighbor_rows(P, A.s_cell[i], rows);
-    for (int r = 0; r < rows.count; ++r) {
-        const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-        for (int j = A.start_s[c0] + lane, je = A.start_s[c1]; j < je; j += 32) {
-            const float4 q = A.s_pos[j];
-            const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
-            const float r2 = dist2(dx, dy, dz);
-            if (r2 < P.R2) {
-                const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
-                nx -= dx * w;
-                ny -= dy * w;
-                nz -= dz * w;
+    if (valid) {
+        const float4 xi = A.s_pos[i];
+        solid_fluid_walk_m<kSolidGroup>(P, A.start_f, A.fposr, A.s_cell[i], xi, g,
+                                        [&](int j, float dx, float dy, float dz) {
+                                            const float r2 = dist2(dx, dy, dz);
+                                            if (r2 < P.R2) {
+                                                const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
+                                                wsum += w;
+                                                psum += eos_delta(P, A.fvelp[j].w) * w;
+                                            }
+                                        });
+        Rows rows;
+        neighbor_rows(P, A.s_cell[i], rows);
+        for (int r = 0; r < rows.count; ++r) {
+            const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+            for (int j = A.start_s[c0] + g, je = A.start_s[c1]; j < je; j += kSolidGroup) {
+                const float4 q = A.s_pos[j];
+                const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 < P.R2) {
+                    const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
+                    nx -= dx * w;
+                    ny -= dy * w;
+                    nz -= dz * w;
+                }
             }
         }
     }
-    nx = warp_sum(nx);
-    ny = warp_sum(ny);
-    nz = warp_sum(nz);
-    psum = warp_sum(psum);
-    wsum = warp_sum(wsum);
-    if (lane) return;
+    nx = group_sum(nx);
+    ny = group_sum(ny);
+    nz = group_sum(nz);
+    psum = group_sum(psum);
+    wsum = group_sum(wsum);
+    if (!valid || g) return;
     const float l2 = nx * nx + ny * ny + nz * nz;
     if (l2 < FSIM_EPS_FOR_SUM) {
         nx = ny = nz = 0.0f;
@@ -1338,14 +1367,6 @@ __device__ __forceinline__ M3 cofactor(const M3 &a)
 // sub-step keeps the entries whose current cell is adjacent to i's, which is
 // exactly that set.  kSolidGroup lanes share one particle and combine their
 // sums with shuffles (a fixed pairing: deterministic).
-constexpr int kSolidGroup = 4;
-
-__device__ __forceinline__ float group_sum(float v)
-{
-#pragma unroll
-    for (int o = 1; o < kSolidGroup; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
-    return v;
-}
 
 // solidDeformationCalculate (src/solid.cu:10-79): F and L over the
 // reference-configuration neighbours, L^-1 (identity when singular),
@@ -1857,6 +1878,21 @@ __global__ void __launch_bounds__(kBlock) k_conservation_solid(const DevParams P
 // =================================================================== handle
 namespace {
 struct Plan; // the launches of a step (or of one phase) over a set of instances
+
+// Online autotuner of the fluid sweep's launch shape (see run_plan_step).
+struct SweepTuner {
+    int chosen = -1; // shape index once tuned
+    int next = 0;    // next shape to time
+    float ms[kSweepShapes] = {};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int shape() const { return chosen >= 0 ? chosen : 0; }
+    void release()
+    {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        e0 = e1 = nullptr;
+    }
+};
 }
 
 struct fsim_batch;
@@ -1904,6 +1940,7 @@ struct fsim_sim {
     unsigned *d_flags = nullptr;
     void *staging = nullptr;
     size_t staging_bytes = 0;
+    SweepTuner tuner;
     Plan *step_plans[2][2] = {};   // full step, by (fluid, solid) buffer parity
     Plan *phase_plans[5][2][2] = {}; // one phase, by parity
     fsim_batch *batch = nullptr;   // set while the handle belongs to a batch
@@ -1968,6 +2005,7 @@ void free_all(fsim_sim *h)
     h->sweep_events.clear();
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    h->tuner.release();
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -2059,6 +2097,8 @@ struct Launch {
     int kind;
     size_t items_off, table_off; // arena offsets
     int ninst, blocks, variant;
+    size_t shape_table_off[kSweepShapes]; // L_SWEEP: block prefix table per launch shape
+    int shape_blocks[kSweepShapes];
 };
 
 struct Plan {
@@ -2106,6 +2146,28 @@ void add_launch(Plan &pl, ArenaBuilder &ab, int kind, const std::vector<Item<Arg
     L.ninst = (int)items.size();
     L.blocks = table.back();
     L.variant = variant;
+    pl.launches.push_back(L);
+}
+
+// The fluid sweep: one block prefix table per launch shape (blocks per
+// instance depend on the warps per block).
+void add_sweep_launch(Plan &pl, ArenaBuilder &ab, const std::vector<Item<FluidSweepArgs>> &items,
+                      const std::vector<int> (&blocks)[kSweepShapes], int variant)
+{
+    Launch L{};
+    L.kind = L_SWEEP;
+    L.items_off = ab.put(items.data(), sizeof(Item<FluidSweepArgs>) * items.size());
+    L.ninst = (int)items.size();
+    L.variant = variant;
+    for (int s = 0; s < kSweepShapes; ++s) {
+        std::vector<int> table(items.size() + 1, 0);
+        for (size_t k = 0; k < items.size(); ++k) table[k + 1] = table[k] + blocks[s][k];
+        if (table.back() == 0) return; // no fluid in any instance
+        L.shape_table_off[s] = ab.put(table.data(), sizeof(int) * table.size());
+        L.shape_blocks[s] = table.back();
+    }
+    L.table_off = L.shape_table_off[0];
+    L.blocks = L.shape_blocks[0];
     pl.launches.push_back(L);
 }
 
@@ -2186,7 +2248,7 @@ void plan_couple(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, i
     for (fsim_sim *h : m) {
         it.push_back({h->P, CoupleArgs{h->s_pos[ps], h->s_cell, h->s_start, h->f_posr[pf], h->f_velp[pf], h->f_start,
                                        h->s_np, h->ns}});
-        nb.push_back(h->nf && h->ns ? blocks_for(32ll * h->ns, kBlock) : 0);
+        nb.push_back(h->nf && h->ns ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
     }
     add_launch(pl, ab, m.empty() || !m[0]->mixed ? L_COUPLE : L_COUPLE_M, it, nb);
 }
@@ -2207,7 +2269,7 @@ void plan_virt(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
 void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
 {
     std::vector<Item<FluidSweepArgs>> it;
-    std::vector<int> nb;
+    std::vector<int> nb[kSweepShapes];
     bool any_check = false;
     int nvisc = 0;
     for (fsim_sim *h : m) {
@@ -2233,7 +2295,7 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         A.keep = h->keep ? 1 : 0;
         A.cm = h->f_cm;
         it.push_back({h->P, A});
-        nb.push_back(blocks_for(h->nf, kSweepWarps * 32));
+        for (int sh = 0; sh < kSweepShapes; ++sh) nb[sh].push_back(blocks_for(h->nf, kShapeWarps[sh] * 32));
         if (h->nf) {
             any_check = any_check || h->check_z;
             nvisc += h->P.viscid ? 1 : 0;
@@ -2243,7 +2305,7 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
     const int visc_mode = nvisc == 0 ? 0 : nvisc == n_active ? 1 : 2;
     const size_t before = pl.launches.size();
     const bool mixed = !m.empty() && m[0]->mixed;
-    add_launch(pl, ab, L_SWEEP, it, nb, mixed ? 6 + visc_mode : (any_check ? 3 : 0) + visc_mode);
+    add_sweep_launch(pl, ab, it, nb, mixed ? 6 + visc_mode : (any_check ? 3 : 0) + visc_mode);
     if (pl.launches.size() > before) pl.sweep_index = (int)before;
 }
 
@@ -2347,19 +2409,32 @@ const Item<Args> &host_item(const Plan &pl, const Launch &L)
 #define FSIM_LAUNCH(KB, ARGS, THREADS) KB<<<g, THREADS, 0, st>>>(items_of<ARGS>(pl, L), tb, n)
 
 // Enqueue a plan's launches; optional events around the fluid sweep.
-fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, cudaEvent_t sweep0 = nullptr, cudaEvent_t sweep1 = nullptr)
+fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0 = nullptr,
+                         cudaEvent_t sweep1 = nullptr)
 {
     using SweepFn = void (*)(const Item<FluidSweepArgs> *, const int *, int);
     using Sweep1Fn = void (*)(const DevParams, const FluidSweepArgs);
-    // variants 0-5: plain (CHECK_Z, VISCID); 6-8: mixed (VISCID)
-    static const SweepFn sweeps[9] = {kb_fluid_sweep<false, 0>, kb_fluid_sweep<false, 1>, kb_fluid_sweep<false, 2>,
-                                      kb_fluid_sweep<true, 0>,  kb_fluid_sweep<true, 1>,  kb_fluid_sweep<true, 2>,
-                                      kb_fluid_sweep_m<0>,      kb_fluid_sweep_m<1>,      kb_fluid_sweep_m<2>};
-    static const Sweep1Fn sweeps1[9] = {kb_fluid_sweep_1<false, 0>, kb_fluid_sweep_1<false, 1>,
-                                        kb_fluid_sweep_1<false, 2>, kb_fluid_sweep_1<true, 0>,
-                                        kb_fluid_sweep_1<true, 1>,  kb_fluid_sweep_1<true, 2>,
-                                        kb_fluid_sweep_m1<0>,       kb_fluid_sweep_m1<1>,
-                                        kb_fluid_sweep_m1<2>};
+    // [variant][shape]; variants 0-5: plain (CHECK_Z, VISCID); 6-8: mixed (VISCID)
+    static const SweepFn sweeps[9][kSweepShapes] = {
+        {kb_fluid_sweep<false, 0, Shape0>, kb_fluid_sweep<false, 0, Shape1>, kb_fluid_sweep<false, 0, Shape2>},
+        {kb_fluid_sweep<false, 1, Shape0>, kb_fluid_sweep<false, 1, Shape1>, kb_fluid_sweep<false, 1, Shape2>},
+        {kb_fluid_sweep<false, 2, Shape0>, kb_fluid_sweep<false, 2, Shape1>, kb_fluid_sweep<false, 2, Shape2>},
+        {kb_fluid_sweep<true, 0, Shape0>, kb_fluid_sweep<true, 0, Shape1>, kb_fluid_sweep<true, 0, Shape2>},
+        {kb_fluid_sweep<true, 1, Shape0>, kb_fluid_sweep<true, 1, Shape1>, kb_fluid_sweep<true, 1, Shape2>},
+        {kb_fluid_sweep<true, 2, Shape0>, kb_fluid_sweep<true, 2, Shape1>, kb_fluid_sweep<true, 2, Shape2>},
+        {kb_fluid_sweep_m<0, Shape0>, kb_fluid_sweep_m<0, Shape1>, kb_fluid_sweep_m<0, Shape2>},
+        {kb_fluid_sweep_m<1, Shape0>, kb_fluid_sweep_m<1, Shape1>, kb_fluid_sweep_m<1, Shape2>},
+        {kb_fluid_sweep_m<2, Shape0>, kb_fluid_sweep_m<2, Shape1>, kb_fluid_sweep_m<2, Shape2>}};
+    static const Sweep1Fn sweeps1[9][kSweepShapes] = {
+        {kb_fluid_sweep_1<false, 0, Shape0>, kb_fluid_sweep_1<false, 0, Shape1>, kb_fluid_sweep_1<false, 0, Shape2>},
+        {kb_fluid_sweep_1<false, 1, Shape0>, kb_fluid_sweep_1<false, 1, Shape1>, kb_fluid_sweep_1<false, 1, Shape2>},
+        {kb_fluid_sweep_1<false, 2, Shape0>, kb_fluid_sweep_1<false, 2, Shape1>, kb_fluid_sweep_1<false, 2, Shape2>},
+        {kb_fluid_sweep_1<true, 0, Shape0>, kb_fluid_sweep_1<true, 0, Shape1>, kb_fluid_sweep_1<true, 0, Shape2>},
+        {kb_fluid_sweep_1<true, 1, Shape0>, kb_fluid_sweep_1<true, 1, Shape1>, kb_fluid_sweep_1<true, 1, Shape2>},
+        {kb_fluid_sweep_1<true, 2, Shape0>, kb_fluid_sweep_1<true, 2, Shape1>, kb_fluid_sweep_1<true, 2, Shape2>},
+        {kb_fluid_sweep_m1<0, Shape0>, kb_fluid_sweep_m1<0, Shape1>, kb_fluid_sweep_m1<0, Shape2>},
+        {kb_fluid_sweep_m1<1, Shape0>, kb_fluid_sweep_m1<1, Shape1>, kb_fluid_sweep_m1<1, Shape2>},
+        {kb_fluid_sweep_m1<2, Shape0>, kb_fluid_sweep_m1<2, Shape1>, kb_fluid_sweep_m1<2, Shape2>}};
     for (size_t k = 0; k < pl.launches.size(); ++k) {
         const Launch &L = pl.launches[k];
         const int *tb = reinterpret_cast<const int *>(pl.arena + L.table_off);
@@ -2377,11 +2452,15 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, cudaEvent_t sweep0 = n
         case L_VIRT: FSIM_LAUNCH(kb_virt, VirtArgs, kBlock); break;
         case L_SWEEP:
             if (sweep0) CK(cudaEventRecord(sweep0, st));
-            if (n == 1) {
-                const Item<FluidSweepArgs> &it = host_item<FluidSweepArgs>(pl, L);
-                sweeps1[L.variant]<<<g, kSweepWarps * 32, 0, st>>>(it.P, it.A);
-            } else {
-                sweeps[L.variant]<<<g, kSweepWarps * 32, 0, st>>>(items_of<FluidSweepArgs>(pl, L), tb, n);
+            {
+                const int *tbs = reinterpret_cast<const int *>(pl.arena + L.shape_table_off[shape]);
+                const int gs = L.shape_blocks[shape], thr = kShapeWarps[shape] * 32;
+                if (n == 1) {
+                    const Item<FluidSweepArgs> &it = host_item<FluidSweepArgs>(pl, L);
+                    sweeps1[L.variant][shape]<<<gs, thr, 0, st>>>(it.P, it.A);
+                } else {
+                    sweeps[L.variant][shape]<<<gs, thr, 0, st>>>(items_of<FluidSweepArgs>(pl, L), tbs, n);
+                }
             }
             CK_LAUNCH();
             if (sweep1) CK(cudaEventRecord(sweep1, st));
@@ -2402,11 +2481,11 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, cudaEvent_t sweep0 = n
     return FSIM_OK;
 }
 
-fsim_status capture_plan(Plan &pl, cudaStream_t st)
+fsim_status capture_plan(Plan &pl, cudaStream_t st, int shape)
 {
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    fsim_status s = enqueue_plan(pl, st);
+    fsim_status s = enqueue_plan(pl, st, shape);
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (s) {
         if (graph) cudaGraphDestroy(graph);
@@ -2453,13 +2532,44 @@ fsim_status handle_step_plan(fsim_sim *h, Plan **out)
     return FSIM_OK;
 }
 
+// One step of a plan: while the sweep's launch shape is untuned, run launch
+// by launch with the next candidate shape and time its sweep (CUDA events on
+// the stream, waited for on the host); once every shape has been timed, keep
+// the fastest and run the plan as a CUDA graph captured with it.
+fsim_status run_plan_step(Plan &pl, cudaStream_t st, SweepTuner &t)
+{
+    if (t.chosen < 0 && pl.sweep_index >= 0) {
+        if (!t.e0) {
+            CK(cudaEventCreate(&t.e0));
+            CK(cudaEventCreate(&t.e1));
+        }
+        const int s = t.next;
+        fsim_status r = enqueue_plan(pl, st, s, t.e0, t.e1);
+        if (r) return r;
+        CK(cudaEventSynchronize(t.e1));
+        CK(cudaEventElapsedTime(&t.ms[s], t.e0, t.e1));
+        if (++t.next == kSweepShapes) {
+            t.chosen = 0;
+            for (int k = 1; k < kSweepShapes; ++k)
+                if (t.ms[k] < t.ms[t.chosen]) t.chosen = k;
+        }
+        return FSIM_OK;
+    }
+    if (t.chosen < 0) t.chosen = 0; // no fluid: nothing to tune
+    if (!pl.graph) {
+        fsim_status r = capture_plan(pl, st, t.chosen);
+        if (r) return r;
+    }
+    CK(cudaGraphLaunch(pl.graph, st));
+    return FSIM_OK;
+}
+
 fsim_status run_step_graph(fsim_sim *h)
 {
     Plan *pl = nullptr;
     fsim_status st = handle_step_plan(h, &pl);
     if (st) return st;
-    if (!pl->graph && (st = capture_plan(*pl, h->stream))) return st;
-    CK(cudaGraphLaunch(pl->graph, h->stream));
+    if ((st = run_plan_step(*pl, h->stream, h->tuner))) return st;
     after_plan(h, kAllPhases, *pl);
     return FSIM_OK;
 }
@@ -2530,7 +2640,7 @@ fsim_status sort_virtual(fsim_sim *h, const float *vpos_host)
     pl.host = ab.bytes;
     CK(cudaMalloc((void **)&pl.arena, ab.bytes.size()));
     cudaError_t e = cudaMemcpy(pl.arena, ab.bytes.data(), ab.bytes.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && (st = enqueue_plan(pl, h->stream)) == FSIM_OK) {
+    if (e == cudaSuccess && (st = enqueue_plan(pl, h->stream, 0)) == FSIM_OK) {
         e = cudaMemsetAsync(h->v_velp, 0, sizeof(float4) * n, h->stream);
         k_virt_normal<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(h->P, h->v_posr, h->v_cell, h->v_start,
                                                                         h->v_normal, n);
@@ -2873,7 +2983,7 @@ extern "C" fsim_status fsim_run_phase(fsim_handle h, int phase)
         fsim_status st = build_plan({h}, 1u << phase, h->f_cur, h->s_cur, &pl);
         if (st) return st;
     }
-    fsim_status st = enqueue_plan(*pl, h->stream);
+    fsim_status st = enqueue_plan(*pl, h->stream, h->tuner.shape());
     if (st) return st;
     after_plan(h, 1u << phase, *pl);
     return FSIM_OK;
@@ -3199,7 +3309,8 @@ extern "C" fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_m
     for (int k = 0; k < nsteps; ++k) {
         Plan *pl = nullptr;
         if ((st = handle_step_plan(h, &pl))) return st;
-        if ((st = enqueue_plan(*pl, h->stream, h->sweep_events[2 * k], h->sweep_events[2 * k + 1]))) return st;
+        if ((st = enqueue_plan(*pl, h->stream, h->tuner.shape(), h->sweep_events[2 * k], h->sweep_events[2 * k + 1])))
+            return st;
         after_plan(h, kAllPhases, *pl);
     }
     CK(cudaEventRecord(h->ev1, h->stream));
@@ -3307,6 +3418,7 @@ struct fsim_batch {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    SweepTuner tuner;
     std::vector<fsim_sim *> members;
     Plan *plans[2][2] = {}; // by (fluid, solid) parity of the members
 };
@@ -3348,6 +3460,7 @@ void free_batch(fsim_batch *b)
         }
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    b->tuner.release();
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -3359,11 +3472,8 @@ fsim_status batch_step_once(fsim_batch *b)
         fsim_status st = build_plan(b->members, kAllPhases, pf, ps, &pl);
         if (st) return st;
     }
-    if (!pl->graph) {
-        fsim_status st = capture_plan(*pl, b->stream);
-        if (st) return st;
-    }
-    CK(cudaGraphLaunch(pl->graph, b->stream));
+    fsim_status st = run_plan_step(*pl, b->stream, b->tuner);
+    if (st) return st;
     for (fsim_sim *h : b->members) after_plan(h, kAllPhases, *pl);
     return FSIM_OK;
 }
@@ -3472,6 +3582,28 @@ extern "C" fsim_status fsim_batch_launches_per_step(fsim_batch_t b, int *n)
     }
     *n = (int)pl->launches.size();
     return FSIM_OK;
+}
+
+namespace {
+fsim_status report_tuning(const SweepTuner &t, int *chosen, float *ms, int n)
+{
+    if (!chosen || (n > 0 && !ms) || n < 0) return FSIM_EINVAL;
+    *chosen = t.chosen;
+    for (int k = 0; k < n; ++k) ms[k] = k < kSweepShapes && k < t.next ? t.ms[k] : 0.0f;
+    return FSIM_OK;
+}
+} // namespace
+
+extern "C" fsim_status fsim_sweep_tuning(fsim_handle h, int *chosen, float *ms, int n)
+{
+    if (!h) return FSIM_EINVAL;
+    return report_tuning(h->tuner, chosen, ms, n);
+}
+
+extern "C" fsim_status fsim_batch_sweep_tuning(fsim_batch_t b, int *chosen, float *ms, int n)
+{
+    if (!b) return FSIM_EINVAL;
+    return report_tuning(b->tuner, chosen, ms, n);
 }
 
 extern "C" fsim_status fsim_batch_destroy(fsim_batch_t b)

@@ -31,6 +31,7 @@ class Request:
     particles: int = 0       # fluid + solid, set when generated
     done_at: float = float("nan")
     result: dict = field(default_factory=dict)
+    data: object = None      # (config, particles) when generated ahead of the stream
 
 
 def poisson_stream(n, rate, seed=7, fluid_range=(10_000, 1_000_000), solid_range=(1_000, 27_000),
@@ -55,6 +56,15 @@ def poisson_stream(n, rate, seed=7, fluid_range=(10_000, 1_000_000), solid_range
     return out
 
 
+def pregenerate(requests):
+    """Generate every request's particles ahead of the stream (a served request
+    arrives with its data; generation is not part of serving)."""
+    for r in requests:
+        r.data = cases.make((r.cfg, r.case))
+        r.particles = r.data[1].n_fluid + r.data[1].n_solid
+    return requests
+
+
 def _result_fields(sim):
     out = {"fluid_pos": sim.get("fluid_pos"), "fluid_vel": sim.get("fluid_vel"), "fluid_rho": sim.get("fluid_rho")}
     if sim.n["solid"]:
@@ -74,7 +84,7 @@ class GpuBackend:
 
     def prepare(self, r):
         """Generate the request's particles; returns (particles, device bytes)."""
-        cfg, pa = cases.make((r.cfg, r.case))
+        cfg, pa = r.data if r.data is not None else cases.make((r.cfg, r.case))
         return (cfg, pa), api.estimate_bytes(cfg, pa.n_fluid, pa.n_solid, pa.n_virt), pa.n_fluid + pa.n_solid
 
     def create(self, prepared):
@@ -96,13 +106,19 @@ class Server:
 
     Every loop turn: release requests whose arrival time has passed into the
     waiting queue; admit from its head while the estimated device memory of
-    the admitted requests stays within the budget (a request larger than the
-    budget is admitted alone when nothing else runs); rebuild the batch when
-    its membership changed; advance the batch by `quantum` steps (fewer if a
-    member needs fewer); retire members whose steps are done."""
+    the admitted requests stays within the HBM budget and their particles
+    within the work budget `max_particles` (a request larger than a budget is
+    admitted alone when nothing else runs); rebuild the batch when its
+    membership changed; advance the batch by `quantum` steps (fewer if a member
+    needs fewer); retire members whose steps are done.
 
-    def __init__(self, budget_bytes, backend=None, quantum=10, keep_results=False):
+    The work budget bounds the batch at about what saturates the GPU: beyond
+    that, admitting more only slows every running request down (they share the
+    GPU), raising latency without raising throughput."""
+
+    def __init__(self, budget_bytes, backend=None, quantum=10, keep_results=False, max_particles=None):
         self.budget = budget_bytes
+        self.max_particles = max_particles
         self.backend = backend or GpuBackend()
         self.quantum = quantum
         self.keep_results = keep_results
@@ -114,6 +130,7 @@ class Server:
         waiting, active = [], []  # active entries: [request, instance, steps left, bytes]
         prepared = {}
         nxt, used, batch = 0, 0, None
+        load = 0  # particles of the admitted requests
         t0 = clock()
         completed, work, rebuilds = 0, 0, 0
         while completed < len(reqs):
@@ -129,11 +146,14 @@ class Server:
                 data, need, npart = prepared[r.rid]
                 if active and used + need > self.budget:
                     break
+                if active and self.max_particles is not None and load + npart > self.max_particles:
+                    break
                 waiting.pop(0)
                 del prepared[r.rid]
                 r.particles = npart
                 active.append([r, be.create(data), r.steps, need])
                 used += need
+                load += npart
                 changed = True
                 self.log.append(("admit", r.rid, clock() - t0))
             if not active:
@@ -164,6 +184,7 @@ class Server:
                         a[0].result = be.result(a[1])
                     be.destroy(a[1])
                     used -= a[3]
+                    load -= a[0].particles
                     completed += 1
                     self.log.append(("done", a[0].rid, now))
                 active = [a for a in active if a[2] > 0]
@@ -185,7 +206,7 @@ def serve_one_by_one(requests, device=0, clock=time.perf_counter, keep_results=F
         wait = r.arrival - (clock() - t0)
         if wait > 0:
             time.sleep(wait)
-        cfg, pa = cases.make((r.cfg, r.case))
+        cfg, pa = r.data if r.data is not None else cases.make((r.cfg, r.case))
         r.particles = pa.n_fluid + pa.n_solid
         with api.Simulation(cfg, pa, device=device) as sim:
             sim.step(r.steps)

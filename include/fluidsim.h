@@ -248,6 +248,17 @@ fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_ms, float *s
 /* Kernel launches one fsim_step(h, 1) issues (for launch accounting). */
 fsim_status fsim_launches_per_step(fsim_handle h, int *n);
 
+/* Launch-shape autotuner of the fluid sweep (no counterpart in the reference).
+ * The sweep has FSIM_SWEEP_SHAPES launch shapes (warps per block / per-lane
+ * neighbour-list capacity in shared memory: 0 = 4/48, 1 = 4/32, 2 = 8/32), all
+ * giving bit-identical results.  The first FSIM_SWEEP_SHAPES steps of a handle
+ * (or of a batch) run one shape each, launch by launch, with CUDA events around
+ * the sweep; the fastest is then used for the CUDA graph of every later step.
+ * *chosen = the chosen shape (-1 while tuning), ms[k] = the timed sweep of
+ * shape k (0 if not yet timed), for k < n. */
+#define FSIM_SWEEP_SHAPES 3
+fsim_status fsim_sweep_tuning(fsim_handle h, int *chosen, float *ms, int n);
+
 /* Conservation totals of the current state, accumulated in FP64 on the device
  * (per-particle terms in FP64, fixed-order block sums; deterministic).  No
  * counterpart in the reference.  Particle mass m = density * particle_volume
@@ -288,6 +299,8 @@ fsim_status fsim_batch_sync(fsim_batch_t b);
 fsim_status fsim_batch_time_steps(fsim_batch_t b, int nsteps, float *ms);
 /* Kernel launches of one batched step. */
 fsim_status fsim_batch_launches_per_step(fsim_batch_t b, int *n);
+/* The batch's own sweep autotuner (see fsim_sweep_tuning). */
+fsim_status fsim_batch_sweep_tuning(fsim_batch_t b, int *chosen, float *ms, int n);
 /* Dissolve the batch; the members continue as standalone handles. */
 fsim_status fsim_batch_destroy(fsim_batch_t b);
 

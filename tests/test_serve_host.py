@@ -103,3 +103,16 @@ def test_work_accounting():
     out = serve.Server(budget_bytes=10, backend=be, quantum=7).run(_reqs([0, 0.001, 0.002], [13, 5, 9]),
                                                                   clock=clock, sleep=clock.sleep)
     assert out["particle_updates"] == 1000 * (13 + 5 + 9)
+
+
+def test_work_budget_bounds_concurrency():
+    """max_particles caps the particles of the running batch (1000 per request
+    here): at most two run together, the rest wait in arrival order."""
+    clock = FakeClock()
+    be = FakeBackend(clock, mem={k: 1 for k in range(5)})
+    srv = serve.Server(budget_bytes=10 ** 9, backend=be, quantum=5, max_particles=2500)
+    out = srv.run(_reqs([0, 0, 0, 0, 0], [10, 20, 10, 10, 10]), clock=clock, sleep=clock.sleep)
+    assert out["requests"] == 5 and not be.alive
+    assert max(len(b) for b in be.batches) == 2
+    admits = [rid for ev, rid, _ in srv.log if ev == "admit"]
+    assert admits == [0, 1, 2, 3, 4]
