@@ -145,6 +145,13 @@ def load():
         "fsim_conservation": (C.c_int, [P, C.POINTER(C.c_double), C.c_int]),
         "fsim_measure_fp32_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
         "fsim_sweep_tuning": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
+        "fsim_snapshot_bytes": (C.c_int, [P, C.POINTER(C.c_size_t)]),
+        "fsim_probe": (C.c_int, [P, P, C.c_int, P]),
+        "fsim_write_vtk_binary": (C.c_int, [P, C.c_char_p, C.c_int]),
+        "fsim_snapshot_save": (C.c_int, [P, C.c_longlong, P, C.c_size_t]),
+        "fsim_snapshot_load": (C.c_int, [P, C.c_size_t, C.c_int, C.POINTER(P), C.POINTER(C.c_longlong)]),
+        "fsim_snapshot_write": (C.c_int, [P, C.c_longlong, C.c_char_p]),
+        "fsim_snapshot_read": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(P), C.POINTER(C.c_longlong)]),
         "fsim_batch_sweep_tuning": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
         "fsim_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
         "fsim_host_free": (C.c_int, [P]),
@@ -176,7 +183,9 @@ EXPORTED = [
     "fsim_launches_per_step", "fsim_host_alloc", "fsim_host_free", "fsim_counts", "fsim_get_derived",
     "fsim_cell_sort_noalloc", "fsim_batch_create", "fsim_batch_step", "fsim_batch_sync", "fsim_batch_time_steps",
     "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes", "fsim_conservation",
-    "fsim_measure_fp32_peak", "fsim_sweep_tuning", "fsim_batch_sweep_tuning",
+    "fsim_measure_fp32_peak", "fsim_sweep_tuning", "fsim_batch_sweep_tuning", "fsim_snapshot_bytes",
+    "fsim_snapshot_save", "fsim_snapshot_load", "fsim_snapshot_write", "fsim_snapshot_read", "fsim_probe",
+    "fsim_write_vtk_binary",
 ]
 SWEEP_SHAPES = ((4, 48), (4, 32), (8, 32))  # (warps per block, list capacity) per shape index
 
@@ -336,9 +345,53 @@ class Simulation:
         self.particles = particles
         self.h = C.c_void_p()
         check(self.lib.fsim_create(C.byref(cfg), C.byref(particles.struct()), device, C.byref(self.h)))
+        self._set_counts()
+        self.snapshot_step = None
+
+    def _set_counts(self):
         nf, ns, nv = C.c_int(), C.c_int(), C.c_int()
         check(self.lib.fsim_counts(self.h, C.byref(nf), C.byref(ns), C.byref(nv)))
         self.n = {"fluid": nf.value, "solid": ns.value, "virt": nv.value}
+
+    @classmethod
+    def _from_handle(cls, h, step):
+        self = cls.__new__(cls)
+        self.lib, self.h, self.cfg, self.particles = load(), h, None, None
+        self._set_counts()
+        self.snapshot_step = step
+        return self
+
+    @classmethod
+    def from_snapshot(cls, data, device=-1):
+        """Restore an instance from fsim_snapshot_save bytes (a bytes object or uint8 array)."""
+        buf = np.frombuffer(data, np.uint8) if not isinstance(data, np.ndarray) else data
+        h, step = C.c_void_p(), C.c_longlong()
+        check(load().fsim_snapshot_load(buf.ctypes.data, buf.nbytes, device, C.byref(h), C.byref(step)))
+        return cls._from_handle(h, step.value)
+
+    @classmethod
+    def from_snapshot_file(cls, path, device=-1):
+        h, step = C.c_void_p(), C.c_longlong()
+        check(load().fsim_snapshot_read(os.fsencode(path), device, C.byref(h), C.byref(step)))
+        return cls._from_handle(h, step.value)
+
+    def probe(self, points):
+        """(n, 5) float32: Shepard-averaged u, v, w, p, rho at each point (fsim_probe)."""
+        pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        out = np.empty((len(pts), 5), np.float32)
+        check(self.lib.fsim_probe(self.h, pts.ctypes.data, len(pts), out.ctypes.data))
+        return out
+
+    def snapshot(self, step=0):
+        """The instance's state as snapshot bytes (numpy uint8 array)."""
+        n = C.c_size_t()
+        check(self.lib.fsim_snapshot_bytes(self.h, C.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        check(self.lib.fsim_snapshot_save(self.h, step, buf.ctypes.data, buf.nbytes))
+        return buf
+
+    def snapshot_write(self, path, step=0):
+        check(self.lib.fsim_snapshot_write(self.h, step, os.fsencode(path)))
 
     def close(self):
         if self.h:
@@ -408,8 +461,9 @@ class Simulation:
         check(self.lib.fsim_get_derived(self.h, C.byref(d)))
         return d
 
-    def write_vtk(self, out_dir, file_step):
-        check(self.lib.fsim_write_vtk(self.h, os.fsencode(out_dir), file_step))
+    def write_vtk(self, out_dir, file_step, binary=False):
+        fn = self.lib.fsim_write_vtk_binary if binary else self.lib.fsim_write_vtk
+        check(fn(self.h, os.fsencode(out_dir), file_step))
 
     def time_steps(self, n):
         ms = C.c_float()

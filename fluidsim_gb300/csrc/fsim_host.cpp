@@ -9,6 +9,7 @@
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -620,16 +621,34 @@ extern "C" fsim_status fsim_case_generate(const fsim_case *cs, const fsim_config
 // numbers through std::to_string(float) ("%f").
 namespace {
 
+// Legacy VTK polydata.  ASCII: the reference's text (std::to_string, 6
+// decimals).  BINARY: the same sections with the numbers as big-endian FP32,
+// as the legacy format defines them (exact values, ~10x smaller, no formatting).
 struct VtkFile {
     std::string s;
+    bool binary = false;
     void header(const char *title, int n)
     {
         s = "# vtk DataFile Version 2.0\n";
         s += title;
-        s += "\nASCII\nDATASET POLYDATA\nPOINTS " + std::to_string(n) + " float\n";
+        s += binary ? "\nBINARY\n" : "\nASCII\n";
+        s += "DATASET POLYDATA\nPOINTS " + std::to_string(n) + " float\n";
+    }
+    void put_be(float v)
+    {
+        uint32_t u;
+        std::memcpy(&u, &v, 4);
+        const char b[4] = {(char)(u >> 24), (char)(u >> 16), (char)(u >> 8), (char)u};
+        s.append(b, 4);
     }
     void points(const float *p, int n)
     {
+        if (binary) {
+            s.reserve(s.size() + 12 * (size_t)n + 1);
+            for (size_t i = 0; i < 3 * (size_t)n; ++i) put_be(p[i]);
+            s += "\n";
+            return;
+        }
         for (int i = 0; i < n; ++i)
             s += std::to_string(p[3 * i]) + " " + std::to_string(p[3 * i + 1]) + " " + std::to_string(p[3 * i + 2]) +
                  "\n";
@@ -644,6 +663,12 @@ struct VtkFile {
     {
         s += "POINT_DATA " + std::to_string(n) + "\n";
         s += std::string("SCALARS ") + name + " float 1\nLOOKUP_TABLE default\n";
+        if (binary) {
+            s.reserve(s.size() + 4 * (size_t)n + 1);
+            for (int i = 0; i < n; ++i) put_be(constant ? *constant : v[i]);
+            s += "\n";
+            return;
+        }
         for (int i = 0; i < n; ++i) s += std::to_string(constant ? *constant : v[i]) + "\n";
     }
     bool write(const std::string &path) const
@@ -657,12 +682,13 @@ struct VtkFile {
 
 } // namespace
 
-fsim_status fsim_write_vtk_host(const char *out_dir, int file_step, const VtkHostState &st)
+fsim_status fsim_write_vtk_host(const char *out_dir, int file_step, const VtkHostState &st, bool binary)
 {
     std::string base(out_dir);
     make_dir(base);
     const std::string k = std::to_string(file_step);
     VtkFile f;
+    f.binary = binary;
     if (st.n_fluid) {
         std::string d = base + "/fluid";
         make_dir(d);

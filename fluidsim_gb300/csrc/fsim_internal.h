@@ -23,4 +23,4 @@ struct VtkHostState {
     float solid_density;
     const float *vpos, *vnormal, *vp;
 };
-fsim_status fsim_write_vtk_host(const char *out_dir, int file_step, const VtkHostState &st);
+fsim_status fsim_write_vtk_host(const char *out_dir, int file_step, const VtkHostState &st, bool binary = false);

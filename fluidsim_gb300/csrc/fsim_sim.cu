@@ -28,6 +28,8 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -1610,6 +1612,107 @@ __device__ __forceinline__ void solid_update_body(const DevParams &P, const Soli
 FSIM_BATCHED_KERNEL(kb_solid_update, SolidArgs, solid_update_body, kBlock)
 
 
+
+// ------------------------------------------------------------------ probes
+// Probe::getData (src/probe.cu, commented out in the reference, 2D), in 3D:
+// the Shepard average, weight (exp(-r^2/h^2) - c1) c2 as in
+// solidPressureCalculate, of fluid velocity, pressure and density and of solid
+// velocity and pressure (solid density 0) over the particles within the
+// impact distance in the 27 cells of the probe's cell (cell lists of the last
+// cell phase, current positions); (0, 0, rho0) when none is in range or the
+// probe is outside the grid.  One warp per probe.
+struct ProbeArgs {
+    const float *pts;
+    int n;
+    float *out; // 5 per probe: u, v, w, p, rho
+    const float4 *fposr, *fvelp;
+    const int *start_f;
+    const float4 *s_pos, *s_vel, *s_np;
+    const int *start_s;
+};
+__global__ void k_probe(const DevParams P, const ProbeArgs A)
+{
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= A.n) return; // whole warp
+    const float4 xi = make_float4(A.pts[3 * k], A.pts[3 * k + 1], A.pts[3 * k + 2], 0.0f);
+    const float xa[3] = {xi.x, xi.y, xi.z};
+    int c[3];
+    bool inside = true;
+    const int nn[3] = {P.nx, P.ny, P.nz};
+    for (int a = 0; a < 3; ++a) {
+        c[a] = (int)__fmul_rn(__fsub_rn(xa[a], P.cmin[a]), P.cinv[a]);
+        inside = inside && c[a] >= 0 && c[a] < nn[a];
+    }
+    float w_sum = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f, p = 0.0f, rho = 0.0f;
+    if (inside) {
+        const int cell = (c[0] * P.ny + c[1]) * P.nz + c[2];
+        auto fluid = [&](int j, float dx, float dy, float dz) {
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2) {
+                const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
+                const float4 q = A.fposr[j], u = A.fvelp[j];
+                w_sum += w;
+                ux += u.x * w;
+                uy += u.y * w;
+                uz += u.z * w;
+                if (P.mixed) {
+                    p += eos_delta(P, u.w) * w;
+                    rho += fmaf(P.rho0, u.w, P.rho0) * w;
+                } else {
+                    p += u.w * w;
+                    rho += q.w * w;
+                }
+            }
+        };
+        if (P.mixed) {
+            solid_fluid_walk_m<32>(P, A.start_f, A.fposr, cell, xi, lane, fluid);
+        }
+        Rows rows;
+        neighbor_rows(P, cell, rows);
+        for (int r = 0; r < rows.count; ++r) {
+            const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+            if (!P.mixed) {
+                for (int j = A.start_f[c0] + lane, je = A.start_f[c1]; j < je; j += 32) {
+                    const float4 q = A.fposr[j];
+                    fluid(j, q.x - xi.x, q.y - xi.y, q.z - xi.z);
+                }
+            }
+            for (int j = A.start_s[c0] + lane, je = A.start_s[c1]; j < je; j += 32) {
+                const float4 q = A.s_pos[j];
+                const float r2 = dist2(q.x - xi.x, q.y - xi.y, q.z - xi.z);
+                if (r2 < P.R2) {
+                    const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
+                    const float4 v = A.s_vel[j];
+                    w_sum += w;
+                    ux += v.x * w;
+                    uy += v.y * w;
+                    uz += v.z * w;
+                    p += A.s_np[j].w * w;
+                }
+            }
+        }
+    }
+    w_sum = warp_sum(w_sum);
+    ux = warp_sum(ux);
+    uy = warp_sum(uy);
+    uz = warp_sum(uz);
+    p = warp_sum(p);
+    rho = warp_sum(rho);
+    if (lane) return;
+    float *o = A.out + 5 * (size_t)k;
+    if (w_sum != 0.0f) {
+        o[0] = ux / w_sum;
+        o[1] = uy / w_sum;
+        o[2] = uz / w_sum;
+        o[3] = p / w_sum;
+        o[4] = rho / w_sum;
+    } else {
+        o[0] = o[1] = o[2] = o[3] = 0.0f;
+        o[4] = P.rho0;
+    }
+}
+
 // ------------------------------------------------------- neighbour counts
 __global__ void k_neighbor_counts(const DevParams P, const float4 *__restrict__ fposr, const int *__restrict__ cell_f,
                                   const int *__restrict__ start_f, const float4 *__restrict__ s_pos,
@@ -2740,9 +2843,10 @@ fsim_status build_solid_neighbors(fsim_sim *h, const float *ref)
     return FSIM_OK;
 }
 
-fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
+// Stream, events and every device array of a handle whose counts are set.
+fsim_status alloc_state(fsim_sim *h)
 {
-    const int nf = p->n_fluid, ns = p->n_solid, nv = p->n_virt, nc = h->ncell;
+    const int nf = h->nf, ns = h->ns, nv = h->nv, nc = h->ncell;
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&h->ev0));
     CK(cudaEventCreate(&h->ev1));
@@ -2788,11 +2892,19 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
     if ((st = dalloc(h, (char **)&h->staging, h->staging_bytes))) return st;
 
     // empty cell structures are valid before the first cell phase
+    CK(cudaMemsetAsync(h->f_cell, 0, sizeof(int) * (nf ? nf : 1), h->stream));
     CK(cudaMemsetAsync(h->f_start, 0, sizeof(int) * (nc + 1), h->stream));
     CK(cudaMemsetAsync(h->s_start, 0, sizeof(int) * (nc + 1), h->stream));
     CK(cudaMemsetAsync(h->v_start, 0, sizeof(int) * (nc + 1), h->stream));
     CK(cudaMemsetAsync(h->s_np, 0, sizeof(float4) * (ns ? ns : 1), h->stream));
+    return FSIM_OK;
+}
 
+fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
+{
+    const int nf = p->n_fluid, ns = p->n_solid, nv = p->n_virt;
+    fsim_status st = alloc_state(h);
+    if (st) return st;
     float *stg = (float *)h->staging;
     if (nf) {
         CK(cudaMemcpyAsync(stg, p->fluid_pos, sizeof(float) * 3 * nf, cudaMemcpyHostToDevice, h->stream));
@@ -2850,17 +2962,12 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
 } // namespace
 
 // =================================================================== C ABI
-extern "C" fsim_status fsim_create(const fsim_config *cfg, const fsim_particles *p, int device, fsim_handle *out)
+namespace {
+// A handle with its configuration, derived constants, device parameters and
+// counts set and checked; nothing allocated on the device yet.
+fsim_status new_handle(const fsim_config *cfg, int nf, int ns, int nv, int device, fsim_sim **out)
 {
-    if (!cfg || !p || !out) return FSIM_EINVAL;
     *out = nullptr;
-    if (p->n_fluid < 0 || p->n_solid < 0 || p->n_virt < 0 || (p->n_fluid && (!p->fluid_pos || !p->fluid_vel ||
-                                                                             !p->fluid_rho || !p->fluid_p)) ||
-        (p->n_solid && (!p->solid_pos || !p->solid_vel || !p->solid_ref_pos || !p->solid_type)) ||
-        (p->n_virt && !p->virt_pos)) {
-        fsim_set_error("invalid particle arrays");
-        return FSIM_EINVAL;
-    }
     if (cfg->solid_sub_step < 1 || !(cfg->dt > 0.0f)) {
         fsim_set_error("dt must be > 0 and solid_sub_step >= 1");
         return FSIM_EINVAL;
@@ -2887,11 +2994,10 @@ extern "C" fsim_status fsim_create(const fsim_config *cfg, const fsim_particles 
         }
     }
     h->device = device;
-    DeviceGuard guard(device);
     fill_params(h);
-    h->nf = p->n_fluid;
-    h->ns = p->n_solid;
-    h->nv = p->n_virt;
+    h->nf = nf;
+    h->ns = ns;
+    h->nv = nv;
     h->ncell = h->der.cell_number_total;
     h->keep = cfg->keep_derivatives != 0;
     h->mixed = h->P.mixed != 0;
@@ -2914,6 +3020,26 @@ extern "C" fsim_status fsim_create(const fsim_config *cfg, const fsim_particles 
         const double margin = (double)h->der.interval[2] / R - 1.0;
         h->check_z = !(margin > 8e-7 * h->der.cell_number[2] + 1e-4);
     }
+    *out = h;
+    return FSIM_OK;
+}
+} // namespace
+
+extern "C" fsim_status fsim_create(const fsim_config *cfg, const fsim_particles *p, int device, fsim_handle *out)
+{
+    if (!cfg || !p || !out) return FSIM_EINVAL;
+    *out = nullptr;
+    if (p->n_fluid < 0 || p->n_solid < 0 || p->n_virt < 0 || (p->n_fluid && (!p->fluid_pos || !p->fluid_vel ||
+                                                                             !p->fluid_rho || !p->fluid_p)) ||
+        (p->n_solid && (!p->solid_pos || !p->solid_vel || !p->solid_ref_pos || !p->solid_type)) ||
+        (p->n_virt && !p->virt_pos)) {
+        fsim_set_error("invalid particle arrays");
+        return FSIM_EINVAL;
+    }
+    fsim_sim *h = nullptr;
+    fsim_status st = new_handle(cfg, p->n_fluid, p->n_solid, p->n_virt, device, &h);
+    if (st) return st;
+    DeviceGuard guard(h->device);
     st = create_impl(h, p);
     if (st) {
         free_all(h);
@@ -3174,6 +3300,45 @@ extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src,
     return FSIM_OK;
 }
 
+extern "C" fsim_status fsim_probe(fsim_handle h, const float *points, int n, float *out)
+{
+    if (!h || n < 0 || (n && (!points || !out))) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
+    if (!h->f_sorted || !h->s_sorted) {
+        fsim_set_error("run FSIM_PHASE_CELL (or a step) first");
+        return FSIM_EINVAL;
+    }
+    if (!n) return FSIM_OK;
+    DeviceGuard guard(h->device);
+    float *d = nullptr;
+    CK(cudaMalloc((void **)&d, sizeof(float) * 8 * (size_t)n));
+    ProbeArgs A;
+    A.pts = d;
+    A.n = n;
+    A.out = d + 3 * (size_t)n;
+    A.fposr = h->f_posr[h->f_cur];
+    A.fvelp = h->f_velp[h->f_cur];
+    A.start_f = h->f_start;
+    A.s_pos = h->s_pos[h->s_cur];
+    A.s_vel = h->s_vel[h->s_cur];
+    A.s_np = h->s_np;
+    A.start_s = h->s_start;
+    cudaError_t e = cudaMemcpyAsync(d, points, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        k_probe<<<blocks_for(32ll * n, kBlock), kBlock, 0, h->stream>>>(h->P, A);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, A.out, sizeof(float) * 5 * n, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        fsim_set_error("probe failed: %s", cudaGetErrorString(e));
+        return FSIM_ECUDA;
+    }
+    return FSIM_OK;
+}
+
 extern "C" fsim_status fsim_neighbor_counts(fsim_handle h, int *out, size_t bytes)
 {
     if (!h || (!out && bytes)) return FSIM_EINVAL;
@@ -3231,7 +3396,8 @@ extern "C" fsim_status fsim_get_cells(fsim_handle h, int species, int *cell_star
     return FSIM_OK;
 }
 
-extern "C" fsim_status fsim_write_vtk(fsim_handle h, const char *out_dir, int file_step)
+namespace {
+fsim_status write_vtk(fsim_handle h, const char *out_dir, int file_step, bool binary)
 {
     if (!h || !out_dir) return FSIM_EINVAL;
     std::vector<float> fpos(3 * (size_t)h->nf), fvel(3 * (size_t)h->nf), frho(h->nf), fp(h->nf);
@@ -3269,7 +3435,18 @@ extern "C" fsim_status fsim_write_vtk(fsim_handle h, const char *out_dir, int fi
     vs.vpos = vpos.data();
     vs.vnormal = vnormal.data();
     vs.vp = vp.data();
-    return fsim_write_vtk_host(out_dir, file_step, vs);
+    return fsim_write_vtk_host(out_dir, file_step, vs, binary);
+}
+} // namespace
+
+extern "C" fsim_status fsim_write_vtk(fsim_handle h, const char *out_dir, int file_step)
+{
+    return write_vtk(h, out_dir, file_step, false);
+}
+
+extern "C" fsim_status fsim_write_vtk_binary(fsim_handle h, const char *out_dir, int file_step)
+{
+    return write_vtk(h, out_dir, file_step, true);
 }
 
 extern "C" fsim_status fsim_time_steps(fsim_handle h, int nsteps, float *ms)
@@ -3373,6 +3550,212 @@ extern "C" fsim_status fsim_conservation(fsim_handle h, double *out, int n_out)
     for (int k = 0; k < n_out && k < FSIM_CONSERVATION_N; ++k) out[k] = tot[k];
     for (int k = FSIM_CONSERVATION_N; k < n_out; ++k) out[k] = 0.0;
     return FSIM_OK;
+}
+
+// =================================================================== snapshots
+// Binary snapshot of an instance: a fixed header, then the device arrays that
+// define the state in their current (cell-sorted) order, so that an instance
+// restored from it continues bit for bit like the original.  Per-step products
+// (cell starts, solid stress, derivatives) are recomputed by the next step.
+namespace {
+struct SnapHeader {
+    char magic[8];
+    uint32_t version, config_bytes;
+    int64_t step;
+    int32_t n_fluid, n_solid, n_virt, ncell;
+    uint64_t payload_bytes;
+    fsim_config cfg;
+};
+constexpr char kSnapMagic[8] = {'F', 'S', 'I', 'M', 'S', 'N', 'P', '1'};
+constexpr size_t kSnapHeaderBytes = 512; // header padded; arrays start 16-byte aligned
+static_assert(sizeof(SnapHeader) <= kSnapHeaderBytes, "snapshot header");
+
+struct SnapArray {
+    void *dev;
+    size_t bytes;
+};
+std::vector<SnapArray> snap_arrays(fsim_sim *h, int pf, int ps)
+{
+    const size_t nf = h->nf, ns = h->ns, nv = h->nv, nc = h->ncell;
+    return {{h->f_posr[pf], 16 * nf}, {h->f_velp[pf], 16 * nf}, {h->f_orig[pf], 4 * nf},   {h->f_cell, 4 * nf},
+            {h->s_pos[ps], 16 * ns},  {h->s_vel[ps], 16 * ns},  {h->s_ref[ps], 16 * ns},   {h->s_type[ps], 4 * ns},
+            {h->s_orig[ps], 4 * ns},  {h->v_posr, 16 * nv},     {h->v_velp, 16 * nv},      {h->v_normal, 16 * nv},
+            {h->v_orig, 4 * nv},      {h->v_cell, 4 * nv},      {h->v_start, 4 * (nc + 1)}};
+}
+size_t snap_payload(fsim_sim *h)
+{
+    size_t b = 0;
+    for (const SnapArray &a : snap_arrays(h, 0, 0)) b += (a.bytes + 15) & ~size_t(15);
+    return b;
+}
+} // namespace
+
+extern "C" fsim_status fsim_snapshot_bytes(fsim_handle h, size_t *bytes)
+{
+    if (!h || !bytes) return FSIM_EINVAL;
+    *bytes = kSnapHeaderBytes + snap_payload(h);
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_snapshot_save(fsim_handle h, long long step, void *buf, size_t bytes)
+{
+    if (!h || !buf) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
+    const size_t need = kSnapHeaderBytes + snap_payload(h);
+    if (bytes != need) {
+        fsim_set_error("a snapshot of this instance takes %zu bytes, got %zu", need, bytes);
+        return FSIM_EINVAL;
+    }
+    DeviceGuard guard(h->device);
+    SnapHeader hd;
+    std::memset(&hd, 0, sizeof hd);
+    std::memcpy(hd.magic, kSnapMagic, 8);
+    hd.version = 1;
+    hd.config_bytes = sizeof(fsim_config);
+    hd.step = step;
+    hd.n_fluid = h->nf;
+    hd.n_solid = h->ns;
+    hd.n_virt = h->nv;
+    hd.ncell = h->ncell;
+    hd.payload_bytes = need - kSnapHeaderBytes;
+    hd.cfg = h->cfg;
+    char *out = static_cast<char *>(buf);
+    std::memset(out, 0, kSnapHeaderBytes);
+    std::memcpy(out, &hd, sizeof hd);
+    size_t off = kSnapHeaderBytes;
+    for (const SnapArray &a : snap_arrays(h, h->f_cur, h->s_cur)) {
+        if (a.bytes) CK(cudaMemcpyAsync(out + off, a.dev, a.bytes, cudaMemcpyDeviceToHost, h->stream));
+        const size_t padded = (a.bytes + 15) & ~size_t(15);
+        if (padded > a.bytes) std::memset(out + off + a.bytes, 0, padded - a.bytes);
+        off += padded;
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_snapshot_load(const void *buf, size_t bytes, int device, fsim_handle *out,
+                                          long long *step)
+{
+    if (!buf || !out) return FSIM_EINVAL;
+    *out = nullptr;
+    SnapHeader hd;
+    if (bytes < kSnapHeaderBytes) {
+        fsim_set_error("snapshot too short");
+        return FSIM_EIO;
+    }
+    std::memcpy(&hd, buf, sizeof hd);
+    if (std::memcmp(hd.magic, kSnapMagic, 8) || hd.version != 1 || hd.config_bytes != sizeof(fsim_config) ||
+        hd.n_fluid < 0 || hd.n_solid < 0 || hd.n_virt < 0) {
+        fsim_set_error("not a version-1 fluidsim snapshot");
+        return FSIM_EIO;
+    }
+    fsim_sim *h = nullptr;
+    fsim_status st = new_handle(&hd.cfg, hd.n_fluid, hd.n_solid, hd.n_virt, device, &h);
+    if (st) return st;
+    if (h->ncell != hd.ncell || bytes != kSnapHeaderBytes + snap_payload(h) ||
+        hd.payload_bytes != bytes - kSnapHeaderBytes) {
+        fsim_set_error("snapshot size does not match its header");
+        delete h;
+        return FSIM_EIO;
+    }
+    DeviceGuard guard(h->device);
+    if ((st = alloc_state(h))) {
+        free_all(h);
+        delete h;
+        return st;
+    }
+    const char *in = static_cast<const char *>(buf);
+    size_t off = kSnapHeaderBytes;
+    const int ns = h->ns;
+    std::vector<float> ref(3 * (size_t)ns);
+    const char *ref_src = nullptr, *orig_src = nullptr;
+    cudaError_t e = cudaSuccess;
+    for (const SnapArray &a : snap_arrays(h, 0, 0)) {
+        if (a.bytes && e == cudaSuccess) e = cudaMemcpy(a.dev, in + off, a.bytes, cudaMemcpyHostToDevice);
+        if (a.dev == h->s_ref[0]) ref_src = in + off;
+        if (a.dev == h->s_orig[0]) orig_src = in + off;
+        off += (a.bytes + 15) & ~size_t(15);
+    }
+    if (e != cudaSuccess) {
+        fsim_set_error("snapshot upload failed: %s", cudaGetErrorString(e));
+        free_all(h);
+        delete h;
+        return FSIM_ECUDA;
+    }
+    // solid: F = L = I, P = 0 until the next solid phase; static neighbour lists
+    // from the reference positions in input order
+    if (ns) {
+        for (int k = 0; k < ns; ++k) {
+            int o;
+            float r[4];
+            std::memcpy(&o, orig_src + 4 * (size_t)k, 4);
+            std::memcpy(r, ref_src + 16 * (size_t)k, 16);
+            if (o < 0 || o >= ns) {
+                fsim_set_error("corrupt snapshot (solid ids)");
+                free_all(h);
+                delete h;
+                return FSIM_EIO;
+            }
+            std::memcpy(&ref[3 * (size_t)o], r, 12);
+        }
+        std::vector<float> eye(9 * (size_t)ns, 0.0f);
+        for (int i = 0; i < ns; ++i) eye[9 * i] = eye[9 * i + 4] = eye[9 * i + 8] = 1.0f;
+        e = cudaMemcpy(h->s_F, eye.data(), sizeof(float) * 9 * ns, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(h->s_L, eye.data(), sizeof(float) * 9 * ns, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemset(h->s_P, 0, sizeof(float) * 9 * ns);
+        if (e == cudaSuccess) e = cudaMemset(h->s_dudt, 0, sizeof(float4) * ns);
+        if (e == cudaSuccess) e = cudaMemset(h->s_couple, 0, sizeof(float4) * ns);
+        if (e != cudaSuccess || (st = build_solid_neighbors(h, ref.data()))) {
+            if (!st) fsim_set_error("snapshot restore failed: %s", cudaGetErrorString(e));
+            free_all(h);
+            delete h;
+            return st ? st : FSIM_ECUDA;
+        }
+    }
+    cudaStreamSynchronize(h->stream);
+    h->f_cur = h->s_cur = 0;
+    h->f_sorted = h->s_sorted = false;
+    h->f_deriv_ok = h->s_np_ok = h->s_mech_ok = false;
+    if (step) *step = hd.step;
+    *out = h;
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_snapshot_write(fsim_handle h, long long step, const char *path)
+{
+    if (!h || !path) return FSIM_EINVAL;
+    size_t n = 0;
+    fsim_status st = fsim_snapshot_bytes(h, &n);
+    if (st) return st;
+    std::vector<char> buf(n);
+    if ((st = fsim_snapshot_save(h, step, buf.data(), n))) return st;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) {
+        fsim_set_error("cannot open %s for writing", path);
+        return FSIM_EIO;
+    }
+    const bool ok = std::fwrite(buf.data(), 1, n, f) == n;
+    if (std::fclose(f) != 0 || !ok) {
+        fsim_set_error("writing %s failed", path);
+        return FSIM_EIO;
+    }
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_snapshot_read(const char *path, int device, fsim_handle *out, long long *step)
+{
+    if (!path || !out) return FSIM_EINVAL;
+    FILE *f = std::fopen(path, "rb");
+    if (!f) {
+        fsim_set_error("cannot open %s", path);
+        return FSIM_EIO;
+    }
+    std::vector<char> buf;
+    char chunk[1 << 16];
+    size_t got;
+    while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+    std::fclose(f);
+    return fsim_snapshot_load(buf.data(), buf.size(), device, out, step);
 }
 
 extern "C" fsim_status fsim_counts(fsim_handle h, int *nf, int *ns, int *nv)

@@ -237,6 +237,10 @@ fsim_status fsim_get_cells(fsim_handle h, int species, int *cell_start, size_t s
  * color field (src/output.cu:75); real fluid pressure goes to the extra file
  * fluid/fluid_true_pressure-k.vtk. */
 fsim_status fsim_write_vtk(fsim_handle h, const char *out_dir, int file_step);
+/* The same files with BINARY legacy-VTK encoding (big-endian FP32): exact
+ * values and no text formatting, for fast snapshots of large instances.  No
+ * counterpart in the reference (its writer is ASCII only). */
+fsim_status fsim_write_vtk_binary(fsim_handle h, const char *out_dir, int file_step);
 
 /* Device timing: run nsteps (CUDA-graph replays) on the handle's stream
  * bracketed by CUDA events recorded on that stream; *ms = elapsed device time. */
@@ -333,6 +337,31 @@ fsim_status fsim_cell_sort_noalloc(const fsim_derived *grid, const float *d_pos,
 /* Device memory an instance of this configuration and these particle
  * counts allocates (an upper estimate, for admission control). */
 fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, int n_solid, int n_virt, size_t *out);
+
+/* Point probes.  Replaces Probe::getData (src/probe.cu and include/probe.h:8-35
+ * of the reference, a 2D helper left commented out there), in 3D: at each of
+ * n points (3 floats each, host memory) the Shepard average, with the weight
+ * (exp(-r^2/h^2) - c1) c2 of solidPressureCalculate, of fluid velocity,
+ * pressure and density and of solid velocity and pressure (solid density 0)
+ * over the particles within the impact distance in the 27 cells of the point's
+ * cell (cell lists of the last cell phase, current positions).  out receives 5
+ * floats per point: u, v, w, p, rho; (0, 0, 0, 0, rho0) where no particle is
+ * in range or the point is outside the grid. */
+fsim_status fsim_probe(fsim_handle h, const float *points, int n, float *out);
+
+/* Binary snapshots (checkpoint / resume; no counterpart in the reference,
+ * whose only restartable state is its .dat input).  A snapshot holds the
+ * configuration, a caller-chosen step number and the particle state in its
+ * current cell-sorted order, so that an instance restored from it continues
+ * bit for bit like the original.  Per-step products (cell starts, solid
+ * stress, derivatives) are recomputed by the next step.  The format is this
+ * library's own: fixed header ("FSIMSNP1", version 1, counts, fsim_config),
+ * then raw device arrays, native byte order. */
+fsim_status fsim_snapshot_bytes(fsim_handle h, size_t *bytes);
+fsim_status fsim_snapshot_save(fsim_handle h, long long step, void *buf, size_t bytes);
+fsim_status fsim_snapshot_load(const void *buf, size_t bytes, int device, fsim_handle *out, long long *step);
+fsim_status fsim_snapshot_write(fsim_handle h, long long step, const char *path);
+fsim_status fsim_snapshot_read(const char *path, int device, fsim_handle *out, long long *step);
 
 /* Sizes of the instance. */
 fsim_status fsim_counts(fsim_handle h, int *n_fluid, int *n_solid, int *n_virt);

@@ -818,3 +818,66 @@ void orc_neighbor_counts(orc_sim *s, int *out)
         out[3 * i + 2] = cnt[2];
     }
 }
+
+/* Probe::getData (src/probe.cu, commented out in the reference, 2D), restated
+ * in 3D: the Shepard average, with the weight (exp(-r^2/h^2) - c1) c2 of
+ * solidPressureCalculate, of fluid velocity, pressure and density and of
+ * solid velocity and pressure (solid density counts 0) over the particles
+ * within the impact distance in the 27 cells of the probe's cell (cell lists
+ * of the last cell phase, current positions); velocity 0, pressure 0 and
+ * density rho0 when no particle is in range or the probe is outside the
+ * grid.  out: 5 doubles per probe (u, v, w, p, rho). */
+void orc_probe(orc_sim *s, int n, const double *pts, double *out)
+{
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int k = 0; k < n; k++) {
+        const v3 xi = v3make((real)pts[3 * k], (real)pts[3 * k + 1], (real)pts[3 * k + 2]);
+        real wsum = 0, p = 0, rho = 0;
+        v3 u = v3make(0, 0, 0);
+        int c[3], inside = 1;
+        const float xf[3] = {(float)pts[3 * k], (float)pts[3 * k + 1], (float)pts[3 * k + 2]};
+        for (int a = 0; a < 3; a++) {
+            c[a] = (int)((xf[a] - s->d.cell_min[a]) * s->d.interval_inv[a]);
+            if (c[a] < 0 || c[a] >= s->d.cell_number[a]) inside = 0;
+        }
+        if (inside) {
+            int nb[27];
+            const int cell = (c[0] * s->d.cell_number[1] + c[1]) * s->d.cell_number[2] + c[2];
+            const int nn = neighbor_cells(&s->d, cell, nb);
+            for (int q = 0; q < nn; q++) {
+                for (int m = s->cf.start[nb[q]]; m < s->cf.start[nb[q] + 1]; m++) {
+                    const int j = s->cf.list[m];
+                    const real r2 = dist2(xi, s->fpos[j]);
+                    if (r2 < s->R2) {
+                        const real w = (R_EXP(-r2 * s->h_inv2) - s->kc1) * s->kc2;
+                        wsum += w;
+                        u = vadd(u, vscale(s->fvel[j], w));
+                        p += s->fp[j] * w;
+                        rho += s->frho[j] * w;
+                    }
+                }
+                for (int m = s->cs.start[nb[q]]; m < s->cs.start[nb[q] + 1]; m++) {
+                    const int j = s->cs.list[m];
+                    const real r2 = dist2(xi, s->spos[j]);
+                    if (r2 < s->R2) {
+                        const real w = (R_EXP(-r2 * s->h_inv2) - s->kc1) * s->kc2;
+                        wsum += w;
+                        u = vadd(u, vscale(s->svel[j], w));
+                        p += s->sp[j] * w;
+                    }
+                }
+            }
+        }
+        double *o = out + 5 * (size_t)k;
+        if (wsum != 0) {
+            o[0] = u.x / wsum;
+            o[1] = u.y / wsum;
+            o[2] = u.z / wsum;
+            o[3] = p / wsum;
+            o[4] = rho / wsum;
+        } else {
+            o[0] = o[1] = o[2] = o[3] = 0;
+            o[4] = s->rho0;
+        }
+    }
+}

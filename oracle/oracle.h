@@ -77,6 +77,8 @@ int  orc_get(orc_sim *s, int field, double *out);
 int  orc_set(orc_sim *s, int field, const double *in);
 /* 3 ints per fluid particle: in-range fluid, solid, virtual neighbours (FP32 distance test) */
 void orc_neighbor_counts(orc_sim *s, int *out);
+/* probe sampling: n points (3 doubles each) -> 5 doubles each (u, v, w, p, rho) */
+void orc_probe(orc_sim *s, int n, const double *pts, double *out);
 void orc_set_threads(int n);
 int  orc_real_bytes(void);
 

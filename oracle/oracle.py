@@ -50,6 +50,7 @@ def load(precision="f64"):
     lib.orc_set.argtypes = [V, I, P]
     lib.orc_set.restype = I
     lib.orc_neighbor_counts.argtypes = [V, P]
+    lib.orc_probe.argtypes = [V, I, P, P]
     lib.orc_set_threads.argtypes = [I]
     lib.orc_real_bytes.restype = I
     _libs[precision] = lib
@@ -118,6 +119,14 @@ class OracleSim:
         a = np.ascontiguousarray(values, dtype=np.float64)
         if self.lib.orc_set(self.s, FIELD_IDS[name], a.ctypes.data):
             raise ValueError("field %s not settable" % name)
+
+    def probe(self, points):
+        """(n, 5) array: Shepard-averaged u, v, w, p, rho at each point."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        out = np.empty((len(pts), 5), np.float64)
+        if len(pts):
+            self.lib.orc_probe(self.s, len(pts), pts.ctypes.data, out.ctypes.data)
+        return out
 
     def neighbor_counts(self):
         out = np.empty((self.n["fluid"], 3), np.int32)

@@ -73,3 +73,13 @@ def test_derive_rejects_degenerate_kernel():
     cfg = api.default_config()
     with pytest.raises(api.FsimError):
         api.derive(cfg)  # smoothing_length = 0
+
+
+def test_snapshot_header_is_checked_before_any_device_work():
+    """Garbage and short inputs are rejected as FSIM_EIO without a GPU."""
+    lib = api.load()
+    h, step = C.c_void_p(), C.c_longlong()
+    for data in (b"", b"FSIMSNP1", b"x" * 4096):
+        buf = C.create_string_buffer(data, len(data) or 1)
+        assert lib.fsim_snapshot_load(buf, len(data), 0, C.byref(h), C.byref(step)) == api.EIO
+        assert not h.value

@@ -140,3 +140,42 @@ def test_unsorted_fields_rejected_until_phase_runs():
         assert np.isfinite(sim.get("solid_normal")).all()
         with pytest.raises(api.FsimError):
             sim.get("fluid_drho_dt")  # keep_derivatives is off
+
+
+def _read_binary_vtk(path):
+    """Parse a BINARY legacy-VTK polydata file with one point-data array."""
+    data = path.read_bytes()
+    head_end = data.index(b"float\n", data.index(b"POINTS")) + len(b"float\n")
+    header = data[:head_end].decode()
+    assert header.split("\n")[2] == "BINARY"
+    n = int(header.split("POINTS ")[1].split()[0])
+    pts = np.frombuffer(data, ">f4", 3 * n, head_end).reshape(n, 3)
+    rest = data[head_end + 12 * n + 1:]
+    line_end = rest.index(b"\n", rest.index(b"\n") + 1) + 1  # POINT_DATA + VECTORS/SCALARS lines
+    kind = rest[:line_end].decode()
+    if "LOOKUP_TABLE" in rest[line_end:line_end + 30].decode(errors="ignore"):
+        line_end = rest.index(b"\n", line_end) + 1
+        return pts, np.frombuffer(rest, ">f4", n, line_end), kind
+    return pts, np.frombuffer(rest, ">f4", 3 * n, line_end).reshape(n, 3), kind
+
+
+def test_binary_vtk_holds_exact_fields(tmp_path):
+    cfg, pa = cases.make(cases.tiny_box(jitter=0.01, seed=8))
+    with api.Simulation(cfg, pa, device=0) as sim:
+        sim.step(2)
+        sim.sync()
+        sim.write_vtk(str(tmp_path), 3, binary=True)
+        pos, vel, rho, p = (sim.get(f) for f in ("fluid_pos", "fluid_vel", "fluid_rho", "fluid_p"))
+        spos = sim.get("solid_pos")
+    d = tmp_path / "fluid"
+    x, v, kind = _read_binary_vtk(d / "fluid_velocity-3.vtk")
+    assert "VECTORS velocity float" in kind
+    assert np.array_equal(x, pos) and np.array_equal(v, vel)
+    x, r, kind = _read_binary_vtk(d / "fluid_density-3.vtk")
+    assert "SCALARS density float 1" in kind and np.array_equal(r, rho)
+    _, tp, _ = _read_binary_vtk(d / "fluid_true_pressure-3.vtk")
+    assert np.array_equal(tp, p)
+    _, zero, _ = _read_binary_vtk(d / "fluid_pressure-3.vtk")
+    assert not zero.any()
+    xs, _, _ = _read_binary_vtk(tmp_path / "solid" / "solid_velocity-3.vtk")
+    assert np.array_equal(xs, spos)

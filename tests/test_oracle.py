@@ -95,3 +95,19 @@ def test_oracle_deterministic_across_threads():
         outs.append(o.get("fluid_pos"))
     orc.load("f64").orc_set_threads(os.cpu_count() or 1)
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_oracle_probe_defaults_and_rest_state():
+    """At rest every velocity is 0; a point with no particle in range or
+    outside the grid reads (0, 0, 0, 0, rho0); inside the column the Shepard
+    density lies between the smallest and largest particle density."""
+    cfg, pa = cases.make(cases.tiny_box())
+    s = orc.OracleSim(cfg, pa, "f64")
+    s.phase(0)
+    lo, hi = pa.fluid_pos.min(0), pa.fluid_pos.max(0)
+    pts = np.vstack([(lo + hi) / 2, [0.2, 0.14, 0.14], [-3.0, 0.0, 0.0]])
+    out = s.probe(pts)
+    assert np.all(out[:, :3] == 0)
+    assert np.array_equal(out[2], [0, 0, 0, 0, cfg.fluid_density])
+    assert pa.fluid_rho.min() <= out[0, 4] <= pa.fluid_rho.max()
+    assert out[0, 3] > 0
