@@ -148,6 +148,7 @@ def load():
         "fsim_snapshot_bytes": (C.c_int, [P, C.POINTER(C.c_size_t)]),
         "fsim_probe": (C.c_int, [P, P, C.c_int, P]),
         "fsim_write_vtk_binary": (C.c_int, [P, C.c_char_p, C.c_int]),
+        "fsim_batch_sync_members": (C.c_int, [P, P, C.c_int]),
         "fsim_snapshot_save": (C.c_int, [P, C.c_longlong, P, C.c_size_t]),
         "fsim_snapshot_load": (C.c_int, [P, C.c_size_t, C.c_int, C.POINTER(P), C.POINTER(C.c_longlong)]),
         "fsim_snapshot_write": (C.c_int, [P, C.c_longlong, C.c_char_p]),
@@ -185,7 +186,7 @@ EXPORTED = [
     "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes", "fsim_conservation",
     "fsim_measure_fp32_peak", "fsim_sweep_tuning", "fsim_batch_sweep_tuning", "fsim_snapshot_bytes",
     "fsim_snapshot_save", "fsim_snapshot_load", "fsim_snapshot_write", "fsim_snapshot_read", "fsim_probe",
-    "fsim_write_vtk_binary",
+    "fsim_write_vtk_binary", "fsim_batch_sync_members",
 ]
 SWEEP_SHAPES = ((4, 48), (4, 32), (8, 32))  # (warps per block, list capacity) per shape index
 
@@ -540,6 +541,13 @@ class Batch:
         n = C.c_int()
         check(self.lib.fsim_batch_launches_per_step(self.b, C.byref(n)))
         return n.value
+
+    def sync_members(self):
+        """Wait for the batch; the status code of every member (OK, or ENUMERIC
+        for a member whose particles left the grid)."""
+        st = np.empty(len(self.sims), np.int32)
+        check(self.lib.fsim_batch_sync_members(self.b, st.ctypes.data, len(st)))
+        return [int(x) for x in st]
 
     def sweep_tuning(self):
         """(chosen shape or -1, [ms per shape]) of the batch's sweep autotuner."""

@@ -3938,6 +3938,15 @@ extern "C" fsim_status fsim_batch_sync(fsim_batch_t b)
     return batch_check_flags(b);
 }
 
+extern "C" fsim_status fsim_batch_sync_members(fsim_batch_t b, int *status, int n)
+{
+    if (!b || !status || n != (int)b->members.size()) return FSIM_EINVAL;
+    DeviceGuard guard(b->device);
+    CK(cudaStreamSynchronize(b->stream));
+    for (int k = 0; k < n; ++k) status[k] = check_flags(b->members[k]);
+    return FSIM_OK;
+}
+
 extern "C" fsim_status fsim_batch_time_steps(fsim_batch_t b, int nsteps, float *ms)
 {
     if (!b || nsteps < 0 || !ms) return FSIM_EINVAL;

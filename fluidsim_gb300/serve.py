@@ -32,6 +32,7 @@ class Request:
     done_at: float = float("nan")
     result: dict = field(default_factory=dict)
     data: object = None      # (config, particles) when generated ahead of the stream
+    error: str = ""          # set when the request failed or was cancelled
 
 
 def poisson_stream(n, rate, seed=7, fluid_range=(10_000, 1_000_000), solid_range=(1_000, 27_000),
@@ -97,6 +98,10 @@ class GpuBackend:
     def result(self, inst):
         return _result_fields(inst)
 
+    def member_status(self, batch):
+        """Per-member status codes after the batch's last step (waits for it)."""
+        return batch.sync_members()
+
     def destroy(self, inst):
         inst.close()
 
@@ -114,7 +119,14 @@ class Server:
 
     The work budget bounds the batch at about what saturates the GPU: beyond
     that, admitting more only slows every running request down (they share the
-    GPU), raising latency without raising throughput."""
+    GPU), raising latency without raising throughput.
+
+    Failures stay per request: a request whose instance cannot be created
+    (e.g. out of device memory) fails at admission; a member whose own error
+    flag is set (its particles left the cell grid) is evicted at the next
+    quantum boundary while the others continue; cancel(rid) drops a waiting
+    request or evicts a running one.  Failed and cancelled requests carry
+    `error` and count in the summary's "failed"."""
 
     def __init__(self, budget_bytes, backend=None, quantum=10, keep_results=False, max_particles=None):
         self.budget = budget_bytes
@@ -123,78 +135,113 @@ class Server:
         self.quantum = quantum
         self.keep_results = keep_results
         self.log = []  # (event, request id, time)
+        self._cancel = set()
+
+    def cancel(self, rid):
+        """Cancel request `rid` (takes effect at the next loop turn)."""
+        self._cancel.add(rid)
 
     def run(self, requests, clock=time.perf_counter, sleep=time.sleep):
         be = self.backend
         reqs = sorted(requests, key=lambda r: r.arrival)
         waiting, active = [], []  # active entries: [request, instance, steps left, bytes]
         prepared = {}
-        nxt, used, batch = 0, 0, None
-        load = 0  # particles of the admitted requests
+        st = {"nxt": 0, "used": 0, "load": 0, "completed": 0, "failed": 0, "work": 0, "rebuilds": 0}
+        batch = None
         t0 = clock()
-        completed, work, rebuilds = 0, 0, 0
-        while completed < len(reqs):
+
+        def close_request(r, now, event, error=""):
+            r.done_at, r.error = now, error
+            st["completed"] += 1
+            st["failed"] += bool(error)
+            self.log.append((event, r.rid, now))
+
+        def retire(a, now, error=""):
+            if self.keep_results and not error:
+                a[0].result = be.result(a[1])
+            be.destroy(a[1])
+            st["used"] -= a[3]
+            st["load"] -= a[0].particles
+            close_request(a[0], now, "failed" if error else "done", error)
+
+        while st["completed"] < len(reqs):
             now = clock() - t0
-            while nxt < len(reqs) and reqs[nxt].arrival <= now:
-                waiting.append(reqs[nxt])
-                nxt += 1
+            while st["nxt"] < len(reqs) and reqs[st["nxt"]].arrival <= now:
+                waiting.append(reqs[st["nxt"]])
+                st["nxt"] += 1
             changed = False
+            if self._cancel:
+                for r in [r for r in waiting if r.rid in self._cancel]:
+                    waiting.remove(r)
+                    prepared.pop(r.rid, None)
+                    close_request(r, now, "cancelled", "cancelled")
+                for a in [a for a in active if a[0].rid in self._cancel]:
+                    active.remove(a)
+                    retire(a, now, "cancelled")
+                    changed = True
             while waiting:
                 r = waiting[0]
                 if r.rid not in prepared:
                     prepared[r.rid] = be.prepare(r)
                 data, need, npart = prepared[r.rid]
-                if active and used + need > self.budget:
+                if active and st["used"] + need > self.budget:
                     break
-                if active and self.max_particles is not None and load + npart > self.max_particles:
+                if active and self.max_particles is not None and st["load"] + npart > self.max_particles:
                     break
                 waiting.pop(0)
                 del prepared[r.rid]
                 r.particles = npart
-                active.append([r, be.create(data), r.steps, need])
-                used += need
-                load += npart
+                try:
+                    inst = be.create(data)
+                except Exception as exc:  # this request fails; the others go on
+                    close_request(r, clock() - t0, "failed", "admission failed: %s" % exc)
+                    continue
+                active.append([r, inst, r.steps, need])
+                st["used"] += need
+                st["load"] += npart
                 changed = True
                 self.log.append(("admit", r.rid, clock() - t0))
             if not active:
-                if nxt < len(reqs):
-                    sleep(max(0.0, min(0.05, reqs[nxt].arrival - (clock() - t0))))
+                if batch is not None:
+                    batch.close()
+                    batch = None
+                if st["nxt"] < len(reqs):
+                    sleep(max(0.0, min(0.05, reqs[st["nxt"]].arrival - (clock() - t0))))
                 continue
             if changed or batch is None:
                 if batch is not None:
                     batch.close()
                 batch = be.batch([a[1] for a in active])
-                rebuilds += 1
+                st["rebuilds"] += 1
             k = min(self.quantum, min(a[2] for a in active))
             batch.step(k)
-            batch.sync()
+            status = be.member_status(batch)
             now = clock() - t0
-            finished = []
-            for a in active:
+            finished, broken = [], []
+            for a, code in zip(active, status):
+                if code:
+                    broken.append((a, code))
+                    continue
                 a[2] -= k
-                work += a[0].particles * k
+                st["work"] += a[0].particles * k
                 if a[2] == 0:
-                    a[0].done_at = now
                     finished.append(a)
-            if finished:
+            if finished or broken:
                 batch.close()
                 batch = None
                 for a in finished:
-                    if self.keep_results:
-                        a[0].result = be.result(a[1])
-                    be.destroy(a[1])
-                    used -= a[3]
-                    load -= a[0].particles
-                    completed += 1
-                    self.log.append(("done", a[0].rid, now))
-                active = [a for a in active if a[2] > 0]
+                    retire(a, now)
+                for a, code in broken:
+                    retire(a, now, "instance error %d" % code)
+                gone = {id(a) for a in finished} | {id(a) for a, _ in broken}
+                active = [a for a in active if id(a) not in gone]
         if batch is not None:
             batch.close()
         makespan = clock() - t0
-        lat = [r.done_at - r.arrival for r in reqs]
-        return {"requests": len(reqs), "makespan_s": makespan, "particle_updates": work,
-                "throughput": work / makespan, "p50_latency_s": _percentile(lat, 50),
-                "p99_latency_s": _percentile(lat, 99), "batch_rebuilds": rebuilds}
+        lat = [r.done_at - r.arrival for r in reqs if not r.error]
+        return {"requests": len(reqs), "makespan_s": makespan, "particle_updates": st["work"],
+                "throughput": st["work"] / makespan, "p50_latency_s": _percentile(lat, 50),
+                "p99_latency_s": _percentile(lat, 99), "batch_rebuilds": st["rebuilds"], "failed": st["failed"]}
 
 
 def serve_one_by_one(requests, device=0, clock=time.perf_counter, keep_results=False):

@@ -299,6 +299,10 @@ fsim_status fsim_batch_create(fsim_handle *members, int n, fsim_batch_t *out);
 /* Enqueue nsteps batched steps on the batch's stream. */
 fsim_status fsim_batch_step(fsim_batch_t b, int nsteps);
 fsim_status fsim_batch_sync(fsim_batch_t b);
+/* Wait for the batch and report every member's own status (FSIM_ENUMERIC for
+ * a member whose particles left the cell grid, FSIM_OK otherwise), so that a
+ * caller can evict only the failing instances; n = number of members. */
+fsim_status fsim_batch_sync_members(fsim_batch_t b, int *status, int n);
 /* Device time of nsteps batched steps (CUDA events on the batch's stream). */
 fsim_status fsim_batch_time_steps(fsim_batch_t b, int nsteps, float *ms);
 /* Kernel launches of one batched step. */

@@ -88,3 +88,20 @@ def test_batch_after_phase_calls_normalises_parity():
         assert np.array_equal(ref.get(f), s.get(f)), f
     ref.close()
     s.close()
+
+
+def test_member_status_is_per_instance():
+    """A member whose particle leaves the cell grid (moved far outside: the
+    cell hash clamps it and sets that instance's flag) reports ENUMERIC; the
+    other members report OK."""
+    sims = [api.Simulation(cfg, pa, device=0) for cfg, pa in _members()]
+    x = sims[1].get("fluid_pos")
+    x[0] = [50.0, 50.0, 50.0]
+    sims[1].set("fluid_pos", x)
+    with api.Batch(sims) as b:
+        b.step(1)
+        assert b.sync_members() == [api.OK, api.ENUMERIC, api.OK]
+        b.step(1)
+        assert b.sync_members() == [api.OK, api.OK, api.OK]  # clamped back into the domain
+    for s in sims:
+        s.close()

@@ -32,3 +32,38 @@ def test_budget_admits_one_at_a_time():
     out = srv.run(reqs)
     assert out["requests"] == 3
     assert out["batch_rebuilds"] == 3
+
+
+def test_instance_error_evicts_only_that_request():
+    reqs = _stream()
+    bad = reqs[2].rid
+    be = serve.GpuBackend(0)
+    create = be.create
+
+    def create_flagged(prepared):
+        inst = create(prepared)
+        if prepared is flagged["data"]:
+            x = inst.get("fluid_pos")
+            x[0] = [50.0, 50.0, 50.0]
+            inst.set("fluid_pos", x)
+        return inst
+
+    flagged = {"data": None}
+    prepare = be.prepare
+
+    def prepare_mark(r):
+        out = prepare(r)
+        if r.rid == bad:
+            flagged["data"] = out[0]
+        return out
+
+    be.prepare, be.create = prepare_mark, create_flagged
+    out = serve.Server(budget_bytes=2 ** 36, backend=be, quantum=3, keep_results=True).run(reqs)
+    assert out["failed"] == 1 and reqs[2].error.startswith("instance error")
+    solo = _stream()
+    serve.serve_one_by_one(solo, keep_results=True)
+    for a, b in zip(reqs, solo):
+        if a.rid == bad:
+            continue
+        for k in a.result:
+            assert np.array_equal(a.result[k], b.result[k]), (a.rid, k)

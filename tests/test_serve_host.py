@@ -1,6 +1,8 @@
 """Host logic of the served form (CPU only): admission by memory budget,
 first-come first-served order, continuous batching at quantum boundaries,
-latency accounting.  A fake backend stands in for the GPU."""
+latency accounting, and per-request failures injected on the host (failed
+admission, an instance's error flag, cancellation).  A fake backend stands in
+for the GPU."""
 import pytest
 
 from fluidsim_gb300 import serve
@@ -18,10 +20,16 @@ class FakeClock:
 
 
 class FakeBackend:
-    """Each instance needs `mem` bytes; a batch step of k steps takes k ms."""
+    """Each instance needs `mem` bytes; a batch step of k steps takes k ms.
+    fail_create: request ids whose instance creation raises (like an allocation
+    failure); flag_after: request id -> steps after which its instance reports
+    an error status (like its particles leaving the grid)."""
 
-    def __init__(self, clock, mem):
+    def __init__(self, clock, mem, fail_create=(), flag_after=None):
         self.clock, self.mem = clock, mem
+        self.fail_create = set(fail_create)
+        self.flag_after = dict(flag_after or {})
+        self.steps_done = {}
         self.alive = set()
         self.batches = []
 
@@ -30,7 +38,10 @@ class FakeBackend:
 
     def create(self, rid):
         assert rid not in self.alive
+        if rid in self.fail_create:
+            raise RuntimeError("out of device memory")
         self.alive.add(rid)
+        self.steps_done[rid] = 0
         return rid
 
     def batch(self, instances):
@@ -38,10 +49,13 @@ class FakeBackend:
 
         class B:
             def __init__(self):
+                self.instances = list(instances)
                 backend.batches.append(tuple(instances))
 
             def step(self, k):
                 backend.clock.t += 1e-3 * k
+                for rid in instances:
+                    backend.steps_done[rid] += k
 
             def sync(self):
                 pass
@@ -53,6 +67,10 @@ class FakeBackend:
 
     def result(self, inst):
         return {"rid": inst}
+
+    def member_status(self, batch):
+        return [5 if rid in self.flag_after and self.steps_done[rid] >= self.flag_after[rid] else 0
+                for rid in batch.instances]
 
     def destroy(self, inst):
         self.alive.remove(inst)
@@ -116,3 +134,52 @@ def test_work_budget_bounds_concurrency():
     assert max(len(b) for b in be.batches) == 2
     admits = [rid for ev, rid, _ in srv.log if ev == "admit"]
     assert admits == [0, 1, 2, 3, 4]
+
+
+def test_admission_failure_fails_that_request_only():
+    clock = FakeClock()
+    be = FakeBackend(clock, mem={0: 1, 1: 1, 2: 1}, fail_create={1})
+    srv = serve.Server(budget_bytes=10, backend=be, quantum=5, keep_results=True)
+    reqs = _reqs([0, 0, 0], [10, 10, 10])
+    out = srv.run(reqs, clock=clock, sleep=clock.sleep)
+    assert out["requests"] == 3 and out["failed"] == 1 and not be.alive
+    assert reqs[1].error.startswith("admission failed") and not reqs[1].result
+    assert reqs[0].result == {"rid": 0} and reqs[2].result == {"rid": 2}
+    assert out["particle_updates"] == 1000 * 20
+
+
+def test_instance_error_evicts_only_that_member():
+    """Request 1's instance reports an error after 10 steps: it is evicted at
+    that quantum boundary; 0 and 2 finish all their steps."""
+    clock = FakeClock()
+    be = FakeBackend(clock, mem={0: 1, 1: 1, 2: 1}, flag_after={1: 10})
+    srv = serve.Server(budget_bytes=10, backend=be, quantum=5, keep_results=True)
+    reqs = _reqs([0, 0, 0], [30, 30, 30])
+    out = srv.run(reqs, clock=clock, sleep=clock.sleep)
+    assert out["failed"] == 1 and reqs[1].error == "instance error 5" and not be.alive
+    assert ("failed", 1, reqs[1].done_at) in srv.log
+    assert reqs[0].result and reqs[2].result and not reqs[0].error
+    assert out["particle_updates"] == 1000 * (30 + 5 + 30)  # 1's erroring quantum does not count
+    assert all(1 not in b for b in be.batches[-1:])
+
+
+def test_cancellation_of_waiting_and_running_requests():
+    """1 is cancelled while it waits (behind 0 for memory); 0 is cancelled
+    while it runs, after 10 of its 40 steps; 2 is unaffected."""
+    clock = FakeClock()
+    be = FakeBackend(clock, mem={0: 60, 1: 60, 2: 1})
+    srv = serve.Server(budget_bytes=100, backend=be, quantum=5, keep_results=True)
+    reqs = _reqs([0, 0, 0], [40, 10, 10])
+    srv.cancel(1)
+    status = be.member_status
+
+    def member_status(batch):
+        if be.steps_done.get(0, 0) >= 10:
+            srv.cancel(0)
+        return status(batch)
+
+    be.member_status = member_status
+    out = srv.run(reqs, clock=clock, sleep=clock.sleep)
+    assert reqs[1].error == "cancelled" and reqs[0].error == "cancelled" and out["failed"] == 2
+    assert be.steps_done[0] < 40 and 1 not in be.steps_done
+    assert reqs[2].result == {"rid": 2} and not be.alive
