@@ -149,6 +149,8 @@ def load():
         "fsim_probe": (C.c_int, [P, P, C.c_int, P]),
         "fsim_write_vtk_binary": (C.c_int, [P, C.c_char_p, C.c_int]),
         "fsim_batch_sync_members": (C.c_int, [P, P, C.c_int]),
+        "fsim_create_case": (C.c_int, [P, P, C.c_int, C.POINTER(P)]),
+        "fsim_case_counts": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "fsim_snapshot_save": (C.c_int, [P, C.c_longlong, P, C.c_size_t]),
         "fsim_snapshot_load": (C.c_int, [P, C.c_size_t, C.c_int, C.POINTER(P), C.POINTER(C.c_longlong)]),
         "fsim_snapshot_write": (C.c_int, [P, C.c_longlong, C.c_char_p]),
@@ -186,7 +188,7 @@ EXPORTED = [
     "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes", "fsim_conservation",
     "fsim_measure_fp32_peak", "fsim_sweep_tuning", "fsim_batch_sweep_tuning", "fsim_snapshot_bytes",
     "fsim_snapshot_save", "fsim_snapshot_load", "fsim_snapshot_write", "fsim_snapshot_read", "fsim_probe",
-    "fsim_write_vtk_binary", "fsim_batch_sync_members",
+    "fsim_write_vtk_binary", "fsim_batch_sync_members", "fsim_create_case", "fsim_case_counts",
 ]
 SWEEP_SHAPES = ((4, 48), (4, 32), (8, 32))  # (warps per block, list capacity) per shape index
 
@@ -232,6 +234,13 @@ def _tuning(fn, handle):
     ms = (C.c_float * len(SWEEP_SHAPES))()
     check(fn(handle, C.byref(chosen), ms, len(SWEEP_SHAPES)))
     return chosen.value, list(ms)
+
+
+def case_counts(case):
+    """(n_fluid, n_solid, n_virt) of a lattice case, without generating it."""
+    nf, ns, nv = C.c_int(), C.c_int(), C.c_int()
+    check(load().fsim_case_counts(C.byref(case), C.byref(nf), C.byref(ns), C.byref(nv)))
+    return nf.value, ns.value, nv.value
 
 
 def measure_fp32_peak(device=0):
@@ -360,6 +369,15 @@ class Simulation:
         self.lib, self.h, self.cfg, self.particles = load(), h, None, None
         self._set_counts()
         self.snapshot_step = step
+        return self
+
+    @classmethod
+    def from_case(cls, cfg, case, device=-1):
+        """Generate a lattice case on the device (fsim_create_case)."""
+        h = C.c_void_p()
+        check(load().fsim_create_case(C.byref(cfg), C.byref(case), device, C.byref(h)))
+        self = cls._from_handle(h, None)
+        self.cfg = cfg
         return self
 
     @classmethod

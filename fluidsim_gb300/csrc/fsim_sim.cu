@@ -1613,6 +1613,151 @@ FSIM_BATCHED_KERNEL(kb_solid_update, SolidArgs, solid_update_body, kBlock)
 
 
 
+
+// ------------------------------------------------------- case generator
+// The lattice case of fsim_case_generate (fsim_host.cpp), generated on the
+// device with the same particles in the same order, bit for bit.  Sites are
+// visited there in (i, j, k) order, k fastest; along one (i, j) row the site
+// types are intervals in k, so a site's index among the particles of its
+// type, and its index among the sites that draw jitter (3 splitmix64 draws
+// each, a counter-based stream), follow from per-row bases (prefix sums over
+// rows, on the host) plus a closed-form count inside the row.
+struct CaseGeom {
+    int T[3], FN[3], SL[3], SN[3];
+    int fixed_layers, L;
+    int has_solid, jitter;
+    double dx, jit;
+    uint64_t seed;
+};
+struct RowIv {
+    int s0, s1;   // solid sites [s0, s1)
+    int f0, f1;   // fluid block sites [f0, f1) (before removing solid)
+    int inside;   // the row lies inside the tank in i and j
+    int fixed;    // solid sites of this row are FIXED (below the floor)
+};
+__host__ __device__ inline void case_row(const CaseGeom &g, int i, int j, RowIv &r)
+{
+    r.inside = !(i < 0 || i >= g.T[0] || j < 0 || j >= g.T[1]);
+    r.fixed = j < 0;
+    const bool solid_ij = g.has_solid && i >= g.SL[0] && i < g.SL[0] + g.SN[0] && j >= g.SL[1] - g.fixed_layers &&
+                          j < g.SL[1] + g.SN[1];
+    r.s0 = r.s1 = 0;
+    if (solid_ij) {
+        int lo = g.SL[2], hi = g.SL[2] + g.SN[2];
+        if (j >= 0) { // above the floor a solid site must be inside the tank
+            if (!r.inside) hi = lo;
+            lo = lo > 0 ? lo : 0;
+            hi = hi < g.T[2] ? hi : g.T[2];
+        }
+        lo = lo > -g.L ? lo : -g.L;
+        hi = hi < g.T[2] + g.L ? hi : g.T[2] + g.L;
+        if (hi > lo) {
+            r.s0 = lo;
+            r.s1 = hi;
+        }
+    }
+    r.f0 = r.f1 = 0;
+    if (r.inside && i < g.FN[0] && j < g.FN[1]) {
+        r.f0 = 0;
+        r.f1 = g.FN[2] < g.T[2] ? g.FN[2] : g.T[2];
+        if (r.f1 < 0) r.f1 = 0;
+    }
+}
+__host__ __device__ inline int iv_before(int a, int b, int k) // |[a, b) n (-inf, k)|
+{
+    const int e = b < k ? b : k;
+    return e > a ? e - a : 0;
+}
+__host__ __device__ inline int iv_overlap_before(int a, int b, int c, int d, int k)
+{
+    return iv_before(a > c ? a : c, b < d ? b : d, k);
+}
+// per-row particle counts: fluid, solid, virtual, jitter-drawing sites
+__host__ __device__ inline void case_row_counts(const CaseGeom &g, const RowIv &r, int c[4])
+{
+    const int kend = g.T[2] + g.L;
+    const int ns = r.s1 - r.s0;
+    const int nf = (r.f1 - r.f0) - iv_overlap_before(r.f0, r.f1, r.s0, r.s1, kend);
+    const int nv = r.inside ? 2 * g.L : (g.T[2] + 2 * g.L) - ns;
+    c[0] = nf;
+    c[1] = ns;
+    c[2] = nv;
+    c[3] = g.jitter ? nf + (r.fixed ? 0 : ns) : 0;
+}
+
+struct RowBase {
+    int f, s, v, pad;
+    long long d; // jitter-drawing sites before the row
+};
+struct CaseGenArgs {
+    CaseGeom g;
+    const RowBase *base;
+    const float2 *hydro; // (rho, p) per lattice row j of the fluid block
+    float rho0;
+    float4 *fposr, *fvelp;
+    int *forig;
+    float4 *spos, *svel, *sref;
+    int *stype, *sorig;
+    float4 *vpos;
+    long long nsite;
+};
+__device__ __forceinline__ double case_uniform(uint64_t seed, long long n) // draw n of splitmix64(seed)
+{
+    uint64_t z = seed + (uint64_t)(n + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return __dmul_rn((double)(z >> 11), 1.0 / 9007199254740992.0);
+}
+__global__ void k_case_generate(const CaseGenArgs A)
+{
+    const long long sidx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (sidx >= A.nsite) return;
+    const CaseGeom &g = A.g;
+    const int nk = g.T[2] + 2 * g.L, nj = g.T[1] + 2 * g.L;
+    const long long row = sidx / nk;
+    const int k = (int)(sidx - row * nk) - g.L;
+    const int i = (int)(row / nj) - g.L, j = (int)(row % nj) - g.L;
+    RowIv r;
+    case_row(g, i, j, r);
+    const RowBase b = A.base[row];
+    const bool in_solid = k >= r.s0 && k < r.s1;
+    const bool outside = !r.inside || k < 0 || k >= g.T[2];
+    const double x = __dmul_rn((double)i + 0.5, g.dx), y = __dmul_rn((double)j + 0.5, g.dx),
+                 z = __dmul_rn((double)k + 0.5, g.dx);
+    const int solid_before = iv_before(r.s0, r.s1, k);
+    const int fluid_before = iv_before(r.f0, r.f1, k) - iv_overlap_before(r.f0, r.f1, r.s0, r.s1, k);
+    auto jittered = [&](double* p) {
+        const long long d = b.d + fluid_before + (r.fixed ? 0 : solid_before);
+        for (int a = 0; a < 3; ++a) {
+            const double u = case_uniform(g.seed, 3 * d + a);
+            p[a] = __dadd_rn(p[a], __dmul_rn(__dsub_rn(__dmul_rn(2.0, u), 1.0), g.jit));
+        }
+    };
+    if (in_solid) {
+        const int idx = b.s + solid_before;
+        double p[3] = {x, y, z};
+        if (!r.fixed && g.jitter) jittered(p);
+        const float4 q = make_float4((float)p[0], (float)p[1], (float)p[2], 0.0f);
+        A.spos[idx] = q;
+        A.sref[idx] = q;
+        A.svel[idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        A.stype[idx] = r.fixed ? 1 : 0;
+        A.sorig[idx] = idx;
+    } else if (outside) {
+        const int before = r.inside ? (k < 0 ? k + g.L : g.L + (k - g.T[2])) : (k + g.L) - solid_before;
+        A.vpos[b.v + before] = make_float4((float)x, (float)y, (float)z, A.rho0);
+    } else if (k >= r.f0 && k < r.f1) {
+        const int idx = b.f + fluid_before;
+        double p[3] = {x, y, z};
+        if (g.jitter) jittered(p);
+        const float2 hp = A.hydro[j];
+        A.fposr[idx] = make_float4((float)p[0], (float)p[1], (float)p[2], hp.x);
+        A.fvelp[idx] = make_float4(0.0f, 0.0f, 0.0f, hp.y);
+        A.forig[idx] = idx;
+    }
+}
+
 // ------------------------------------------------------------------ probes
 // Probe::getData (src/probe.cu, commented out in the reference, 2D), in 3D:
 // the Shepard average, weight (exp(-r^2/h^2) - c1) c2 as in
@@ -2707,19 +2852,25 @@ struct DeviceGuard {
 
 // counting-sort the virtual particles once (walls are static), with the same
 // batched sort kernels run as a one-instance plan over temporary arrays
-fsim_status sort_virtual(fsim_sim *h, const float *vpos_host)
+// vpos_host: 3 floats per wall particle in host memory; or vpos_dev: float4
+// (x, y, z, rho0) per wall particle already on the device (consumed)
+fsim_status sort_virtual(fsim_sim *h, const float *vpos_host, float4 *vpos_dev = nullptr)
 {
     const int n = h->nv;
     float *d_xyz = nullptr;
     float4 *tmp_pos = nullptr;
     int *key = nullptr, *slot = nullptr, *tmp = nullptr, *cnt = nullptr, *orig0 = nullptr;
     fsim_status st;
-    if ((st = dalloc(h, &d_xyz, 3 * (size_t)n)) || (st = dalloc(h, &tmp_pos, n)) || (st = dalloc(h, &key, n)) ||
-        (st = dalloc(h, &slot, n)) || (st = dalloc(h, &tmp, n)) || (st = dalloc(h, &cnt, h->ncell)) ||
-        (st = dalloc(h, &orig0, n)))
+    if ((st = dalloc(h, &d_xyz, vpos_dev ? 1 : 3 * (size_t)n)) || (st = dalloc(h, &tmp_pos, n)) ||
+        (st = dalloc(h, &key, n)) || (st = dalloc(h, &slot, n)) || (st = dalloc(h, &tmp, n)) ||
+        (st = dalloc(h, &cnt, h->ncell)) || (st = dalloc(h, &orig0, n)))
         return st;
-    CK(cudaMemcpyAsync(d_xyz, vpos_host, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, h->stream));
-    k_pack_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(d_xyz, nullptr, n, h->P.rho0, tmp_pos);
+    if (vpos_dev) {
+        CK(cudaMemcpyAsync(tmp_pos, vpos_dev, sizeof(float4) * n, cudaMemcpyDeviceToDevice, h->stream));
+    } else {
+        CK(cudaMemcpyAsync(d_xyz, vpos_host, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+        k_pack_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(d_xyz, nullptr, n, h->P.rho0, tmp_pos);
+    }
     k_iota<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(orig0, n);
     CK_LAUNCH();
     Plan pl;
@@ -3756,6 +3907,192 @@ extern "C" fsim_status fsim_snapshot_read(const char *path, int device, fsim_han
     while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
     std::fclose(f);
     return fsim_snapshot_load(buf.data(), buf.size(), device, out, step);
+}
+
+// =================================================================== case on the device
+namespace {
+fsim_status case_geometry(const fsim_case *cs, CaseGeom &g)
+{
+    if (!(cs->dx > 0.0f) || cs->tank_n[0] <= 0 || cs->tank_n[1] <= 0 || cs->tank_n[2] <= 0 || cs->virt_layers < 0 ||
+        cs->solid_fixed_layers < 0) {
+        fsim_set_error("invalid case description");
+        return FSIM_EINVAL;
+    }
+    for (int a = 0; a < 3; ++a) {
+        g.T[a] = cs->tank_n[a];
+        g.FN[a] = cs->fluid_n[a];
+        g.SL[a] = cs->solid_lo[a];
+        g.SN[a] = cs->solid_n[a];
+    }
+    g.fixed_layers = cs->solid_fixed_layers;
+    g.L = cs->virt_layers;
+    g.has_solid = cs->solid_n[0] > 0 && cs->solid_n[1] > 0 && cs->solid_n[2] > 0;
+    g.dx = cs->dx;
+    g.jit = (double)cs->jitter * (double)cs->dx;
+    g.jitter = g.jit > 0.0;
+    g.seed = cs->seed;
+    const double sites = (double)(g.T[0] + 2 * g.L) * (g.T[1] + 2 * g.L) * (g.T[2] + 2 * g.L);
+    if (sites > 2e9) {
+        fsim_set_error("case lattice too large");
+        return FSIM_EINVAL;
+    }
+    return FSIM_OK;
+}
+
+// per-row bases and the totals
+void case_rows(const CaseGeom &g, std::vector<RowBase> &base, long long tot[4])
+{
+    const int ni = g.T[0] + 2 * g.L, nj = g.T[1] + 2 * g.L;
+    base.resize((size_t)ni * nj);
+    tot[0] = tot[1] = tot[2] = tot[3] = 0;
+    for (int i = -g.L; i < g.T[0] + g.L; ++i)
+        for (int j = -g.L; j < g.T[1] + g.L; ++j) {
+            RowIv r;
+            case_row(g, i, j, r);
+            int c[4];
+            case_row_counts(g, r, c);
+            RowBase &b = base[(size_t)(i + g.L) * nj + (j + g.L)];
+            b.f = (int)tot[0];
+            b.s = (int)tot[1];
+            b.v = (int)tot[2];
+            b.pad = 0;
+            b.d = tot[3];
+            for (int a = 0; a < 4; ++a) tot[a] += c[a];
+        }
+}
+} // namespace
+
+extern "C" fsim_status fsim_case_counts(const fsim_case *cs, int *n_fluid, int *n_solid, int *n_virt)
+{
+    if (!cs || !n_fluid || !n_solid || !n_virt) return FSIM_EINVAL;
+    CaseGeom g;
+    fsim_status st = case_geometry(cs, g);
+    if (st) return st;
+    std::vector<RowBase> base;
+    long long tot[4];
+    case_rows(g, base, tot);
+    if (tot[0] > INT_MAX || tot[1] > INT_MAX || tot[2] > INT_MAX) {
+        fsim_set_error("case too large");
+        return FSIM_EINVAL;
+    }
+    *n_fluid = (int)tot[0];
+    *n_solid = (int)tot[1];
+    *n_virt = (int)tot[2];
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_create_case(const fsim_config *cfg, const fsim_case *cs, int device, fsim_handle *out)
+{
+    if (!cfg || !cs || !out) return FSIM_EINVAL;
+    *out = nullptr;
+    CaseGeom g;
+    fsim_status st = case_geometry(cs, g);
+    if (st) return st;
+    std::vector<RowBase> base;
+    long long tot[4];
+    case_rows(g, base, tot);
+    if (tot[0] > INT_MAX || tot[1] > INT_MAX || tot[2] > INT_MAX) {
+        fsim_set_error("case too large");
+        return FSIM_EINVAL;
+    }
+    // hydrostatic (rho, p) per fluid lattice row, as fsim_case_generate computes them
+    std::vector<float2> hydro(g.FN[1] > 0 ? g.FN[1] : 1, make_float2(cfg->fluid_density, 0.0f));
+    if (cs->hydrostatic) {
+        const double rho0 = cfg->fluid_density, c0 = cfg->fluid_sound_speed, gam = cfg->gamma, gr = cfg->gravity;
+        const double H = g.FN[1] * g.dx, p2rho = gam / (rho0 * c0 * c0);
+        for (int j = 0; j < g.FN[1]; ++j) {
+            const double y = (j + 0.5) * g.dx;
+            const double p = rho0 * gr * (H - y);
+            const double rho = rho0 * std::pow(p * p2rho + 1.0, 1.0 / gam);
+            hydro[j] = make_float2((float)rho, (float)p);
+        }
+    }
+    fsim_sim *h = nullptr;
+    if ((st = new_handle(cfg, (int)tot[0], (int)tot[1], (int)tot[2], device, &h))) return st;
+    DeviceGuard guard(h->device);
+    auto fail = [&](fsim_status code) {
+        free_all(h);
+        delete h;
+        return code;
+    };
+    if ((st = alloc_state(h))) return fail(st);
+    RowBase *d_base = nullptr;
+    float2 *d_hydro = nullptr;
+    float4 *d_vpos = nullptr;
+    if ((st = dalloc(h, &d_base, base.size())) || (st = dalloc(h, &d_hydro, hydro.size())) ||
+        (st = dalloc(h, &d_vpos, (size_t)h->nv)))
+        return fail(st);
+    CK(cudaMemcpyAsync(d_base, base.data(), sizeof(RowBase) * base.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(d_hydro, hydro.data(), sizeof(float2) * hydro.size(), cudaMemcpyHostToDevice, h->stream));
+    CaseGenArgs A;
+    A.g = g;
+    A.base = d_base;
+    A.hydro = d_hydro;
+    A.rho0 = h->P.rho0;
+    A.fposr = h->f_posr[0];
+    A.fvelp = h->f_velp[0];
+    A.forig = h->f_orig[0];
+    A.spos = h->s_pos[0];
+    A.svel = h->s_vel[0];
+    A.sref = h->s_ref[0];
+    A.stype = h->s_type[0];
+    A.sorig = h->s_orig[0];
+    A.vpos = d_vpos;
+    A.nsite = (long long)(g.T[0] + 2 * g.L) * (g.T[1] + 2 * g.L) * (g.T[2] + 2 * g.L);
+    k_case_generate<<<blocks_for(A.nsite, kBlock), kBlock, 0, h->stream>>>(A);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        fsim_set_error("case generation failed: %s", cudaGetErrorString(e));
+        return fail(FSIM_ECUDA);
+    }
+    const int nf = h->nf, ns = h->ns;
+    if (nf && h->mixed) {
+        k_fluid_to_mixed<<<blocks_for(nf, kBlock), kBlock, 0, h->stream>>>(h->P, h->f_posr[0], h->f_velp[0],
+                                                                           h->f_cell, nf, h->d_flags);
+        CK(cudaGetLastError());
+    }
+    if (ns) {
+        std::vector<float4> ref4(ns);
+        CK(cudaMemcpyAsync(ref4.data(), h->s_ref[0], sizeof(float4) * ns, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        std::vector<float> ref(3 * (size_t)ns);
+        for (int k = 0; k < ns; ++k) {
+            ref[3 * k] = ref4[k].x;
+            ref[3 * k + 1] = ref4[k].y;
+            ref[3 * k + 2] = ref4[k].z;
+        }
+        std::vector<float> eye(9 * (size_t)ns, 0.0f);
+        for (int k = 0; k < ns; ++k) eye[9 * k] = eye[9 * k + 4] = eye[9 * k + 8] = 1.0f;
+        CK(cudaMemcpy(h->s_F, eye.data(), sizeof(float) * 9 * ns, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->s_L, eye.data(), sizeof(float) * 9 * ns, cudaMemcpyHostToDevice));
+        CK(cudaMemset(h->s_P, 0, sizeof(float) * 9 * ns));
+        CK(cudaMemset(h->s_dudt, 0, sizeof(float4) * ns));
+        CK(cudaMemset(h->s_couple, 0, sizeof(float4) * ns));
+        h->s_mech_ok = h->s_np_ok = true;
+        if ((st = build_solid_neighbors(h, ref.data()))) return fail(st);
+    }
+    if (h->nv) {
+        if ((st = sort_virtual(h, nullptr, d_vpos))) return fail(st);
+        if (h->mixed) {
+            k_offsets_in_cells<<<blocks_for(h->nv, kBlock), kBlock, 0, h->stream>>>(h->P, h->v_posr, h->v_cell,
+                                                                                     h->nv);
+            CK(cudaGetLastError());
+        }
+    }
+    // generation temporaries are released now
+    CK(cudaStreamSynchronize(h->stream));
+    void *tmps[] = {d_base, d_hydro, d_vpos};
+    for (void *p : tmps) {
+        cudaFree(p);
+        for (auto it = h->allocations.begin(); it != h->allocations.end(); ++it)
+            if (*it == p) {
+                h->allocations.erase(it);
+                break;
+            }
+    }
+    if ((st = check_flags(h))) return fail(st);
+    *out = h;
+    return FSIM_OK;
 }
 
 extern "C" fsim_status fsim_counts(fsim_handle h, int *nf, int *ns, int *nv)

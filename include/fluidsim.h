@@ -168,6 +168,8 @@ typedef struct fsim_case {
 } fsim_case;
 fsim_status fsim_case_generate(const fsim_case *c, const fsim_config *cfg,
                                fsim_particle_set_t *out);
+/* Particle counts of a case, without generating it. */
+fsim_status fsim_case_counts(const fsim_case *c, int *n_fluid, int *n_solid, int *n_virt);
 
 /* -------------------------------------------------------------- simulation */
 typedef struct fsim_sim *fsim_handle;
@@ -178,6 +180,12 @@ typedef struct fsim_sim *fsim_handle;
  * device < 0 keeps the current device. */
 fsim_status fsim_create(const fsim_config *cfg, const fsim_particles *p,
                         int device, fsim_handle *out);
+/* The same case generated on the device straight into a new handle (no host
+ * particle arrays): identical particles in identical order, bit for bit, as
+ * fsim_case_generate + fsim_create.  For admitting many scenarios quickly
+ * (host generation and copies would dominate their start-up).  No
+ * counterpart in the reference (its generator is a separate host program). */
+fsim_status fsim_create_case(const fsim_config *cfg, const fsim_case *c, int device, fsim_handle *out);
 fsim_status fsim_destroy(fsim_handle h);
 
 /* Advance nsteps fluid steps (each with solid_sub_step solid sub-steps);

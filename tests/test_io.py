@@ -99,3 +99,25 @@ def test_jitter_bounded_and_seeded():
     assert not np.array_equal(a.fluid_pos, c.fluid_pos)
     assert np.abs(a.fluid_pos - z.fluid_pos).max() <= 0.01 * 0.01 * 1.0001
     assert np.array_equal(a.virt_pos, z.virt_pos)  # walls are not jittered
+
+
+@pytest.mark.parametrize("spec", [
+    cases.tiny_box(), cases.tiny_box(with_solid=False), cases.small_dam_break(),
+    cases.tiny_box(fluid=(30, 20, 30)),  # fluid block larger than the tank: clipped
+])
+def test_case_counts_match_host_generator(spec):
+    """The per-row interval logic of the device generator counts the same
+    particles as the host generator's site loop."""
+    cfg, case = spec
+    _, pa = cases.make(spec)
+    assert api.case_counts(case) == (pa.n_fluid, pa.n_solid, pa.n_virt)
+
+
+def test_case_counts_with_solid_below_the_floor_and_outside():
+    """Fixed layers below the floor, and a solid block reaching out of the tank."""
+    cfg, case = cases.tiny_box()
+    case.solid_fixed_layers = 3
+    case.solid_lo[2] = -2
+    case.solid_n[2] = 30
+    _, pa = cases.make((cfg, case))
+    assert api.case_counts(case) == (pa.n_fluid, pa.n_solid, pa.n_virt)
