@@ -262,12 +262,13 @@ def run_gb300(args, dist):
     dist.barrier()
     sim.sync()
     t0 = time.perf_counter()
+    names = list(bufs)
+    ptrs = [bufs[k].ptr for k in names]
+    sizes = [bufs[k].nbytes for k in names]
     for _ in range(e2e_steps):
-        for k, b in bufs.items():
-            sim.set_ptr(k, b.ptr, b.nbytes)
+        sim.set_many_ptr(names, ptrs, sizes)   # fsim_set_fields: the step's whole input state
         sim.step(1)
-        for k, b in bufs.items():
-            sim.get_ptr(k, b.ptr, b.nbytes)
+        sim.get_many_ptr(names, ptrs, sizes)   # fsim_get_fields: the step's whole result
     sim.sync()
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e = nupd * e2e_steps * dist.ws / e2e_s

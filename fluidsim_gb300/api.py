@@ -151,6 +151,8 @@ def load():
         "fsim_batch_sync_members": (C.c_int, [P, P, C.c_int]),
         "fsim_create_case": (C.c_int, [P, P, C.c_int, C.POINTER(P)]),
         "fsim_case_counts": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "fsim_get_fields": (C.c_int, [P, C.c_int, P, P, P]),
+        "fsim_set_fields": (C.c_int, [P, C.c_int, P, P, P]),
         "fsim_snapshot_save": (C.c_int, [P, C.c_longlong, P, C.c_size_t]),
         "fsim_snapshot_load": (C.c_int, [P, C.c_size_t, C.c_int, C.POINTER(P), C.POINTER(C.c_longlong)]),
         "fsim_snapshot_write": (C.c_int, [P, C.c_longlong, C.c_char_p]),
@@ -189,6 +191,7 @@ EXPORTED = [
     "fsim_measure_fp32_peak", "fsim_sweep_tuning", "fsim_batch_sweep_tuning", "fsim_snapshot_bytes",
     "fsim_snapshot_save", "fsim_snapshot_load", "fsim_snapshot_write", "fsim_snapshot_read", "fsim_probe",
     "fsim_write_vtk_binary", "fsim_batch_sync_members", "fsim_create_case", "fsim_case_counts",
+    "fsim_get_fields", "fsim_set_fields",
 ]
 SWEEP_SHAPES = ((4, 48), (4, 32), (8, 32))  # (warps per block, list capacity) per shape index
 
@@ -461,6 +464,22 @@ class Simulation:
 
     def get_ptr(self, name, ptr, nbytes):
         check(self.lib.fsim_get_field(self.h, FIELDS[name], ptr, nbytes))
+
+    def get_many_ptr(self, names, ptrs, nbytes):
+        """fsim_get_fields: several fields into host pointers, one synchronisation."""
+        n = len(names)
+        ids = (C.c_int * n)(*[FIELDS[k] for k in names])
+        dst = (C.c_void_p * n)(*[p.value if isinstance(p, C.c_void_p) else p for p in ptrs])
+        nb = (C.c_size_t * n)(*nbytes)
+        check(self.lib.fsim_get_fields(self.h, n, ids, dst, nb))
+
+    def set_many_ptr(self, names, ptrs, nbytes):
+        """fsim_set_fields: several fields from host pointers."""
+        n = len(names)
+        ids = (C.c_int * n)(*[FIELDS[k] for k in names])
+        src = (C.c_void_p * n)(*[p.value if isinstance(p, C.c_void_p) else p for p in ptrs])
+        nb = (C.c_size_t * n)(*nbytes)
+        check(self.lib.fsim_set_fields(self.h, n, ids, src, nb))
 
     def neighbor_counts(self):
         out = np.empty((self.n["fluid"], 3), np.int32)

@@ -2188,6 +2188,10 @@ struct fsim_sim {
     unsigned *d_flags = nullptr;
     void *staging = nullptr;
     size_t staging_bytes = 0;
+    void *bulk = nullptr;            // several fields at once (fsim_get_fields / fsim_set_fields)
+    size_t bulk_bytes = 0;
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> xfer_events;
     SweepTuner tuner;
     Plan *step_plans[2][2] = {};   // full step, by (fluid, solid) buffer parity
     Plan *phase_plans[5][2][2] = {}; // one phase, by parity
@@ -2254,6 +2258,10 @@ void free_all(fsim_sim *h)
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     h->tuner.release();
+    if (h->bulk) cudaFree(h->bulk);
+    for (cudaEvent_t e : h->xfer_events) cudaEventDestroy(e);
+    h->xfer_events.clear();
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -3291,10 +3299,10 @@ static int field_count(fsim_sim *h, int field)
     return h->nv;
 }
 
-extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_t bytes)
+namespace {
+// Field size check shared by the getters and setters.
+fsim_status check_field_bytes(fsim_sim *h, int field, size_t bytes, int *count)
 {
-    if (!h || (!dst && bytes)) return FSIM_EINVAL;
-    if (h->batch) batch_wait(h);
     const int width = fsim_field_width(field);
     if (!width) {
         fsim_set_error("unknown field %d", field);
@@ -3305,10 +3313,15 @@ extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_
         fsim_set_error("field %d needs %zu bytes, got %zu", field, (size_t)n * width * 4, bytes);
         return FSIM_EINVAL;
     }
-    if (n == 0) return FSIM_OK;
-    DeviceGuard guard(h->device);
+    *count = n;
+    return FSIM_OK;
+}
+
+// Enqueue on the handle's stream the kernel that writes `field` in input
+// order into device memory `stg` (n = the field's particle count > 0).
+fsim_status enqueue_unpermute(fsim_sim *h, int field, int n, float *stg)
+{
     const int g = blocks_for(n, kBlock);
-    float *stg = (float *)h->staging;
     const int *forig = h->f_orig[h->f_cur];
     const int *sorig = h->s_orig[h->s_cur];
     if (h->mixed && (field == FSIM_FLUID_POS || field == FSIM_FLUID_RHO || field == FSIM_FLUID_P ||
@@ -3324,8 +3337,6 @@ extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_
                                                                                       : MF_P,
                                                             stg);
         CK_LAUNCH();
-        CK(cudaMemcpyAsync(dst, stg, bytes, cudaMemcpyDeviceToHost, h->stream));
-        CK(cudaStreamSynchronize(h->stream));
         return FSIM_OK;
     }
     switch (field) {
@@ -3403,51 +3414,178 @@ extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_
     default: return FSIM_EINVAL;
     }
     CK_LAUNCH();
+    return FSIM_OK;
+}
+} // namespace
+
+extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_t bytes)
+{
+    if (!h || (!dst && bytes)) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
+    int n = 0;
+    fsim_status st = check_field_bytes(h, field, bytes, &n);
+    if (st) return st;
+    if (n == 0) return FSIM_OK;
+    DeviceGuard guard(h->device);
+    float *stg = (float *)h->staging;
+    if ((st = enqueue_unpermute(h, field, n, stg))) return st;
     CK(cudaMemcpyAsync(dst, stg, bytes, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return FSIM_OK;
 }
 
-extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src, size_t bytes)
+namespace {
+// The destination of a settable field; FSIM_EINVAL for the others.
+fsim_status set_target(fsim_sim *h, int field, float4 **dst, const int **orig, int *comp)
 {
-    if (!h || (!src && bytes)) return FSIM_EINVAL;
-    if (h->batch) batch_wait(h);
-    const int width = fsim_field_width(field);
-    const int n = field_count(h, field);
-    float4 *dst = nullptr;
-    const int *orig = nullptr;
-    int comp = 0;
     switch (field) {
-    case FSIM_FLUID_POS: dst = h->f_posr[h->f_cur]; comp = 0; break;
-    case FSIM_FLUID_RHO: dst = h->f_posr[h->f_cur]; comp = 3; break;
-    case FSIM_FLUID_VEL: dst = h->f_velp[h->f_cur]; comp = 0; break;
-    case FSIM_FLUID_P: dst = h->f_velp[h->f_cur]; comp = 3; break;
-    case FSIM_SOLID_POS: dst = h->s_pos[h->s_cur]; comp = 0; break;
-    case FSIM_SOLID_VEL: dst = h->s_vel[h->s_cur]; comp = 0; break;
+    case FSIM_FLUID_POS: *dst = h->f_posr[h->f_cur]; *comp = 0; break;
+    case FSIM_FLUID_RHO: *dst = h->f_posr[h->f_cur]; *comp = 3; break;
+    case FSIM_FLUID_VEL: *dst = h->f_velp[h->f_cur]; *comp = 0; break;
+    case FSIM_FLUID_P: *dst = h->f_velp[h->f_cur]; *comp = 3; break;
+    case FSIM_SOLID_POS: *dst = h->s_pos[h->s_cur]; *comp = 0; break;
+    case FSIM_SOLID_VEL: *dst = h->s_vel[h->s_cur]; *comp = 0; break;
     default: fsim_set_error("field %d is not settable", field); return FSIM_EINVAL;
     }
-    orig = field < 10 ? h->f_orig[h->f_cur] : h->s_orig[h->s_cur];
+    *orig = field < 10 ? h->f_orig[h->f_cur] : h->s_orig[h->s_cur];
     if (h->mixed && field == FSIM_FLUID_P) {
         fsim_set_error("in the mixed form the fluid pressure is the EOS of the density; set FSIM_FLUID_RHO");
         return FSIM_EINVAL;
     }
-    if (bytes != (size_t)n * width * 4) {
-        fsim_set_error("field %d needs %zu bytes, got %zu", field, (size_t)n * width * 4, bytes);
-        return FSIM_EINVAL;
-    }
-    if (n == 0) return FSIM_OK;
-    DeviceGuard guard(h->device);
-    CK(cudaMemcpyAsync(h->staging, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    return FSIM_OK;
+}
+
+// Enqueue on the handle's stream the kernel that scatters `field` (input
+// order, device memory `stg`) into the state (n > 0).
+fsim_status enqueue_permute_in(fsim_sim *h, int field, int n, const float *stg)
+{
+    float4 *dst = nullptr;
+    const int *orig = nullptr;
+    int comp = 0;
+    fsim_status st = set_target(h, field, &dst, &orig, &comp);
+    if (st) return st;
+    const int width = fsim_field_width(field);
     if (h->mixed && (field == FSIM_FLUID_POS || field == FSIM_FLUID_RHO))
         k_permute_in_mixed<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(
             h->P, h->f_posr[h->f_cur], h->f_velp[h->f_cur], h->f_cell, orig, n,
-            field == FSIM_FLUID_POS ? MF_POS : MF_RHO, (const float *)h->staging);
+            field == FSIM_FLUID_POS ? MF_POS : MF_RHO, stg);
     else
-        k_permute_in_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(dst, orig, n, comp, width,
-                                                                          (const float *)h->staging);
+        k_permute_in_f4<<<blocks_for(n, kBlock), kBlock, 0, h->stream>>>(dst, orig, n, comp, width, stg);
     CK_LAUNCH();
+    return FSIM_OK;
+}
+} // namespace
+
+extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src, size_t bytes)
+{
+    if (!h || (!src && bytes)) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
+    float4 *dst = nullptr;
+    const int *orig = nullptr;
+    int comp = 0, n = 0;
+    fsim_status st = set_target(h, field, &dst, &orig, &comp);
+    if (st) return st;
+    if ((st = check_field_bytes(h, field, bytes, &n))) return st;
+    if (n == 0) return FSIM_OK;
+    DeviceGuard guard(h->device);
+    CK(cudaMemcpyAsync(h->staging, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    if ((st = enqueue_permute_in(h, field, n, (const float *)h->staging))) return st;
     if (h->batch) CK(cudaStreamSynchronize(h->stream)); // the batch stream must see it
-    // positions changed: derived per-step products are stale until the next phases
+    return FSIM_OK;
+}
+
+namespace {
+// Device buffer for several fields at once, grown on demand; a copy stream
+// and events so that copies overlap the (un)permute kernels.
+fsim_status bulk_reserve(fsim_sim *h, size_t bytes, int nev)
+{
+    if (bytes > h->bulk_bytes) {
+        if (h->bulk) cudaFree(h->bulk);
+        h->bulk = nullptr;
+        h->bulk_bytes = 0;
+        cudaError_t e = cudaMalloc(&h->bulk, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            fsim_set_error("cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+            return FSIM_ENOMEM;
+        }
+        h->bulk_bytes = bytes;
+    }
+    if (!h->copy_stream) CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    while ((int)h->xfer_events.size() < nev) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        h->xfer_events.push_back(e);
+    }
+    return FSIM_OK;
+}
+} // namespace
+
+extern "C" fsim_status fsim_get_fields(fsim_handle h, int nfields, const int *fields, void *const *dst,
+                                       const size_t *bytes)
+{
+    if (!h || nfields < 0 || (nfields && (!fields || !dst || !bytes))) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
+    std::vector<int> counts(nfields);
+    size_t total = 0;
+    for (int k = 0; k < nfields; ++k) {
+        fsim_status st = check_field_bytes(h, fields[k], bytes[k], &counts[k]);
+        if (st) return st;
+        if (bytes[k] && !dst[k]) return FSIM_EINVAL;
+        total += (bytes[k] + 255) & ~size_t(255);
+    }
+    DeviceGuard guard(h->device);
+    fsim_status st = bulk_reserve(h, total, nfields);
+    if (st) return st;
+    size_t off = 0;
+    for (int k = 0; k < nfields; ++k) {
+        if (!counts[k]) continue;
+        float *stg = reinterpret_cast<float *>(static_cast<char *>(h->bulk) + off);
+        if ((st = enqueue_unpermute(h, fields[k], counts[k], stg))) return st;
+        CK(cudaEventRecord(h->xfer_events[k], h->stream));
+        CK(cudaStreamWaitEvent(h->copy_stream, h->xfer_events[k], 0));
+        CK(cudaMemcpyAsync(dst[k], stg, bytes[k], cudaMemcpyDeviceToHost, h->copy_stream));
+        off += (bytes[k] + 255) & ~size_t(255);
+    }
+    CK(cudaStreamSynchronize(h->copy_stream));
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_set_fields(fsim_handle h, int nfields, const int *fields, const void *const *src,
+                                       const size_t *bytes)
+{
+    if (!h || nfields < 0 || (nfields && (!fields || !src || !bytes))) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
+    std::vector<int> counts(nfields);
+    size_t total = 0;
+    for (int k = 0; k < nfields; ++k) {
+        float4 *d;
+        const int *o;
+        int c;
+        fsim_status st = set_target(h, fields[k], &d, &o, &c);
+        if (st) return st;
+        if ((st = check_field_bytes(h, fields[k], bytes[k], &counts[k]))) return st;
+        if (bytes[k] && !src[k]) return FSIM_EINVAL;
+        total += (bytes[k] + 255) & ~size_t(255);
+    }
+    DeviceGuard guard(h->device);
+    fsim_status st = bulk_reserve(h, total, nfields);
+    if (st) return st;
+    // the copies start after the handle's queued work (they overwrite the bulk buffer)
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaStreamWaitEvent(h->copy_stream, h->ev1, 0));
+    size_t off = 0;
+    for (int k = 0; k < nfields; ++k) {
+        if (!counts[k]) continue;
+        float *stg = reinterpret_cast<float *>(static_cast<char *>(h->bulk) + off);
+        CK(cudaMemcpyAsync(stg, src[k], bytes[k], cudaMemcpyHostToDevice, h->copy_stream));
+        CK(cudaEventRecord(h->xfer_events[k], h->copy_stream));
+        CK(cudaStreamWaitEvent(h->stream, h->xfer_events[k], 0));
+        if ((st = enqueue_permute_in(h, fields[k], counts[k], stg))) return st;
+        off += (bytes[k] + 255) & ~size_t(255);
+    }
+    CK(cudaStreamSynchronize(h->copy_stream)); // the host buffers may be reused on return
+    if (h->batch) CK(cudaStreamSynchronize(h->stream));
     return FSIM_OK;
 }
 

@@ -227,6 +227,14 @@ fsim_status fsim_get_field(fsim_handle h, int field, void *host_dst, size_t byte
  * FLUID_POS/VEL/RHO/P, SOLID_POS/VEL.  Used by the end-to-end benchmark
  * (host->device inputs per step) and by tests. */
 fsim_status fsim_set_field(fsim_handle h, int field, const void *host_src, size_t bytes);
+/* Several fields in one call (field ids, host pointers, byte counts; same
+ * checks as fsim_get_field / fsim_set_field): the device-side (un)permutes
+ * run on the handle's stream while the host copies run on a copy stream, with
+ * one host synchronisation for all of them.  fsim_set_fields returns once the
+ * host buffers have been read.  An extension for callers that move the whole
+ * state every step. */
+fsim_status fsim_get_fields(fsim_handle h, int n, const int *fields, void *const *dst, const size_t *bytes);
+fsim_status fsim_set_fields(fsim_handle h, int n, const int *fields, const void *const *src, const size_t *bytes);
 
 /* Neighbour search products.
  * counts: for every fluid particle (input order) the number of fluid, solid

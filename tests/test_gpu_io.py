@@ -179,3 +179,25 @@ def test_binary_vtk_holds_exact_fields(tmp_path):
     assert not zero.any()
     xs, _, _ = _read_binary_vtk(tmp_path / "solid" / "solid_velocity-3.vtk")
     assert np.array_equal(xs, spos)
+
+
+def test_many_fields_equal_single_fields():
+    """fsim_get_fields / fsim_set_fields move the same bytes as the one-field calls."""
+    cfg, pa = cases.make(cases.tiny_box(jitter=0.01, seed=6))
+    names = ("fluid_pos", "fluid_vel", "fluid_rho", "fluid_p", "solid_pos", "solid_vel")
+    with api.Simulation(cfg, pa, device=0) as sim:
+        sim.step(2)
+        sim.sync()
+        single = {k: sim.get(k) for k in names}
+        bufs = {k: api.PinnedBuffer(single[k].shape) for k in names}
+        sim.get_many_ptr(names, [bufs[k].ptr for k in names], [bufs[k].nbytes for k in names])
+        for k in names:
+            assert np.array_equal(bufs[k].array, single[k]), k
+        # set: perturb and write back all at once; read back one by one
+        for k in names:
+            bufs[k].array[...] = single[k] * 1.001
+        sim.set_many_ptr(names, [bufs[k].ptr for k in names], [bufs[k].nbytes for k in names])
+        for k in names:
+            assert np.array_equal(sim.get(k), bufs[k].array), k
+        for b in bufs.values():
+            b.free()
