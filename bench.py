@@ -392,6 +392,17 @@ def run_ensemble(dev, steps):
         chosen, tune_ms = b.sweep_tuning()
     for sm in sims:
         sm.close()
+    # the same ensemble with the solid sub-steps as one persistent cooperative launch
+    for cfg, _ in members:
+        cfg.solid_fused = 1
+    sims = [api.Simulation(cfg, pa, device=dev) for cfg, pa in members]
+    with api.Batch(sims) as b:
+        b.step(3)
+        b.sync()
+        fused_ms = b.time_steps(steps)
+        fused_launches = b.launches_per_step()
+    for sm in sims:
+        sm.close()
     return {
         "workload": "ensemble of 64 dam-break instances (seed 2024), %d fluid+solid particles in total, "
                     "dx=0.01, dt=1e-4, 4-5 solid sub-steps" % total,
@@ -402,6 +413,8 @@ def run_ensemble(dev, steps):
         "unit": "particle-updates/s",
         "batched_launches_per_step": launches,
         "autotuner": {"chosen_shape": chosen, "sweep_ms_per_shape": tune_ms},
+        "batched_fused_solid": total * steps / (fused_ms * 1e-3),
+        "batched_fused_solid_launches_per_step": fused_launches,
     }
 
 

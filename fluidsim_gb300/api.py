@@ -49,6 +49,7 @@ class Config(C.Structure):
         ("thread_num", C.c_int),
         ("precision", C.c_int),
         ("keep_derivatives", C.c_int),
+        ("solid_fused", C.c_int),
     ]
 
     def as_dict(self):

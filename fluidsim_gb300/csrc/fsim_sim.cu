@@ -57,7 +57,7 @@ struct DevParams {
     int mixed;
 };
 
-enum : unsigned { FLAG_OUT_OF_GRID = 1u };
+enum : unsigned { FLAG_OUT_OF_GRID = 1u, FLAG_BARRIER_TIMEOUT = 2u };
 constexpr unsigned kFull = 0xffffffffu;
 
 constexpr int kBlock = 256;
@@ -1332,6 +1332,8 @@ struct SolidArgs {
     const int *orig, *inv, *nbr_off, *nbr_orig;
     const float4 *nbr_dXw; // (X_j - X_i, kernel weight)
     const unsigned *cxyz;
+    int nsub;              // this instance's solid sub-steps per step
+    unsigned *flags;       // this instance's error flags
 };
 
 struct M3 {
@@ -1858,6 +1860,86 @@ __global__ void k_probe(const DevParams P, const ProbeArgs A)
     }
 }
 
+
+// ------------------------------------------------ fused solid sub-steps
+// All solid sub-steps of a step, for every instance of a plan, in ONE
+// persistent cooperative launch: per sub-step deformation, force and update
+// phases separated by grid barriers; each CTA walks the phases' virtual blocks
+// (the batched kernels' block prefix tables) with a grid stride.  Instances
+// with fewer sub-steps sit out the later ones.  The cooperative launch makes
+// every CTA resident at once; the barrier still gives up after a bounded wait
+// (FLAG_BARRIER_TIMEOUT on every instance, reported as FSIM_ETIMEOUT) instead
+// of spinning for ever.
+struct GridBarrier {
+    unsigned count, gen;
+};
+constexpr unsigned kBarrierSpinLimit = 1u << 22; // x ~64 ns sleeps: about a quarter of a second and more
+
+__device__ __forceinline__ void grid_sync(GridBarrier *b, bool &ok)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = &b->gen;
+        const unsigned g = *vgen; // read before arriving
+        __threadfence();
+        if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            unsigned spins = 0;
+            while (*vgen == g) {
+                if (++spins > kBarrierSpinLimit) {
+                    ok = false;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+struct SolidFusedArgs {
+    const int *bstart_w, *bstart_t; // prefix tables: 4 lanes per particle / thread per particle
+    int ninst, max_sub;
+    GridBarrier *barrier;
+};
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock, 3) kb_solid_fused(const Item<SolidArgs> *__restrict__ items,
+                                                         const SolidFusedArgs F)
+{
+    const int total_w = F.bstart_w[F.ninst], total_t = F.bstart_t[F.ninst];
+    bool ok = true;
+    for (int k = 0; k < F.max_sub; ++k) {
+        for (int b = blockIdx.x; b < total_w; b += gridDim.x) {
+            const int inst = locate_instance(F.bstart_w, F.ninst, b);
+            if (k >= items[inst].A.nsub) continue;
+            const DevParams P = items[inst].P;
+            solid_deform_body<MIXED>(P, items[inst].A, b - F.bstart_w[inst]);
+        }
+        grid_sync(F.barrier, ok);
+        for (int b = blockIdx.x; b < total_w; b += gridDim.x) {
+            const int inst = locate_instance(F.bstart_w, F.ninst, b);
+            if (k >= items[inst].A.nsub) continue;
+            const DevParams P = items[inst].P;
+            solid_force_body<MIXED>(P, items[inst].A, b - F.bstart_w[inst]);
+        }
+        grid_sync(F.barrier, ok);
+        for (int b = blockIdx.x; b < total_t; b += gridDim.x) {
+            const int inst = locate_instance(F.bstart_t, F.ninst, b);
+            if (k >= items[inst].A.nsub) continue;
+            const DevParams P = items[inst].P;
+            solid_update_body(P, items[inst].A, b - F.bstart_t[inst]);
+        }
+        if (k + 1 < F.max_sub) grid_sync(F.barrier, ok);
+    }
+    if (!ok && threadIdx.x == 0)
+        for (int inst = 0; inst < F.ninst; ++inst) atomicOr(items[inst].A.flags, FLAG_BARRIER_TIMEOUT);
+}
+
 // ------------------------------------------------------- neighbour counts
 __global__ void k_neighbor_counts(const DevParams P, const float4 *__restrict__ fposr, const int *__restrict__ cell_f,
                                   const int *__restrict__ start_f, const float4 *__restrict__ s_pos,
@@ -2346,7 +2428,7 @@ void fill_params(fsim_sim *h)
 enum LaunchKind {
     L_ZERO, L_HASH, L_SCAN_REDUCE, L_SCAN_PARTIALS, L_SCAN_APPLY, L_SCATTER, L_GATHER_F, L_GATHER_S,
     L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE,
-    L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M
+    L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M, L_SOLID_FUSED
 };
 
 struct Launch {
@@ -2355,6 +2437,8 @@ struct Launch {
     int ninst, blocks, variant;
     size_t shape_table_off[kSweepShapes]; // L_SWEEP: block prefix table per launch shape
     int shape_blocks[kSweepShapes];
+    size_t table2_off, barrier_off;       // L_SOLID_FUSED: thread-per-particle table, grid barrier
+    int max_sub;
 };
 
 struct Plan {
@@ -2565,51 +2649,94 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
     if (pl.launches.size() > before) pl.sweep_index = (int)before;
 }
 
-// solid sub-steps (in place on parity ps; the fluid is read at parity pf)
+// solid sub-steps (in place on parity ps; the fluid is read at parity pf):
+// per-phase batched launches, or (solid_fused) one persistent cooperative
+// launch for all sub-steps of all instances
+// CTAs of the fused solid kernel that can be resident at once on the current
+// device (a cooperative launch needs all of them resident), capped at `want`
+int fused_grid(bool mixed, int want)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (mixed)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_solid_fused<true>, kBlock, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_solid_fused<false>, kBlock, 0);
+    const int c = std::max(1, sms * per_sm);
+    return std::max(1, std::min(want, c));
+}
+
 void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
 {
     int max_sub = 0;
     for (fsim_sim *h : m)
         if (h->ns) max_sub = std::max(max_sub, h->cfg.solid_sub_step);
-    for (int k = 0; k < max_sub; ++k) {
-        std::vector<Item<SolidArgs>> it;
-        std::vector<int> wb, tb;
-        for (fsim_sim *h : m) {
-            SolidArgs S;
-            S.pos = h->s_pos[ps];
-            S.vel = h->s_vel[ps];
-            S.ref = h->s_ref[ps];
-            S.type = h->s_type[ps];
-            S.cell = h->s_cell;
-            S.start_s = h->s_start;
-            S.np = h->s_np;
-            S.F = h->s_F;
-            S.Pk = h->s_P;
-            S.L = h->s_L;
-            S.PL = h->s_PL;
-            S.AV = h->s_AV;
-            S.dudt = h->s_dudt;
-            S.couple = h->s_couple;
-            S.fposr = h->f_posr[pf];
-            S.fvelp = h->f_velp[pf];
-            S.start_f = h->f_start;
-            S.n = h->ns;
-            S.orig = h->s_orig[ps];
-            S.inv = h->s_inv;
-            S.nbr_off = h->s_nbr_off;
-            S.nbr_orig = h->s_nbr_orig;
-            S.nbr_dXw = h->s_nbr_dXw;
-            S.cxyz = h->s_cxyz;
-            it.push_back({h->P, S});
-            const bool active = h->ns && k < h->cfg.solid_sub_step;
-            wb.push_back(active ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
-            tb.push_back(active ? blocks_for(h->ns, kBlock) : 0);
-        }
-        const bool mixed = !m.empty() && m[0]->mixed;
-        add_launch(pl, ab, mixed ? L_DEFORM_M : L_DEFORM, it, wb);
-        add_launch(pl, ab, mixed ? L_FORCE_M : L_FORCE, it, wb);
-        add_launch(pl, ab, L_UPDATE, it, tb);
+    if (!max_sub) return;
+    std::vector<Item<SolidArgs>> it;
+    std::vector<int> tw(m.size() + 1, 0), tt(m.size() + 1, 0);
+    for (size_t q = 0; q < m.size(); ++q) {
+        fsim_sim *h = m[q];
+        SolidArgs S;
+        S.pos = h->s_pos[ps];
+        S.vel = h->s_vel[ps];
+        S.ref = h->s_ref[ps];
+        S.type = h->s_type[ps];
+        S.cell = h->s_cell;
+        S.start_s = h->s_start;
+        S.np = h->s_np;
+        S.F = h->s_F;
+        S.Pk = h->s_P;
+        S.L = h->s_L;
+        S.PL = h->s_PL;
+        S.AV = h->s_AV;
+        S.dudt = h->s_dudt;
+        S.couple = h->s_couple;
+        S.fposr = h->f_posr[pf];
+        S.fvelp = h->f_velp[pf];
+        S.start_f = h->f_start;
+        S.n = h->ns;
+        S.orig = h->s_orig[ps];
+        S.inv = h->s_inv;
+        S.nbr_off = h->s_nbr_off;
+        S.nbr_orig = h->s_nbr_orig;
+        S.nbr_dXw = h->s_nbr_dXw;
+        S.cxyz = h->s_cxyz;
+        S.nsub = h->ns ? h->cfg.solid_sub_step : 0;
+        S.flags = h->d_flags;
+        it.push_back({h->P, S});
+        tw[q + 1] = tw[q] + (h->ns ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
+        tt[q + 1] = tt[q] + (h->ns ? blocks_for(h->ns, kBlock) : 0);
     }
+    const bool mixed = !m.empty() && m[0]->mixed;
+    if (m.empty() || !m[0]->cfg.solid_fused) {
+        // one batched launch per phase per sub-step; an instance takes part in
+        // the sub-steps it has
+        for (int k = 0; k < max_sub; ++k) {
+            std::vector<int> wb, tb;
+            for (fsim_sim *h : m) {
+                const bool active = h->ns && k < h->cfg.solid_sub_step;
+                wb.push_back(active ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
+                tb.push_back(active ? blocks_for(h->ns, kBlock) : 0);
+            }
+            add_launch(pl, ab, mixed ? L_DEFORM_M : L_DEFORM, it, wb);
+            add_launch(pl, ab, mixed ? L_FORCE_M : L_FORCE, it, wb);
+            add_launch(pl, ab, L_UPDATE, it, tb);
+        }
+        return;
+    }
+    Launch L{};
+    L.kind = L_SOLID_FUSED;
+    L.items_off = ab.put(it.data(), sizeof(Item<SolidArgs>) * it.size());
+    L.table_off = ab.put(tw.data(), sizeof(int) * tw.size());
+    L.table2_off = ab.put(tt.data(), sizeof(int) * tt.size());
+    const GridBarrier zero{0u, 0u};
+    L.barrier_off = ab.put(&zero, sizeof zero);
+    L.ninst = (int)it.size();
+    L.blocks = fused_grid(mixed, std::max(tw.back(), tt.back()));
+    L.variant = mixed ? 1 : 0;
+    L.max_sub = max_sub;
+    pl.launches.push_back(L);
 }
 
 // phases: bit k = FSIM_PHASE k
@@ -2730,6 +2857,30 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
         case L_VIRT_M: FSIM_LAUNCH(kb_virt_mixed, VirtArgs, kBlock); break;
         case L_DEFORM_M: FSIM_LAUNCH(kb_solid_deform_mixed, SolidArgs, kBlock); break;
         case L_FORCE_M: FSIM_LAUNCH(kb_solid_force_mixed, SolidArgs, kBlock); break;
+        case L_SOLID_FUSED: {
+            SolidFusedArgs F;
+            F.bstart_w = tb;
+            F.bstart_t = reinterpret_cast<const int *>(pl.arena + L.table2_off);
+            F.ninst = n;
+            F.max_sub = L.max_sub;
+            F.barrier = reinterpret_cast<GridBarrier *>(pl.arena + L.barrier_off);
+            CK(cudaMemsetAsync(F.barrier, 0, sizeof(GridBarrier), st));
+            cudaLaunchConfig_t lc = {};
+            lc.gridDim = dim3((unsigned)g);
+            lc.blockDim = dim3(kBlock);
+            lc.stream = st;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            lc.attrs = attr;
+            lc.numAttrs = 1;
+            const Item<SolidArgs> *items = items_of<SolidArgs>(pl, L);
+            if (L.variant)
+                CK(cudaLaunchKernelEx(&lc, kb_solid_fused<true>, items, F));
+            else
+                CK(cudaLaunchKernelEx(&lc, kb_solid_fused<false>, items, F));
+            break;
+        }
         default: fsim_set_error("unknown launch kind"); return FSIM_EINVAL;
         }
         CK_LAUNCH();
@@ -2835,9 +2986,13 @@ fsim_status check_flags(fsim_sim *h)
     unsigned flags = 0;
     CK(cudaMemcpyAsync(&flags, h->d_flags, sizeof flags, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    if (flags) CK(cudaMemsetAsync(h->d_flags, 0, sizeof(unsigned), h->stream));
+    if (flags & FLAG_BARRIER_TIMEOUT) {
+        fsim_set_error("a grid barrier of the solid sub-step kernel gave up waiting (results invalid)");
+        return FSIM_ETIMEOUT;
+    }
     if (flags & FLAG_OUT_OF_GRID) {
         fsim_set_error("a particle position fell outside the cell grid (clamped)");
-        CK(cudaMemsetAsync(h->d_flags, 0, sizeof(unsigned), h->stream));
         return FSIM_ENUMERIC;
     }
     return FSIM_OK;
@@ -4358,8 +4513,9 @@ extern "C" fsim_status fsim_batch_create(fsim_handle *members, int n, fsim_batch
             fsim_set_error("batch members must be distinct standalone handles on one device");
             return FSIM_EINVAL;
         }
-        if (members[k]->mixed != members[0]->mixed) {
-            fsim_set_error("batch members must share the precision form");
+        if (members[k]->mixed != members[0]->mixed ||
+            members[k]->cfg.solid_fused != members[0]->cfg.solid_fused) {
+            fsim_set_error("batch members must share the precision form and the solid launch form");
             return FSIM_EINVAL;
         }
         for (int j = 0; j < k; ++j)

@@ -88,6 +88,9 @@ typedef struct fsim_config {
     /* extension keys (a [gb300] section the reference ignores) */
     int   precision;                /* FSIM_PRECISION_*                       */
     int   keep_derivatives;         /* 1: keep drho_dt/du_dt readable         */
+    int   solid_fused;              /* 1: all solid sub-steps of a step in one
+                                       persistent cooperative launch (else one
+                                       launch per phase per sub-step)         */
 } fsim_config;
 
 /* Derived constants, as Parameter::initiateParameter computes them in FP32

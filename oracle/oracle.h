@@ -38,6 +38,7 @@ typedef struct orc_config {
     int   thread_num;
     int   precision;
     int   keep_derivatives;
+    int   solid_fused; /* device launch choice; no effect on the oracle */
 } orc_config;
 
 typedef struct orc_derived {

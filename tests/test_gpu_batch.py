@@ -105,3 +105,42 @@ def test_member_status_is_per_instance():
         assert b.sync_members() == [api.OK, api.OK, api.OK]  # clamped back into the domain
     for s in sims:
         s.close()
+
+
+def test_fused_solid_launch_matches_standalone_and_oracle_policy():
+    """solid_fused: all solid sub-steps of a step in one persistent cooperative
+    launch.  Batch members still equal their standalone runs bit for bit, and
+    the state stays within the FP32 parity policy of the per-phase launches."""
+    members = _members()
+    for cfg, _ in members:
+        cfg.solid_fused = 1
+    alone = []
+    for cfg, pa in members:
+        with api.Simulation(cfg, pa, device=0) as s:
+            s.step(7)
+            s.sync()
+            alone.append(_fields(s))
+    sims = [api.Simulation(cfg, pa, device=0) for cfg, pa in members]
+    with api.Batch(sims) as b:
+        b.step(7)
+        b.sync()
+        assert b.launches_per_step() <= 15  # the solid sub-steps are one launch
+        batched = [_fields(s) for s in sims]
+    for k, (a, c) in enumerate(zip(alone, batched)):
+        for f in a:
+            assert np.array_equal(a[f], c[f]), (k, f)
+    # against the per-phase launches: the same physics up to FP32 rounding
+    cfg, pa = members[0]
+    ref_cfg = api.Config.from_buffer_copy(cfg)
+    ref_cfg.solid_fused = 0
+    with api.Simulation(ref_cfg, pa, device=0) as r:
+        r.step(7)
+        r.sync()
+        for f in ("solid_pos", "fluid_pos", "fluid_rho"):
+            assert np.allclose(r.get(f), alone[0][f], rtol=1e-5, atol=1e-7), f
+    # a batch takes one solid launch form
+    plain = api.Simulation(ref_cfg, pa, device=0)
+    with pytest.raises(api.FsimError):
+        api.Batch([sims[0], plain])
+    for s in sims + [plain]:
+        s.close()

@@ -128,6 +128,8 @@ def test_extension_keys_ignored_by_reference_semantics():
     g, text = _load("small_dam_break")
     cfg = api.config_from_ini_text(text + "\n[gb300]\ngb300_precision = mixed\ngb300_keep_derivatives = yes\n")
     assert cfg.precision == api.PRECISION_MIXED and cfg.keep_derivatives == 1
+    cfg = api.config_from_ini_text(text + "\n[gb300]\ngb300_solid_fused = yes\n")
+    assert cfg.solid_fused == 1 and cfg.precision == api.PRECISION_FP32
     base = api.config_from_ini_text(text)
     for k in RAW_FLOAT + RAW_INT:
         assert getattr(cfg, k) == getattr(base, k)
