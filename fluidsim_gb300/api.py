@@ -153,6 +153,8 @@ def load():
         "fsim_create_case": (C.c_int, [P, P, C.c_int, C.POINTER(P)]),
         "fsim_case_counts": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "fsim_get_fields": (C.c_int, [P, C.c_int, P, P, P]),
+        "fsim_batch_add": (C.c_int, [P, P]),
+        "fsim_batch_remove": (C.c_int, [P, P]),
         "fsim_set_fields": (C.c_int, [P, C.c_int, P, P, P]),
         "fsim_snapshot_save": (C.c_int, [P, C.c_longlong, P, C.c_size_t]),
         "fsim_snapshot_load": (C.c_int, [P, C.c_size_t, C.c_int, C.POINTER(P), C.POINTER(C.c_longlong)]),
@@ -192,7 +194,7 @@ EXPORTED = [
     "fsim_measure_fp32_peak", "fsim_sweep_tuning", "fsim_batch_sweep_tuning", "fsim_snapshot_bytes",
     "fsim_snapshot_save", "fsim_snapshot_load", "fsim_snapshot_write", "fsim_snapshot_read", "fsim_probe",
     "fsim_write_vtk_binary", "fsim_batch_sync_members", "fsim_create_case", "fsim_case_counts",
-    "fsim_get_fields", "fsim_set_fields",
+    "fsim_get_fields", "fsim_set_fields", "fsim_batch_add", "fsim_batch_remove",
 ]
 SWEEP_SHAPES = ((4, 48), (4, 32), (8, 32))  # (warps per block, list capacity) per shape index
 
@@ -579,6 +581,16 @@ class Batch:
         n = C.c_int()
         check(self.lib.fsim_batch_launches_per_step(self.b, C.byref(n)))
         return n.value
+
+    def add(self, sim):
+        """Admit a standalone Simulation into the live batch."""
+        check(self.lib.fsim_batch_add(self.b, sim.h))
+        self.sims.append(sim)
+
+    def remove(self, sim):
+        """Let a member leave; it continues standalone."""
+        check(self.lib.fsim_batch_remove(self.b, sim.h))
+        self.sims.remove(sim)
 
     def sync_members(self):
         """Wait for the batch; the status code of every member (OK, or ENUMERIC

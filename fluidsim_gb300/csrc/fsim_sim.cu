@@ -4479,6 +4479,7 @@ void free_batch(fsim_batch *b)
 
 fsim_status batch_step_once(fsim_batch *b)
 {
+    if (b->members.empty()) return FSIM_OK;
     const int pf = b->members[0]->f_cur, ps = b->members[0]->s_cur;
     Plan *&pl = b->plans[pf][ps];
     if (!pl) {
@@ -4569,9 +4570,61 @@ extern "C" fsim_status fsim_batch_sync(fsim_batch_t b)
     return batch_check_flags(b);
 }
 
+namespace {
+void drop_batch_plans(fsim_batch *b)
+{
+    for (auto &row : b->plans)
+        for (Plan *&pl : row) {
+            free_plan(pl);
+            pl = nullptr;
+        }
+}
+} // namespace
+
+extern "C" fsim_status fsim_batch_add(fsim_batch_t b, fsim_handle h)
+{
+    if (!b || !h) return FSIM_EINVAL;
+    if (h->batch || h->device != b->device) {
+        fsim_set_error("a batch member must be a standalone handle on the batch's device");
+        return FSIM_EINVAL;
+    }
+    if (!b->members.empty() && (h->mixed != b->members[0]->mixed ||
+                                h->cfg.solid_fused != b->members[0]->cfg.solid_fused)) {
+        fsim_set_error("batch members must share the precision form and the solid launch form");
+        return FSIM_EINVAL;
+    }
+    DeviceGuard guard(b->device);
+    CK(cudaStreamSynchronize(b->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    const int pf = b->members.empty() ? 0 : b->members[0]->f_cur;
+    const int ps = b->members.empty() ? h->s_cur : b->members[0]->s_cur;
+    fsim_status st = set_parity(h, pf, ps);
+    if (st) return st;
+    drop_batch_plans(b); // rebuilt (and recaptured) at the next step; the tuned sweep shape is kept
+    b->members.push_back(h);
+    h->batch = b;
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_batch_remove(fsim_batch_t b, fsim_handle h)
+{
+    if (!b || !h) return FSIM_EINVAL;
+    auto it = std::find(b->members.begin(), b->members.end(), h);
+    if (it == b->members.end()) {
+        fsim_set_error("the handle is not a member of this batch");
+        return FSIM_EINVAL;
+    }
+    DeviceGuard guard(b->device);
+    CK(cudaStreamSynchronize(b->stream));
+    drop_batch_plans(b);
+    b->members.erase(it);
+    h->batch = nullptr;
+    return FSIM_OK;
+}
+
 extern "C" fsim_status fsim_batch_sync_members(fsim_batch_t b, int *status, int n)
 {
-    if (!b || !status || n != (int)b->members.size()) return FSIM_EINVAL;
+    if (!b || (n && !status) || n != (int)b->members.size()) return FSIM_EINVAL;
     DeviceGuard guard(b->device);
     CK(cudaStreamSynchronize(b->stream));
     for (int k = 0; k < n; ++k) status[k] = check_flags(b->members[k]);
@@ -4596,6 +4649,8 @@ extern "C" fsim_status fsim_batch_time_steps(fsim_batch_t b, int nsteps, float *
 extern "C" fsim_status fsim_batch_launches_per_step(fsim_batch_t b, int *n)
 {
     if (!b || !n) return FSIM_EINVAL;
+    *n = 0;
+    if (b->members.empty()) return FSIM_OK;
     DeviceGuard guard(b->device);
     const int pf = b->members[0]->f_cur, ps = b->members[0]->s_cur;
     Plan *&pl = b->plans[pf][ps];

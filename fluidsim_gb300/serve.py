@@ -95,6 +95,12 @@ class GpuBackend:
     def batch(self, instances):
         return api.Batch(instances)
 
+    def add(self, batch, inst):
+        batch.add(inst)
+
+    def remove(self, batch, inst):
+        batch.remove(inst)
+
     def result(self, inst):
         return _result_fields(inst)
 
@@ -146,8 +152,9 @@ class Server:
         reqs = sorted(requests, key=lambda r: r.arrival)
         waiting, active = [], []  # active entries: [request, instance, steps left, bytes]
         prepared = {}
-        st = {"nxt": 0, "used": 0, "load": 0, "completed": 0, "failed": 0, "work": 0, "rebuilds": 0}
-        batch = None
+        st = {"nxt": 0, "used": 0, "load": 0, "completed": 0, "failed": 0, "work": 0, "rebuilds": 0, "joins": 0,
+              "leaves": 0}
+        batch, batch_members = None, []
         t0 = clock()
 
         def close_request(r, now, event, error=""):
@@ -177,6 +184,9 @@ class Server:
                     close_request(r, now, "cancelled", "cancelled")
                 for a in [a for a in active if a[0].rid in self._cancel]:
                     active.remove(a)
+                    if batch is not None:
+                        batch.close()
+                        batch = None
                     retire(a, now, "cancelled")
                     changed = True
             while waiting:
@@ -208,10 +218,20 @@ class Server:
                 if st["nxt"] < len(reqs):
                     sleep(max(0.0, min(0.05, reqs[st["nxt"]].arrival - (clock() - t0))))
                 continue
+            if batch is not None and changed and hasattr(be, "add"):
+                # keep the live batch: admit the new members into it
+                current = list(batch_members)
+                for a in active:
+                    if not any(a[1] is c for c in current):
+                        be.add(batch, a[1])
+                        batch_members.append(a[1])
+                        st["joins"] += 1
+                changed = False
             if changed or batch is None:
                 if batch is not None:
                     batch.close()
                 batch = be.batch([a[1] for a in active])
+                batch_members = [a[1] for a in active]
                 st["rebuilds"] += 1
             k = min(self.quantum, min(a[2] for a in active))
             batch.step(k)
@@ -227,8 +247,15 @@ class Server:
                 if a[2] == 0:
                     finished.append(a)
             if finished or broken:
-                batch.close()
-                batch = None
+                leaving = finished + [a for a, _ in broken]
+                if hasattr(be, "remove") and len(leaving) < len(active):
+                    for a in leaving:
+                        be.remove(batch, a[1])
+                        batch_members = [c for c in batch_members if c is not a[1]]
+                        st["leaves"] += 1
+                else:
+                    batch.close()
+                    batch = None
                 for a in finished:
                     retire(a, now)
                 for a, code in broken:
@@ -241,7 +268,8 @@ class Server:
         lat = [r.done_at - r.arrival for r in reqs if not r.error]
         return {"requests": len(reqs), "makespan_s": makespan, "particle_updates": st["work"],
                 "throughput": st["work"] / makespan, "p50_latency_s": _percentile(lat, 50),
-                "p99_latency_s": _percentile(lat, 99), "batch_rebuilds": st["rebuilds"], "failed": st["failed"]}
+                "p99_latency_s": _percentile(lat, 99), "batch_rebuilds": st["rebuilds"],
+                "batch_joins": st["joins"], "batch_leaves": st["leaves"], "failed": st["failed"]}
 
 
 def serve_one_by_one(requests, device=0, clock=time.perf_counter, keep_results=False):

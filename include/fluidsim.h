@@ -328,6 +328,12 @@ fsim_status fsim_batch_time_steps(fsim_batch_t b, int nsteps, float *ms);
 fsim_status fsim_batch_launches_per_step(fsim_batch_t b, int *n);
 /* The batch's own sweep autotuner (see fsim_sweep_tuning). */
 fsim_status fsim_batch_sweep_tuning(fsim_batch_t b, int *chosen, float *ms, int n);
+/* Change the membership of a live batch: a standalone handle joins (same
+ * device, precision form and solid launch form), or a member leaves and
+ * continues standalone.  The batch's step plans are rebuilt at its next step;
+ * its tuned sweep shape is kept.  A batch may become empty. */
+fsim_status fsim_batch_add(fsim_batch_t b, fsim_handle h);
+fsim_status fsim_batch_remove(fsim_batch_t b, fsim_handle h);
 /* Dissolve the batch; the members continue as standalone handles. */
 fsim_status fsim_batch_destroy(fsim_batch_t b);
 

@@ -144,3 +144,38 @@ def test_fused_solid_launch_matches_standalone_and_oracle_policy():
         api.Batch([sims[0], plain])
     for s in sims + [plain]:
         s.close()
+
+
+def test_add_and_remove_members_of_a_live_batch():
+    """Members join and leave a live batch; every member's trajectory still
+    equals its standalone run bit for bit."""
+    members = _members()
+    ref = []
+    for cfg, pa in members:
+        with api.Simulation(cfg, pa, device=0) as s:
+            s.step(9)
+            s.sync()
+            ref.append(_fields(s))
+    sims = [api.Simulation(cfg, pa, device=0) for cfg, pa in members]
+    b = api.Batch(sims[:1])
+    b.step(3)
+    sims[1].step(3)        # standalone for a while, then joins
+    b.add(sims[1])
+    b.step(3)
+    b.add(sims[2])         # joins fresh: 3 batched steps, then 6 alone
+    b.remove(sims[0])      # leaves after 6 steps, continues alone
+    sims[0].step(3)
+    b.step(3)
+    b.remove(sims[1])
+    b.remove(sims[2])
+    assert b.launches_per_step() == 0  # empty batch
+    b.step(1)
+    sims[2].step(6)
+    b.close()
+    for s in sims:
+        s.sync()
+    for k, s in enumerate(sims):
+        got = _fields(s)
+        for f, want in ref[k].items():
+            assert np.array_equal(got[f], want), (k, f)
+        s.close()

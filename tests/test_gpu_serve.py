@@ -17,7 +17,8 @@ def _stream():
 def test_served_results_equal_solo():
     mixed = _stream()
     out = serve.Server(budget_bytes=2 ** 36, quantum=3, keep_results=True).run(mixed)
-    assert out["requests"] == 5 and out["batch_rebuilds"] >= 2
+    # requests joined and left the live batch while it ran
+    assert out["requests"] == 5 and out["batch_rebuilds"] + out["batch_joins"] >= 2 and out["batch_leaves"] >= 1
     solo = _stream()
     serve.serve_one_by_one(solo, keep_results=True)
     for a, b in zip(mixed, solo):
