@@ -163,14 +163,34 @@ struct HashArgs {
     int *key, *slot, *cnt;
     unsigned *flags;
 };
+// A slot in cell c's count: lanes of a warp with the same cell share one
+// atomic (particles arrive sorted by their previous cell, so a warp holds few
+// distinct cells).  Slots only need to be distinct within a cell: the gather
+// orders a cell's particles by their previous position.  All lanes call it.
+__device__ __forceinline__ int cell_slot(int *cnt, int c, bool active)
+{
+    const unsigned act = __ballot_sync(kFull, active);
+    if (!active) return 0;
+    const unsigned peers = __match_any_sync(act, c);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&cnt[c], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 __device__ __forceinline__ void hash_body(const DevParams &P, const HashArgs &A, int blk)
 {
     const int s = blk * blockDim.x + threadIdx.x;
-    if (s >= A.n) return;
-    const float4 p = A.pos[s];
-    const int c = cell_index(P, p.x, p.y, p.z, A.flags);
-    A.key[s] = c;
-    A.slot[s] = atomicAdd(&A.cnt[c], 1);
+    const bool active = s < A.n;
+    int c = 0;
+    if (active) {
+        const float4 p = A.pos[s];
+        c = cell_index(P, p.x, p.y, p.z, A.flags);
+        A.key[s] = c;
+    }
+    const int slot = cell_slot(A.cnt, c, active);
+    if (active) A.slot[s] = slot;
 }
 FSIM_BATCHED_KERNEL(kb_hash, HashArgs, hash_body, kBlock)
 
@@ -920,19 +940,23 @@ struct HashMixedArgs {
 __device__ __forceinline__ void hash_mixed_body(const DevParams &P, const HashMixedArgs &A, int blk)
 {
     const int s = blk * blockDim.x + threadIdx.x;
-    if (s >= A.n) return;
-    float4 p = A.pos[s];
-    int cx, cy, cz;
-    cell_xyz(P, A.cell_old[s], cx, cy, cz);
-    bool bad = false;
-    cx = rebin_axis(p.x, cx, P.cinv[0], P.cdx[0], P.nx, bad);
-    cy = rebin_axis(p.y, cy, P.cinv[1], P.cdx[1], P.ny, bad);
-    cz = rebin_axis(p.z, cz, P.cinv[2], P.cdx[2], P.nz, bad);
-    if (bad) atomicOr(A.flags, FLAG_OUT_OF_GRID);
-    const int c = (cx * P.ny + cy) * P.nz + cz;
-    A.pos[s] = p;
-    A.key[s] = c;
-    A.slot[s] = atomicAdd(&A.cnt[c], 1);
+    const bool active = s < A.n;
+    int c = 0;
+    if (active) {
+        float4 p = A.pos[s];
+        int cx, cy, cz;
+        cell_xyz(P, A.cell_old[s], cx, cy, cz);
+        bool bad = false;
+        cx = rebin_axis(p.x, cx, P.cinv[0], P.cdx[0], P.nx, bad);
+        cy = rebin_axis(p.y, cy, P.cinv[1], P.cdx[1], P.ny, bad);
+        cz = rebin_axis(p.z, cz, P.cinv[2], P.cdx[2], P.nz, bad);
+        if (bad) atomicOr(A.flags, FLAG_OUT_OF_GRID);
+        c = (cx * P.ny + cy) * P.nz + cz;
+        A.pos[s] = p;
+        A.key[s] = c;
+    }
+    const int slot = cell_slot(A.cnt, c, active);
+    if (active) A.slot[s] = slot;
 }
 FSIM_BATCHED_KERNEL(kb_hash_mixed, HashMixedArgs, hash_mixed_body, kBlock)
 
@@ -1902,7 +1926,7 @@ __device__ __forceinline__ void grid_sync(GridBarrier *b, bool &ok)
 }
 
 struct SolidFusedArgs {
-    const int *bstart_w, *bstart_t; // prefix tables: 4 lanes per particle / thread per particle
+    const int *bstart_w, *bstart_t; // prefix tables: kSolidGroup lanes per particle / thread per particle
     int ninst, max_sub;
     GridBarrier *barrier;
 };
