@@ -5,6 +5,13 @@
  * FP64 oracle) or, with -DORACLE_F32, REAL = float.  Always compiled with
  * -ffp-contract=off so that the FP32 helpers below round exactly as written.
  *
+ * Parity: partially pinned.  The configuration parsing, derived constants and
+ * cell grid are pinned against the reference's own host sources compiled here
+ * (oracle/build.py -> oracle/_ref, fixtures in tests/golden).  The pair
+ * physics of src/fluid.cu, src/virt.cu and src/solid.cu needs the glm library,
+ * which the reference neither vendors nor pins, so that part is restated from
+ * the formulas and is unpinned.
+ *
  * Every function cites the reference code it restates (paths within
  * niji127/FluidSim).  Differences from the reference that are deliberate:
  *   - Cell lists are rebuilt from scratch every step (counting sort, ascending
