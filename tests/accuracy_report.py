@@ -76,12 +76,26 @@ def main():
             pos = f.endswith("_pos")
             row[f] = {"plain": field_errors(plain.get(f), want, dx if pos else 0.0),
                       "mixed": field_errors(mixed.get(f), want, dx if pos else 0.0)}
+        # where the largest fluid errors sit: distance of the worst particles to the nearest domain wall
+        lo = np.array([cfg_p.xmin, cfg_p.ymin, cfg_p.zmin])
+        hi = np.array([cfg_p.xmax, cfg_p.ymax, cfg_p.zmax])
+        pos = ref.get("fluid_pos")
+        wall = np.minimum(pos - lo, hi - pos).min(1) / dx
+        for f in ("fluid_vel", "fluid_p"):
+            want = ref.get(f)
+            for form, sim in (("plain", plain), ("mixed", mixed)):
+                d = np.abs(np.asarray(sim.get(f), np.float64) - want)
+                d = d.reshape(len(d), -1).max(1)
+                top = np.argsort(d)[-5:][::-1]
+                row[f][form]["worst_wall_dist_dx"] = [float(wall[k]) for k in top]
+                row[f][form]["share_of_max_err_within_3dx_of_wall"] = float(
+                    (d[wall < 3.0] > 0.5 * d.max()).sum() / max(1, (d > 0.5 * d.max()).sum()))
         report["checkpoints"][str(c)] = row
         print("step %d (%.0f s)" % (c, time.perf_counter() - t0), flush=True)
         for f, e in row.items():
-            print("  %-10s plain max %.3g rms %.3g | mixed max %.3g rms %.3g" % (
-                f, e["plain"]["max_rel"], e["plain"]["rms_rel"], e["mixed"]["max_rel"], e["mixed"]["rms_rel"]),
-                flush=True)
+            print("  %-10s plain max %.3g rms %.3g | mixed max %.3g rms %.3g %s" % (
+                f, e["plain"]["max_rel"], e["plain"]["rms_rel"], e["mixed"]["max_rel"], e["mixed"]["rms_rel"],
+                e["mixed"].get("worst_wall_dist_dx", "")), flush=True)
         if args.json:
             with open(args.json, "w") as fh:
                 json.dump(report, fh, indent=1)
