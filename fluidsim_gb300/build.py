@@ -20,7 +20,7 @@ CLI = os.path.join(BUILD, "fluidsim")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_UNITS = ["fsim_sim.cu", "fsim_noalloc.cu", "fsim_probe.cu"]
+CUDA_UNITS = ["fsim_kernels.cu", "fsim_sim.cu", "fsim_noalloc.cu", "fsim_probe.cu"]
 HOST_UNITS = ["fsim_host.cpp"]
 HEADERS = ["fsim_internal.h"]
 

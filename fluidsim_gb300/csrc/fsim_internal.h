@@ -1,5 +1,5 @@
 // fsim_internal.h — declarations shared by the host (fsim_host.cpp) and the
-// device side (fsim_sim.cu) of the library.  Not part of the public ABI.
+// device side (fsim_sim.cu, fsim_kernels.cu) of the library.  Not part of the public ABI.
 #pragma once
 
 #include "../../include/fluidsim.h"

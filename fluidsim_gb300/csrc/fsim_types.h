@@ -1,0 +1,381 @@
+// fsim_types.h — what the device kernels (fsim_kernels.cu) and the host side
+// of the library (fsim_sim.cu) share: the device parameters of an instance,
+// the argument block of every batched launch, the plans that list a step's
+// launches, and the launch entry points of fsim_kernels.cu.  Internal; not
+// part of the public ABI (include/fluidsim.h).
+#pragma once
+
+#include "fsim_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+namespace fsim_rt {
+
+struct DevParams {
+    // kernel (src/kernel.cpp:43-60)
+    float R2, h, h_inv2, kdiff, kc1, kc2, eps_h2, exp2_scale;
+    // fluid (src/properties.cpp:47-57)
+    float c0, c0_inv, rho0, rho0_inv, gamma, rho2p, min_p, min_rho, max_rho, mu10, vmax;
+    int viscid;
+    // solid (src/properties.cpp:59-66)
+    float rho_s_inv, lambda, mu_s, cs_s, alpha, beta;
+    // physics, time
+    float gx, gy, gz, dt, dt_sub;
+    // domain
+    float dmin[3], dmax[3], cmin[3], cinv[3];
+    int nx, ny, nz, ncell;
+    // mixed form: cell size, domain bounds relative to the grid origin,
+    // density-deviation clamp, FP16 scales of the gathered deviations
+    float cdx[3], dlo_rel[3], dhi_rel[3];
+    float dlt_min, dlt_max, p_unit, p_unit_inv;
+    int mixed;
+};
+
+// per-instance error flags (device word, read by check_flags)
+enum : unsigned { FLAG_OUT_OF_GRID = 1u, FLAG_BARRIER_TIMEOUT = 2u };
+
+constexpr int kBlock = 256;         // threads per block of the element-wise and solid kernels
+constexpr int kScanThreads = 1024;  // cell-count scan: threads per block
+constexpr int kScanItems = 4;       //   and counts per thread
+constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int kMaxScanTiles = 16384; // cell grids up to 67M cells
+
+__host__ __device__ inline int blocks_for(long long n, int b) { return (int)((n + b - 1) / b); }
+
+// One instance's share of a batched launch: its parameters and buffers.
+template <class Args>
+struct Item {
+    DevParams P;
+    Args A;
+};
+
+// ---- argument blocks of the batched kernels (one Item per instance)
+// cell phase: hash (plain / mixed), count reset, scans, scatter, gathers
+struct HashArgs {
+    const float4 *pos;
+    int n;
+    int *key, *slot, *cnt;
+    unsigned *flags;
+};
+
+struct ZeroArgs {
+    int *p;
+    int n;
+};
+
+struct ScanArgs {
+    const int *in;
+    int *out;
+    int n;
+    int *partial;
+};
+
+struct ScatterArgs {
+    const int *key, *slot, *start;
+    int *tmp;
+    int n;
+};
+
+struct GatherFluidArgs {
+    const int *tmp, *key, *start;
+    int n;
+    const float4 *posr_in, *velp_in;
+    const int *orig_in;
+    float4 *posr_out, *velp_out;
+    int *orig_out, *cell_out;
+};
+
+struct GatherSolidArgs {
+    const int *tmp, *key, *start;
+    int n;
+    const float4 *pos_in, *vel_in, *ref_in;
+    const int *type_in, *orig_in;
+    float4 *pos_out, *vel_out, *ref_out;
+    int *type_out, *orig_out, *cell_out;
+    int *inv_out;       // sorted position of every input id
+    unsigned *cxyz_out; // cell coordinates packed x | y << 11 | z << 21
+};
+
+// fused fluid sweep + update (plain and mixed)
+struct FluidSweepArgs {
+    const float4 *posr, *velp;   // sorted step-start state
+    const int *start_f, *cell_f, *orig_in;
+    const float4 *s_pos, *s_vel, *s_np; // solid position, velocity, (normal, pressure)
+    const int *start_s;
+    const float4 *v_posr, *v_velp;
+    const int *start_v;
+    float4 *posr_out, *velp_out;
+    int *orig_out;
+    float *drho_out;
+    float4 *dudt_out;
+    int n;
+    int keep; // write drho/dt and du/dt
+    const float2 *cm; // mixed form: per-cell (density deviation, pressure) references
+};
+
+// wall particles' data from their nearest fluid particle
+struct VirtArgs {
+    const float4 *v_posr_in, *v_normal;
+    const int *v_cell;
+    const float4 *fposr, *fvelp;
+    const int *forig, *start_f;
+    float4 *v_posr, *v_velp;
+    int n;
+};
+
+// solid normal and Shepard pressure
+struct CoupleArgs {
+    const float4 *s_pos;
+    const int *s_cell, *start_s;
+    const float4 *fposr, *fvelp;
+    const int *start_f;
+    float4 *s_np;
+    int n;
+};
+
+// mixed form: re-binning hash, per-cell references of the FP16 gather
+struct HashMixedArgs {
+    float4 *pos;
+    const int *cell_old;
+    int n;
+    int *key, *slot, *cnt;
+    unsigned *flags;
+};
+
+struct CellRefArgs {
+    float4 *posr;
+    const float4 *velp;
+    const int *start;
+    float2 *cm;
+    int ncell;
+};
+
+// solid sub-step kernels (deformation, force, update, fused)
+struct SolidArgs {
+    float4 *pos, *vel;
+    const float4 *ref;
+    const int *type, *cell, *start_s;
+    const float4 *np;
+    float *F, *Pk, *L, *PL, *AV; // 9 floats per particle, row-major
+    float4 *dudt, *couple;
+    const float4 *fposr, *fvelp;
+    const int *start_f;
+    int n;
+    // static reference-configuration neighbours (CSR over input ids)
+    const int *orig, *inv, *nbr_off, *nbr_orig;
+    const float4 *nbr_dXw; // (X_j - X_i, kernel weight)
+    const unsigned *cxyz;
+    int nsub;              // this instance's solid sub-steps per step
+    unsigned *flags;       // this instance's error flags
+};
+
+// ---- device case generator (fsim_create_case): lattice rows and their bases
+struct CaseGeom {
+    int T[3], FN[3], SL[3], SN[3];
+    int fixed_layers, L;
+    int has_solid, jitter;
+    double dx, jit;
+    uint64_t seed;
+};
+
+struct RowIv {
+    int s0, s1;   // solid sites [s0, s1)
+    int f0, f1;   // fluid block sites [f0, f1) (before removing solid)
+    int inside;   // the row lies inside the tank in i and j
+    int fixed;    // solid sites of this row are FIXED (below the floor)
+};
+
+__host__ __device__ inline void case_row(const CaseGeom &g, int i, int j, RowIv &r)
+{
+    r.inside = !(i < 0 || i >= g.T[0] || j < 0 || j >= g.T[1]);
+    r.fixed = j < 0;
+    const bool solid_ij = g.has_solid && i >= g.SL[0] && i < g.SL[0] + g.SN[0] && j >= g.SL[1] - g.fixed_layers &&
+                          j < g.SL[1] + g.SN[1];
+    r.s0 = r.s1 = 0;
+    if (solid_ij) {
+        int lo = g.SL[2], hi = g.SL[2] + g.SN[2];
+        if (j >= 0) { // above the floor a solid site must be inside the tank
+            if (!r.inside) hi = lo;
+            lo = lo > 0 ? lo : 0;
+            hi = hi < g.T[2] ? hi : g.T[2];
+        }
+        lo = lo > -g.L ? lo : -g.L;
+        hi = hi < g.T[2] + g.L ? hi : g.T[2] + g.L;
+        if (hi > lo) {
+            r.s0 = lo;
+            r.s1 = hi;
+        }
+    }
+    r.f0 = r.f1 = 0;
+    if (r.inside && i < g.FN[0] && j < g.FN[1]) {
+        r.f0 = 0;
+        r.f1 = g.FN[2] < g.T[2] ? g.FN[2] : g.T[2];
+        if (r.f1 < 0) r.f1 = 0;
+    }
+}
+
+__host__ __device__ inline int iv_before(int a, int b, int k) // |[a, b) n (-inf, k)|
+{
+    const int e = b < k ? b : k;
+    return e > a ? e - a : 0;
+}
+
+__host__ __device__ inline int iv_overlap_before(int a, int b, int c, int d, int k)
+{
+    return iv_before(a > c ? a : c, b < d ? b : d, k);
+}
+
+__host__ __device__ inline void case_row_counts(const CaseGeom &g, const RowIv &r, int c[4])
+{
+    const int kend = g.T[2] + g.L;
+    const int ns = r.s1 - r.s0;
+    const int nf = (r.f1 - r.f0) - iv_overlap_before(r.f0, r.f1, r.s0, r.s1, kend);
+    const int nv = r.inside ? 2 * g.L : (g.T[2] + 2 * g.L) - ns;
+    c[0] = nf;
+    c[1] = ns;
+    c[2] = nv;
+    c[3] = g.jitter ? nf + (r.fixed ? 0 : ns) : 0;
+}
+
+struct RowBase {
+    int f, s, v, pad;
+    long long d; // jitter-drawing sites before the row
+};
+
+struct CaseGenArgs {
+    CaseGeom g;
+    const RowBase *base;
+    const float2 *hydro; // (rho, p) per lattice row j of the fluid block
+    float rho0;
+    float4 *fposr, *fvelp;
+    int *forig;
+    float4 *spos, *svel, *sref;
+    int *stype, *sorig;
+    float4 *vpos;
+    long long nsite;
+};
+
+// point probes (fsim_probe)
+struct ProbeArgs {
+    const float *pts;
+    int n;
+    float *out; // 5 per probe: u, v, w, p, rho
+    const float4 *fposr, *fvelp;
+    const int *start_f;
+    const float4 *s_pos, *s_vel, *s_np;
+    const int *start_s;
+};
+
+// grid barrier of the fused solid kernel
+struct GridBarrier {
+    unsigned count, gen;
+};
+
+// what the mixed-form field (un)permutes move
+enum MixedField { MF_POS = 0, MF_RHO = 1, MF_P = 2 };
+
+// lanes per solid particle in the solid sweeps and the coupling
+constexpr int kSolidGroup = 4;
+
+// mixed sweep: neighbour-list entry = particle index | 6-bit cell code << kCodeShift
+constexpr int kCodeShift = 26;                   // neighbour-list entry = j | cell code << 26
+
+constexpr int kIndexMask = (1 << kCodeShift) - 1;
+
+// launch shapes of the fluid sweep the autotuner chooses among
+constexpr int kSweepShapes = 3;
+
+constexpr int kShapeWarps[kSweepShapes] = {4, 4, 8}; // warps per block of sweep shapes 0..2
+
+// ---------------------------------------------------------------- plans
+// A plan is the ordered list of batched launches that advance a set of
+// instances by one step (or one phase), with every launch's {params, args}
+// items and block prefix tables in one device arena.
+enum LaunchKind {
+    L_ZERO, L_HASH, L_SCAN_REDUCE, L_SCAN_PARTIALS, L_SCAN_APPLY, L_SCATTER, L_GATHER_F, L_GATHER_S,
+    L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE,
+    L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M, L_SOLID_FUSED
+};
+
+struct Launch {
+    int kind;
+    size_t items_off, table_off; // arena offsets
+    int ninst, blocks, variant;
+    size_t shape_table_off[kSweepShapes]; // L_SWEEP: block prefix table per launch shape
+    int shape_blocks[kSweepShapes];
+    size_t table2_off, barrier_off;       // L_SOLID_FUSED: thread-per-particle table, grid barrier
+    int max_sub;
+};
+
+struct Plan {
+    int device = 0;
+    int pf = 0, ps = 0;           // buffer parities at the start
+    int pf_after = 0, ps_after = 0;
+    std::vector<Launch> launches;
+    char *arena = nullptr;
+    std::vector<char> host; // host image of the arena (one-instance launches pass items by value)
+    cudaGraphExec_t graph = nullptr;
+    int sweep_index = -1;         // launch index of the fluid sweep
+};
+
+template <class Args>
+const Item<Args> *items_of(const Plan &pl, const Launch &L)
+{
+    return reinterpret_cast<const Item<Args> *>(pl.arena + L.items_off);
+}
+
+template <class Args>
+const Item<Args> &host_item(const Plan &pl, const Launch &L)
+{
+    return *reinterpret_cast<const Item<Args> *>(pl.host.data() + L.items_off);
+}
+
+// ------------------------------------------------------ host error checks
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            fsim_set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return FSIM_ECUDA;                                                                          \
+        }                                                                                               \
+    } while (0)
+
+#define CK_LAUNCH()                                                                                            \
+    do {                                                                                                       \
+        cudaError_t e_ = cudaGetLastError();                                                                   \
+        if (e_ != cudaSuccess) {                                                                               \
+            fsim_set_error("kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__);    \
+            return FSIM_ECUDA;                                                                                 \
+        }                                                                                                      \
+    } while (0)
+
+// ---------------------------------------------- entry points of the kernels
+// Enqueue a plan's launches on `st`, the fluid sweep with launch shape
+// `shape`; optional events around the sweep.
+fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0 = nullptr,
+                         cudaEvent_t sweep1 = nullptr);
+// CTAs of the fused solid kernel that fit on the current device at once (<= want)
+int fused_grid(bool mixed, int want);
+// One launch of a utility kernel (kBlock threads per block) on `st`.
+void launch_k_pack_f4(int grid, cudaStream_t st, const float *xyz, const float *w, int n, float wconst, float4 *out);
+void launch_k_iota(int grid, cudaStream_t st, int *a, int n);
+void launch_k_virt_normal(int grid, cudaStream_t st, const DevParams P, const float4 *v_posr, const int *v_cell, const int *start_v, float4 *v_normal, int n);
+void launch_k_solid_pair_weights(int grid, cudaStream_t st, const DevParams P, float4 *dXw, int n);
+void launch_k_fluid_to_mixed(int grid, cudaStream_t st, const DevParams P, float4 *posr, float4 *velp, int *cell, int n, unsigned *flags);
+void launch_k_offsets_in_cells(int grid, cudaStream_t st, const DevParams P, float4 *pos, const int *cell, int n);
+void launch_k_unpermute_mixed(int grid, cudaStream_t st, const DevParams P, const float4 *pos, const float4 *velp, const int *cell, const int *orig, int n, int what, float *out);
+void launch_k_unpermute_f4(int grid, cudaStream_t st, const float4 *src, const int *orig, int n, int comp, int width, float *out);
+void launch_k_unpermute_words(int grid, cudaStream_t st, const int *src, const int *orig, int n, int width, int *out);
+void launch_k_permute_in_mixed(int grid, cudaStream_t st, const DevParams P, float4 *pos, float4 *velp, const int *cell, const int *orig, int n, int what, const float *in);
+void launch_k_permute_in_f4(int grid, cudaStream_t st, float4 *dst, const int *orig, int n, int comp, int width, const float *in);
+void launch_k_probe(int grid, cudaStream_t st, const DevParams P, const ProbeArgs A);
+void launch_k_neighbor_counts(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *cell_f, const int *start_f, const float4 *s_pos, const int *start_s, const float4 *v_posr, const int *start_v, int *out, int n);
+void launch_k_conservation_fluid(int grid, cudaStream_t st, const DevParams P, const float4 *posr, const float4 *velp, const int *cell, int n, double vol, double *partials);
+void launch_k_conservation_solid(int grid, cudaStream_t st, const DevParams P, const float4 *pos, const float4 *vel, const float *F, int n, double rho_s, double vol, double *partials);
+void launch_k_case_generate(int grid, cudaStream_t st, const CaseGenArgs A);
+
+} // namespace fsim_rt
