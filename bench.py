@@ -241,6 +241,7 @@ def run_gb300(args, dist):
     step_bytes = (ALG_BYTES_FLUID * pa.n_fluid + pa.n_solid * (ALG_BYTES_SOLID * cfg.solid_sub_step +
                                                                ALG_BYTES_SOLID_STEP) + ALG_BYTES_VIRT * pa.n_virt)
     fp32 = sweep_flop_roofline(api, sim, dev, t_launch)
+    phases = {k: v / args.steps for k, v in sim.time_phases(args.steps).items()}
     traffic = None
     prof = os.path.join(ROOT, "profiles", "fluid_sweep_traffic.json")
     if os.path.exists(prof):
@@ -306,6 +307,7 @@ def run_gb300(args, dist):
                          "step_frac": step_bytes / (ms * 1e-3 / args.steps) / 1e9 / hbm_peak},
             "roofline_fp32": fp32,
             "autotuner": tuning,
+            "phases_ms_per_step": phases,
             "cpu_baseline": cpu,
             "clocks": clk,
             "forms": forms,

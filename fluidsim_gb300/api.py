@@ -154,6 +154,7 @@ def load():
         "fsim_case_counts": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "fsim_get_fields": (C.c_int, [P, C.c_int, P, P, P]),
         "fsim_batch_add": (C.c_int, [P, P]),
+        "fsim_time_phases": (C.c_int, [P, C.c_int, C.POINTER(C.c_float), C.c_int]),
         "fsim_batch_remove": (C.c_int, [P, P]),
         "fsim_set_fields": (C.c_int, [P, C.c_int, P, P, P]),
         "fsim_snapshot_save": (C.c_int, [P, C.c_longlong, P, C.c_size_t]),
@@ -195,6 +196,7 @@ EXPORTED = [
     "fsim_snapshot_save", "fsim_snapshot_load", "fsim_snapshot_write", "fsim_snapshot_read", "fsim_probe",
     "fsim_write_vtk_binary", "fsim_batch_sync_members", "fsim_create_case", "fsim_case_counts",
     "fsim_get_fields", "fsim_set_fields", "fsim_batch_add", "fsim_batch_remove",
+    "fsim_time_phases",
 ]
 SWEEP_SHAPES = ((4, 48), (4, 32), (8, 32))  # (warps per block, list capacity) per shape index
 
@@ -520,6 +522,12 @@ class Simulation:
         n = C.c_int()
         check(self.lib.fsim_launches_per_step(self.h, C.byref(n)))
         return n.value
+
+    def time_phases(self, n):
+        """Device ms per phase over n launch-by-launch steps (fsim_time_phases)."""
+        ms = (C.c_float * 5)()
+        check(self.lib.fsim_time_phases(self.h, n, ms, 5))
+        return dict(zip(("cell", "couple", "virt", "fluid", "solid"), list(ms)))
 
     def sweep_tuning(self):
         """(chosen shape or -1, [ms per shape]) of the sweep autotuner."""

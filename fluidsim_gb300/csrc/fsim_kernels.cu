@@ -2000,7 +2000,8 @@ namespace fsim_rt {
 #define FSIM_LAUNCH(KB, ARGS, THREADS) KB<<<g, THREADS, 0, st>>>(items_of<ARGS>(pl, L), tb, n)
 
 // Enqueue a plan's launches; optional events around the fluid sweep.
-fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0, cudaEvent_t sweep1)
+fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0, cudaEvent_t sweep1,
+                         const cudaEvent_t *per_launch)
 {
     using SweepFn = void (*)(const Item<FluidSweepArgs> *, const int *, int);
     using Sweep1Fn = void (*)(const DevParams, const FluidSweepArgs);
@@ -2029,6 +2030,7 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
         const Launch &L = pl.launches[k];
         const int *tb = reinterpret_cast<const int *>(pl.arena + L.table_off);
         const int g = L.blocks, n = L.ninst;
+        if (per_launch) CK(cudaEventRecord(per_launch[2 * k], st));
         switch (L.kind) {
         case L_ZERO: FSIM_LAUNCH(kb_zero, ZeroArgs, kBlock); break;
         case L_HASH: FSIM_LAUNCH(kb_hash, HashArgs, kBlock); break;
@@ -2091,8 +2093,21 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
         default: fsim_set_error("unknown launch kind"); return FSIM_EINVAL;
         }
         CK_LAUNCH();
+        if (per_launch) CK(cudaEventRecord(per_launch[2 * k + 1], st));
     }
     return FSIM_OK;
+}
+
+int launch_phase(int kind)
+{
+    switch (kind) {
+    case L_COUPLE: case L_COUPLE_M: return FSIM_PHASE_COUPLE;
+    case L_VIRT: case L_VIRT_M: return FSIM_PHASE_VIRT;
+    case L_SWEEP: return FSIM_PHASE_FLUID;
+    case L_DEFORM: case L_FORCE: case L_UPDATE: case L_DEFORM_M: case L_FORCE_M: case L_SOLID_FUSED:
+        return FSIM_PHASE_SOLID;
+    default: return FSIM_PHASE_CELL;
+    }
 }
 
 // CTAs of the fused solid kernel that can be resident at once on the current

@@ -6,6 +6,7 @@
 #include "fsim_types.h"
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <climits>
@@ -17,6 +18,14 @@
 #include <vector>
 
 using namespace fsim_rt;
+
+namespace {
+// NVTX range over an API call (visible to Nsight tools; free without them)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+} // namespace
 
 // =================================================================== handle
 namespace {
@@ -985,6 +994,7 @@ fsim_status new_handle(const fsim_config *cfg, int nf, int ns, int nv, int devic
 
 extern "C" fsim_status fsim_create(const fsim_config *cfg, const fsim_particles *p, int device, fsim_handle *out)
 {
+    NvtxRange nvtx_("fsim_create");
     if (!cfg || !p || !out) return FSIM_EINVAL;
     *out = nullptr;
     if (p->n_fluid < 0 || p->n_solid < 0 || p->n_virt < 0 || (p->n_fluid && (!p->fluid_pos || !p->fluid_vel ||
@@ -1024,6 +1034,7 @@ extern "C" fsim_status fsim_destroy(fsim_handle h)
 
 extern "C" fsim_status fsim_step(fsim_handle h, int nsteps)
 {
+    NvtxRange nvtx_("fsim_step");
     if (!h || nsteps < 0) return FSIM_EINVAL;
     if (h->batch) {
         fsim_set_error("the handle belongs to a batch; step it through the batch");
@@ -1048,6 +1059,7 @@ extern "C" fsim_status fsim_sync(fsim_handle h)
 
 extern "C" fsim_status fsim_run_phase(fsim_handle h, int phase)
 {
+    NvtxRange nvtx_("fsim_run_phase");
     if (!h) return FSIM_EINVAL;
     if (phase < FSIM_PHASE_CELL || phase > FSIM_PHASE_SOLID) {
         fsim_set_error("unknown phase %d", phase);
@@ -1219,6 +1231,7 @@ fsim_status enqueue_unpermute(fsim_sim *h, int field, int n, float *stg)
 
 extern "C" fsim_status fsim_get_field(fsim_handle h, int field, void *dst, size_t bytes)
 {
+    NvtxRange nvtx_("fsim_get_field");
     if (!h || (!dst && bytes)) return FSIM_EINVAL;
     if (h->batch) batch_wait(h);
     int n = 0;
@@ -1277,6 +1290,7 @@ fsim_status enqueue_permute_in(fsim_sim *h, int field, int n, const float *stg)
 
 extern "C" fsim_status fsim_set_field(fsim_handle h, int field, const void *src, size_t bytes)
 {
+    NvtxRange nvtx_("fsim_set_field");
     if (!h || (!src && bytes)) return FSIM_EINVAL;
     if (h->batch) batch_wait(h);
     float4 *dst = nullptr;
@@ -1323,6 +1337,7 @@ fsim_status bulk_reserve(fsim_sim *h, size_t bytes, int nev)
 extern "C" fsim_status fsim_get_fields(fsim_handle h, int nfields, const int *fields, void *const *dst,
                                        const size_t *bytes)
 {
+    NvtxRange nvtx_("fsim_get_fields");
     if (!h || nfields < 0 || (nfields && (!fields || !dst || !bytes))) return FSIM_EINVAL;
     if (h->batch) batch_wait(h);
     std::vector<int> counts(nfields);
@@ -1353,6 +1368,7 @@ extern "C" fsim_status fsim_get_fields(fsim_handle h, int nfields, const int *fi
 extern "C" fsim_status fsim_set_fields(fsim_handle h, int nfields, const int *fields, const void *const *src,
                                        const size_t *bytes)
 {
+    NvtxRange nvtx_("fsim_set_fields");
     if (!h || nfields < 0 || (nfields && (!fields || !src || !bytes))) return FSIM_EINVAL;
     if (h->batch) batch_wait(h);
     std::vector<int> counts(nfields);
@@ -1390,6 +1406,7 @@ extern "C" fsim_status fsim_set_fields(fsim_handle h, int nfields, const int *fi
 
 extern "C" fsim_status fsim_probe(fsim_handle h, const float *points, int n, float *out)
 {
+    NvtxRange nvtx_("fsim_probe");
     if (!h || n < 0 || (n && (!points || !out))) return FSIM_EINVAL;
     if (h->batch) batch_wait(h);
     if (!h->f_sorted || !h->s_sorted) {
@@ -1529,6 +1546,7 @@ fsim_status write_vtk(fsim_handle h, const char *out_dir, int file_step, bool bi
 
 extern "C" fsim_status fsim_write_vtk(fsim_handle h, const char *out_dir, int file_step)
 {
+    NvtxRange nvtx_("fsim_write_vtk");
     return write_vtk(h, out_dir, file_step, false);
 }
 
@@ -1590,6 +1608,48 @@ extern "C" fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_m
         }
     }
     *sweep_ms = sum;
+    return check_flags(h);
+}
+
+extern "C" fsim_status fsim_time_phases(fsim_handle h, int nsteps, float *ms, int n)
+{
+    NvtxRange nvtx_("fsim_time_phases");
+    if (!h || nsteps < 0 || !ms || n < 1) return FSIM_EINVAL;
+    if (h->batch) {
+        fsim_set_error("the handle belongs to a batch");
+        return FSIM_EINVAL;
+    }
+    DeviceGuard guard(h->device);
+    double tot[5] = {0, 0, 0, 0, 0};
+    std::vector<cudaEvent_t> ev;
+    fsim_status st = FSIM_OK;
+    for (int k = 0; k < nsteps && !st; ++k) {
+        Plan *pl = nullptr;
+        if ((st = handle_step_plan(h, &pl))) break;
+        const size_t need = 2 * pl->launches.size();
+        while (ev.size() < need) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) {
+                st = FSIM_ECUDA;
+                break;
+            }
+            ev.push_back(e);
+        }
+        if (st || (st = enqueue_plan(*pl, h->stream, h->tuner.shape(), nullptr, nullptr, ev.data()))) break;
+        after_plan(h, kAllPhases, *pl);
+        if (cudaEventSynchronize(ev[need - 1]) != cudaSuccess) {
+            st = FSIM_ECUDA;
+            break;
+        }
+        for (size_t q = 0; q < pl->launches.size(); ++q) {
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, ev[2 * q], ev[2 * q + 1]);
+            tot[launch_phase(pl->launches[q].kind)] += t;
+        }
+    }
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (st) return st;
+    for (int p = 0; p < n; ++p) ms[p] = p < 5 ? (float)tot[p] : 0.0f;
     return check_flags(h);
 }
 
@@ -1687,6 +1747,7 @@ extern "C" fsim_status fsim_snapshot_bytes(fsim_handle h, size_t *bytes)
 
 extern "C" fsim_status fsim_snapshot_save(fsim_handle h, long long step, void *buf, size_t bytes)
 {
+    NvtxRange nvtx_("fsim_snapshot_save");
     if (!h || !buf) return FSIM_EINVAL;
     if (h->batch) batch_wait(h);
     const size_t need = kSnapHeaderBytes + snap_payload(h);
@@ -1724,6 +1785,7 @@ extern "C" fsim_status fsim_snapshot_save(fsim_handle h, long long step, void *b
 extern "C" fsim_status fsim_snapshot_load(const void *buf, size_t bytes, int device, fsim_handle *out,
                                           long long *step)
 {
+    NvtxRange nvtx_("fsim_snapshot_load");
     if (!buf || !out) return FSIM_EINVAL;
     *out = nullptr;
     SnapHeader hd;
@@ -1920,6 +1982,7 @@ extern "C" fsim_status fsim_case_counts(const fsim_case *cs, int *n_fluid, int *
 
 extern "C" fsim_status fsim_create_case(const fsim_config *cfg, const fsim_case *cs, int device, fsim_handle *out)
 {
+    NvtxRange nvtx_("fsim_create_case");
     if (!cfg || !cs || !out) return FSIM_EINVAL;
     *out = nullptr;
     CaseGeom g;
@@ -2198,6 +2261,7 @@ extern "C" fsim_status fsim_batch_create(fsim_handle *members, int n, fsim_batch
 
 extern "C" fsim_status fsim_batch_step(fsim_batch_t b, int nsteps)
 {
+    NvtxRange nvtx_("fsim_batch_step");
     if (!b || nsteps < 0) return FSIM_EINVAL;
     DeviceGuard guard(b->device);
     for (int k = 0; k < nsteps; ++k) {

@@ -356,8 +356,11 @@ const Item<Args> &host_item(const Plan &pl, const Launch &L)
 // ---------------------------------------------- entry points of the kernels
 // Enqueue a plan's launches on `st`, the fluid sweep with launch shape
 // `shape`; optional events around the sweep.
+// per_launch: 2 events per launch, recorded before and after it.
 fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0 = nullptr,
-                         cudaEvent_t sweep1 = nullptr);
+                         cudaEvent_t sweep1 = nullptr, const cudaEvent_t *per_launch = nullptr);
+// the FSIM_PHASE_* a launch kind belongs to
+int launch_phase(int kind);
 // CTAs of the fused solid kernel that fit on the current device at once (<= want)
 int fused_grid(bool mixed, int want);
 // One launch of a utility kernel (kBlock threads per block) on `st`.

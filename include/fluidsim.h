@@ -268,6 +268,10 @@ fsim_status fsim_time_steps(fsim_handle h, int nsteps, float *ms);
  * every launch of the fluid sweep kernel; *total_ms = elapsed device time of
  * the nsteps, *sweep_ms = summed device time of the nsteps sweep launches. */
 fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_ms, float *sweep_ms);
+/* Per-phase device time: run nsteps launch by launch with CUDA events around
+ * every launch; ms[p] = summed time of phase p (FSIM_PHASE_CELL .. SOLID) for
+ * p < n (at most 5).  The reference prints only wall-clock times of its I/O. */
+fsim_status fsim_time_phases(fsim_handle h, int nsteps, float *ms, int n);
 /* Kernel launches one fsim_step(h, 1) issues (for launch accounting). */
 fsim_status fsim_launches_per_step(fsim_handle h, int *n);
 

@@ -201,3 +201,14 @@ def test_many_fields_equal_single_fields():
             assert np.array_equal(sim.get(k), bufs[k].array), k
         for b in bufs.values():
             b.free()
+
+
+def test_time_phases_reports_every_phase():
+    cfg, pa = cases.make(cases.small_dam_break())
+    with api.Simulation(cfg, pa, device=0) as sim:
+        sim.step(2)
+        ph = sim.time_phases(3)
+        assert set(ph) == {"cell", "couple", "virt", "fluid", "solid"}
+        assert all(v > 0 for v in ph.values())
+        sim.step(1)  # timing steps are ordinary steps
+        sim.sync()
