@@ -854,21 +854,26 @@ FSIM_BATCHED_KERNEL(kb_hash_mixed, HashMixedArgs, hash_mixed_body, kBlock)
 // water at dx = 5 mm, where an absolute FP16 pressure would be ~3 Pa.
 __device__ __forceinline__ void cell_ref_body(const DevParams &P, const CellRefArgs &A, int blk)
 {
-    const int c = blk * blockDim.x + threadIdx.x;
-    if (c >= A.ncell) return;
+    // one warp per cell, one particle per lane (a cell holds ~18 at the
+    // benchmark spacing; larger cells loop in chunks of 32)
+    const int c = (blk * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (c >= A.ncell) return; // whole warp
     const int b = A.start[c], e = A.start[c + 1];
     if (b == e) return; // never read: no particle refers to an empty cell
     float sd = 0.0f, sp = 0.0f;
-    for (int j = b; j < e; ++j) {
+    for (int j = b + lane; j < e; j += 32) {
         const float d = A.velp[j].w;
         sd += d;
         sp += eos_delta(P, d);
     }
+    sd = warp_sum(sd);
+    sp = warp_sum(sp);
     const float inv_n = 1.0f / (float)(e - b);
     const float dm = sd * inv_n, pm = sp * inv_n;
-    A.cm[c] = make_float2(dm, pm);
+    if (lane == 0) A.cm[c] = make_float2(dm, pm);
     float *w = reinterpret_cast<float *>(A.posr);
-    for (int j = b; j < e; ++j) {
+    for (int j = b + lane; j < e; j += 32) {
         const float d = A.velp[j].w;
         w[4 * (size_t)j + 3] = __uint_as_float(half2_bits((d - dm) * kDeltaScale, (eos_delta(P, d) - pm) * P.p_unit_inv));
     }

@@ -353,7 +353,7 @@ void plan_cell(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
     for (fsim_sim *h : m) {
         if (!h->mixed) continue;
         cr.push_back({h->P, CellRefArgs{h->f_posr[1 - pf], h->f_velp[1 - pf], h->f_start, h->f_cm, h->ncell}});
-        crb.push_back(h->nf ? blocks_for(h->ncell, kBlock) : 0);
+        crb.push_back(h->nf ? blocks_for(32ll * h->ncell, kBlock) : 0);
     }
     add_launch(pl, ab, L_CELLREF, cr, crb);
 }
