@@ -13,8 +13,10 @@ virtual walls, fused fluid sweep + update, 4 solid sub-steps) over the
   on the handle's stream, max over ranks.
 * ``e2e``: the same metric through the C ABI with host buffers: every step
   copies the fluid and solid state in from pinned host memory
-  (fsim_set_field), advances one step (fsim_step) and reads the state back
-  (fsim_get_field).
+  (fsim_set_fields), advances one step (fsim_step) and reads the state back
+  (fsim_get_fields).  ``serial_bound`` is the rate if the step took its device
+  time plus the upload and download at the link's measured copy rates
+  (``link_*_gbps``, one pinned buffer of the step's bytes each way).
 * ``roofline``: the fluid sweep kernel (the dominant kernel) against the
   measured HBM bandwidth, with the algorithmic 64 B per fluid particle-step.
 * ``cpu_baseline``: the FP64 CPU oracle on this host's cores, 2 steps of the
@@ -273,6 +275,10 @@ def run_gb300(args, dist):
     sim.sync()
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e = nupd * e2e_steps * dist.ws / e2e_s
+    # the serial bound: device step + upload + download at the link's measured rates
+    link = link_bandwidth(dev, h2d)
+    bound_s = ms * 1e-3 / args.steps + h2d / (link["h2d_gbps"] * 1e9) + d2h / (link["d2h_gbps"] * 1e9)
+    e2e_bound = nupd * dist.ws / bound_s
     for b in bufs.values():
         b.free()
     sim.close()
@@ -298,7 +304,8 @@ def run_gb300(args, dist):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(workload_desc(cfg, pa), parallelism="replicas%d" % dist.ws),
             "e2e": {"value": e2e, "unit": "particle-updates/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps, "link_h2d_gbps": link["h2d_gbps"],
+                    "link_d2h_gbps": link["d2h_gbps"], "serial_bound": e2e_bound, "frac_of_bound": e2e / e2e_bound},
             "roofline": {"bound": "hbm", "kernel": "k_fluid_sweep", "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "peak_source": peak_src,
@@ -347,6 +354,31 @@ def sweep_flop_roofline(api, sim, dev, t_launch):
             "peak_source": "measured (fsim_measure_fp32_peak, FMA chains at full residency)",
             "flop_per_launch": flop, "candidates_per_particle": cand / nf, "pairs_per_particle": pairs / nf,
             "flop_model": "10 FLOP per 27-cell candidate test + 80 FLOP per in-range pair"}
+
+
+def link_bandwidth(dev, nbytes, reps=5):
+    """Host<->device copy rate of one pinned buffer of nbytes each way (GB/s),
+    timed with CUDA events: the bound the end-to-end figure is held to."""
+    import torch
+
+    with torch.cuda.device(dev):
+        h = torch.empty(max(1, nbytes // 4), dtype=torch.float32, pin_memory=True)
+        d = torch.empty_like(h, device="cuda")
+        out = {}
+        for name, fn in (("h2d_gbps", lambda: d.copy_(h, non_blocking=True)),
+                         ("d2h_gbps", lambda: h.copy_(d, non_blocking=True))):
+            fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            out[name] = h.numel() * 4 * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+        del h, d
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_mixed(dev, steps):

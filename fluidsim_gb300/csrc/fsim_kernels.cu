@@ -1262,6 +1262,19 @@ __device__ __forceinline__ M3 cofactor(const M3 &a)
 // exactly that set.  kSolidGroup lanes share one particle and combine their
 // sums with shuffles (a fixed pairing: deterministic).
 
+// The list entries resolved once per step (the cells and the sort order are
+// fixed for the step's sub-steps): the sorted slot of each entry's neighbour,
+// or -1 where its current cell is not adjacent to the owner's.  The sub-steps
+// then read one index per entry instead of a chain of three loads.
+__device__ __forceinline__ void solid_slots_body(const DevParams &, const SolidArgs &S, int blk)
+{
+    const int e = blk * blockDim.x + threadIdx.x;
+    if (e >= S.ne) return;
+    const int i = S.inv[S.nbr_owner[e]], j = S.inv[S.nbr_orig[e]];
+    S.nbr_slot[e] = cells_adjacent(S.cxyz[i], S.cxyz[j]) ? j : -1;
+}
+FSIM_BATCHED_KERNEL(kb_solid_slots, SolidArgs, solid_slots_body, kBlock)
+
 // solidDeformationCalculate (src/solid.cu:10-79): F and L over the
 // reference-configuration neighbours, L^-1 (identity when singular),
 // F <- F L^-1, Green strain, St-Venant-Kirchhoff 2nd Piola, P = F S.
@@ -1278,11 +1291,10 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
     for (int k = 0; k < 9; ++k) F.m[k] = L.m[k] = 0.0f;
     if (valid) {
         const float4 xi = S.pos[i];
-        const unsigned ci = S.cxyz[i];
         const int o = S.orig[i];
         for (int e = S.nbr_off[o] + g, ee = S.nbr_off[o + 1]; e < ee; e += kSolidGroup) {
-            const int j = S.inv[S.nbr_orig[e]];
-            if (!cells_adjacent(ci, S.cxyz[j])) continue;
+            const int j = S.nbr_slot[e];
+            if (j < 0) continue;
             const float4 dXw = S.nbr_dXw[e];
             const float4 xj = S.pos[j];
             const float dx[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
@@ -1434,11 +1446,10 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
             PLi[k] = S.PL[9 * i + k];
             AVi[k] = S.AV[9 * i + k];
         }
-        const unsigned ci = S.cxyz[i];
         const int o = S.orig[i];
         for (int e = S.nbr_off[o] + g, ee = S.nbr_off[o + 1]; e < ee; e += kSolidGroup) {
-            const int j = S.inv[S.nbr_orig[e]];
-            if (!cells_adjacent(ci, S.cxyz[j])) continue;
+            const int j = S.nbr_slot[e];
+            if (j < 0) continue;
             const float4 dXw = S.nbr_dXw[e];
             const float dX = dXw.x, dY = dXw.y, dZ = dXw.z, w = dXw.w;
             const float *PLj = S.PL + 9 * j;
@@ -2065,6 +2076,7 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
         case L_DEFORM: FSIM_LAUNCH(kb_solid_deform, SolidArgs, kBlock); break;
         case L_FORCE: FSIM_LAUNCH(kb_solid_force, SolidArgs, kBlock); break;
         case L_UPDATE: FSIM_LAUNCH(kb_solid_update, SolidArgs, kBlock); break;
+        case L_SOLID_SLOTS: FSIM_LAUNCH(kb_solid_slots, SolidArgs, kBlock); break;
         case L_HASH_M: FSIM_LAUNCH(kb_hash_mixed, HashMixedArgs, kBlock); break;
         case L_CELLREF: FSIM_LAUNCH(kb_cell_ref, CellRefArgs, kBlock); break;
         case L_COUPLE_M: FSIM_LAUNCH(kb_couple_mixed, CoupleArgs, kBlock); break;
@@ -2110,6 +2122,7 @@ int launch_phase(int kind)
     case L_VIRT: case L_VIRT_M: return FSIM_PHASE_VIRT;
     case L_SWEEP: return FSIM_PHASE_FLUID;
     case L_DEFORM: case L_FORCE: case L_UPDATE: case L_DEFORM_M: case L_FORCE_M: case L_SOLID_FUSED:
+    case L_SOLID_SLOTS:
         return FSIM_PHASE_SOLID;
     default: return FSIM_PHASE_CELL;
     }

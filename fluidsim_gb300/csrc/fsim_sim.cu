@@ -79,6 +79,9 @@ struct fsim_sim {
     unsigned *s_cxyz = nullptr;   // packed cell coordinates, sorted order
     int *s_nbr_off = nullptr, *s_nbr_orig = nullptr; // static reference neighbours (CSR, input ids)
     float4 *s_nbr_dXw = nullptr;  // (X_j - X_i, kernel weight) per list entry
+    int *s_nbr_owner = nullptr;   // input id of each entry's particle
+    int *s_nbr_slot = nullptr;    // per step: sorted slot of each entry's neighbour (-1: cells not adjacent)
+    int s_ne = 0;                 // list entries
     int s_cur = 0;
     bool s_sorted = false;
     bool s_np_ok = false;    // normal + pressure are in the order of s_cur
@@ -464,6 +467,9 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         S.nbr_off = h->s_nbr_off;
         S.nbr_orig = h->s_nbr_orig;
         S.nbr_dXw = h->s_nbr_dXw;
+        S.nbr_owner = h->s_nbr_owner;
+        S.nbr_slot = h->s_nbr_slot;
+        S.ne = h->s_ne;
         S.cxyz = h->s_cxyz;
         S.nsub = h->ns ? h->cfg.solid_sub_step : 0;
         S.flags = h->d_flags;
@@ -472,6 +478,11 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         tt[q + 1] = tt[q] + (h->ns ? blocks_for(h->ns, kBlock) : 0);
     }
     const bool mixed = !m.empty() && m[0]->mixed;
+    {
+        std::vector<int> eb;
+        for (fsim_sim *h : m) eb.push_back(h->ns ? blocks_for(h->s_ne, kBlock) : 0);
+        add_launch(pl, ab, L_SOLID_SLOTS, it, eb);
+    }
     if (m.empty() || !m[0]->cfg.solid_fused) {
         // one batched launch per phase per sub-step; an instance takes part in
         // the sub-steps it has
@@ -796,13 +807,23 @@ fsim_status build_solid_neighbors(fsim_sim *h, const float *ref)
         off[i + 1] = (int)nbr.size();
     }
     const size_t ne = nbr.size();
+    if (ne > (size_t)INT_MAX) {
+        fsim_set_error("%zu solid neighbour entries exceed the index range", ne);
+        return FSIM_EINVAL;
+    }
+    h->s_ne = (int)ne;
+    std::vector<int> owner(ne);
+    for (int i = 0; i < ns; ++i)
+        for (int e = off[i]; e < off[i + 1]; ++e) owner[e] = i;
     fsim_status st;
     if ((st = dalloc(h, &h->s_nbr_off, (size_t)ns + 1)) || (st = dalloc(h, &h->s_nbr_orig, ne)) ||
-        (st = dalloc(h, &h->s_nbr_dXw, ne)))
+        (st = dalloc(h, &h->s_nbr_dXw, ne)) || (st = dalloc(h, &h->s_nbr_owner, ne)) ||
+        (st = dalloc(h, &h->s_nbr_slot, ne)))
         return st;
     CK(cudaMemcpy(h->s_nbr_off, off.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
     if (ne) {
         CK(cudaMemcpy(h->s_nbr_orig, nbr.data(), sizeof(int) * ne, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->s_nbr_owner, owner.data(), sizeof(int) * ne, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(h->s_nbr_dXw, dXw.data(), sizeof(float4) * ne, cudaMemcpyHostToDevice));
         launch_k_solid_pair_weights(blocks_for((long long)ne, kBlock), h->stream, h->P, h->s_nbr_dXw, (int)ne);
         CK_LAUNCH();
@@ -2417,10 +2438,11 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
     b += ns * (2 * 3 * sizeof(float4) + 2 * 2 * sizeof(int) + 4 * sizeof(int)); // state x2, cell/key/slot/tmp
     b += ns * (3 * sizeof(float4) + 5 * 9 * sizeof(float) + 2 * sizeof(int));  // per-step products, inv, cells
     {
-        // static solid neighbour lists: lattice count within 2h, plus slack
+        // static solid neighbour lists (id, owner, per-step slot, dX and weight):
+        // lattice count within 2h, plus slack
         const double r = std::sqrt((double)d.impact_distance_square) / (double)cfg->particle_diameter;
         const size_t per = (size_t)(4.18879 * r * r * r * 1.25) + 8;
-        b += ns * per * (sizeof(int) + sizeof(float4)) + (ns + 1) * sizeof(int);
+        b += ns * per * (3 * sizeof(int) + sizeof(float4)) + (ns + 1) * sizeof(int);
     }
     b += nv * (3 * sizeof(float4) + 2 * sizeof(int));
     b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 3; // counts, starts

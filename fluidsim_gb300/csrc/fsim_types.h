@@ -168,6 +168,9 @@ struct SolidArgs {
     // static reference-configuration neighbours (CSR over input ids)
     const int *orig, *inv, *nbr_off, *nbr_orig;
     const float4 *nbr_dXw; // (X_j - X_i, kernel weight)
+    const int *nbr_owner;  // input id of each entry's particle
+    int *nbr_slot;         // this step: sorted slot of each entry's neighbour, -1 if its cell is not adjacent
+    int ne;                // list entries
     const unsigned *cxyz;
     int nsub;              // this instance's solid sub-steps per step
     unsigned *flags;       // this instance's error flags
@@ -298,7 +301,7 @@ constexpr int kShapeWarps[kSweepShapes] = {4, 4, 8}; // warps per block of sweep
 enum LaunchKind {
     L_ZERO, L_HASH, L_SCAN_REDUCE, L_SCAN_PARTIALS, L_SCAN_APPLY, L_SCATTER, L_GATHER_F, L_GATHER_S,
     L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE,
-    L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M, L_SOLID_FUSED
+    L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M, L_SOLID_FUSED, L_SOLID_SLOTS
 };
 
 struct Launch {
