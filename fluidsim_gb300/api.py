@@ -50,6 +50,7 @@ class Config(C.Structure):
         ("precision", C.c_int),
         ("keep_derivatives", C.c_int),
         ("solid_fused", C.c_int),
+        ("solid_full_walk", C.c_int),
     ]
 
     def as_dict(self):

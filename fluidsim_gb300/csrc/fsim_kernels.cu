@@ -1381,7 +1381,18 @@ FSIM_BATCHED_KERNEL(kb_solid_deform_mixed, SolidArgs, solid_deform_body<true>, k
 // the 27 cells of the step-start cell) plus stress divergence and artificial
 // viscosity over the reference-configuration solid neighbours.
 // MIXED: fluid positions are cell offsets, fluid (rho, p) come from delta.
-template <bool MIXED>
+//
+// Fluid lists (plain form, FLIST): the fluid does not move during a step's
+// sub-steps and the candidates come from the step's cells, so sub-step 0
+// (FLIST 1) walks the 27 cells and records, per lane, the candidates within
+// (R + d)(1 + 1e-5) of the particle; later sub-steps (FLIST 2) walk only that
+// list while the particle is within d of where it was recorded (then every
+// dropped candidate is farther than R, with room for FP32 rounding).  A lane
+// keeps exactly the candidates it walked, in the same order, so the sums are
+// those of the full walk (FLIST 0) bit for bit; an overflowing list (count -1)
+// or a larger displacement falls back to the walk.  Every rounding of the
+// sums is spelled out so that the three instantiations compute alike.
+template <bool MIXED, int FLIST = 0>
 __device__ __forceinline__ void solid_force_body(const DevParams &P, const SolidArgs &S, int blk)
 {
     const int t = blk * blockDim.x + threadIdx.x;
@@ -1392,16 +1403,18 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
         const float4 xi = S.pos[i], vi = S.vel[i], ni = S.np[i];
         // solidFluidCouple (src/solid.cu:81-117)
         auto traction = [&](float dx, float dy, float dz, float r2, float4 u, float rhoj, float pj) {
-            const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
-            const float k2 = 2.0f * ((u.x - vi.x) * ni.x + (u.y - vi.y) * ni.y + (u.z - vi.z) * ni.z);
+            const float w = __fmul_rn(__expf(__fmul_rn(-r2, P.h_inv2)), P.kdiff);
+            const float k2 = __fmul_rn(2.0f, fmaf(__fsub_rn(u.z, vi.z), ni.z,
+                                                  fmaf(__fsub_rn(u.y, vi.y), ni.y,
+                                                       __fmul_rn(__fsub_rn(u.x, vi.x), ni.x))));
             const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
-            const float du = -k2 * (ni.x * dx + ni.y * dy + ni.z * dz) * inv_r;
-            float ps = 0.5f * (ni.w + pj);
-            if (du >= 0.0f) ps += 0.5f * rhoj * du * P.c0;
-            const float f = -2.0f * ps * P.rho_s_inv * w;
-            cx += f * dx;
-            cy += f * dy;
-            cz += f * dz;
+            const float du = __fmul_rn(__fmul_rn(-k2, fmaf(ni.z, dz, fmaf(ni.y, dy, __fmul_rn(ni.x, dx)))), inv_r);
+            float ps = __fmul_rn(0.5f, __fadd_rn(ni.w, pj));
+            if (du >= 0.0f) ps = fmaf(__fmul_rn(__fmul_rn(0.5f, rhoj), du), P.c0, ps);
+            const float f = __fmul_rn(__fmul_rn(-2.0f, ps), __fmul_rn(P.rho_s_inv, w));
+            cx = fmaf(f, dx, cx);
+            cy = fmaf(f, dy, cy);
+            cz = fmaf(f, dz, cz);
         };
         if (MIXED) {
             solid_fluid_walk_m<kSolidGroup>(P, S.start_f, S.fposr, S.cell[i], xi, g,
@@ -1414,29 +1427,48 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
                                                 }
                                             });
         }
-        Rows rows;
-        neighbor_rows(P, S.cell[i], rows);
-        if (MIXED) rows.count = 0;
-        for (int r = 0; r < rows.count; ++r) {
-            const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-            for (int j = S.start_f[c0] + g, je = S.start_f[c1]; j < je; j += kSolidGroup) {
-                const float4 q = S.fposr[j];
-                const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
-                const float r2 = dist2(dx, dy, dz);
-                if (r2 < P.R2) {
-                    const float4 u = S.fvelp[j];
-                    const float w = __expf(-r2 * P.h_inv2) * P.kdiff;
-                    const float k2 = 2.0f * ((u.x - vi.x) * ni.x + (u.y - vi.y) * ni.y + (u.z - vi.z) * ni.z);
-                    // u_i - u_j = -k2 n ; du = (u_i - u_j).e
-                    const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
-                    const float du = -k2 * (ni.x * dx + ni.y * dy + ni.z * dz) * inv_r;
-                    float ps = 0.5f * (ni.w + u.w);
-                    if (du >= 0.0f) ps += 0.5f * q.w * du * P.c0;
-                    const float f = -2.0f * ps * P.rho_s_inv * w;
-                    cx += f * dx;
-                    cy += f * dy;
-                    cz += f * dz;
+        bool walk = !MIXED;
+        const int T = kSolidGroup * S.n; // stride of the entry-major lane lists
+        if (!MIXED && FLIST == 2) {
+            const float4 o = S.fl_org[i];
+            const int c = S.fl_cnt[t];
+            if (c >= 0 && dist2(xi.x - o.x, xi.y - o.y, xi.z - o.z) < P.fl_move2) {
+                walk = false;
+                for (int e = 0; e < c; ++e) {
+                    const int j = S.fl[(size_t)e * T + t];
+                    const float4 q = S.fposr[j];
+                    const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+                    const float r2 = dist2(dx, dy, dz);
+                    if (r2 < P.R2) {
+                        const float4 u = S.fvelp[j];
+                        traction(dx, dy, dz, r2, u, q.w, u.w);
+                    }
                 }
+            }
+        }
+        if (walk) {
+            Rows rows;
+            neighbor_rows(P, S.cell[i], rows);
+            int nrec = 0;
+            for (int r = 0; r < rows.count; ++r) {
+                const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
+                for (int j = S.start_f[c0] + g, je = S.start_f[c1]; j < je; j += kSolidGroup) {
+                    const float4 q = S.fposr[j];
+                    const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
+                    const float r2 = dist2(dx, dy, dz);
+                    if (FLIST == 1 && r2 < P.fl_build2) {
+                        if (nrec < kFluidListCap) S.fl[(size_t)nrec * T + t] = j;
+                        ++nrec;
+                    }
+                    if (r2 < P.R2) {
+                        const float4 u = S.fvelp[j];
+                        traction(dx, dy, dz, r2, u, q.w, u.w);
+                    }
+                }
+            }
+            if (FLIST == 1) {
+                S.fl_cnt[t] = nrec <= kFluidListCap ? nrec : -1;
+                if (g == 0) S.fl_org[i] = xi;
             }
         }
         // solidSolidForce (src/solid.cu:119-157)
@@ -1453,18 +1485,23 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
             const float4 dXw = S.nbr_dXw[e];
             const float dX = dXw.x, dY = dXw.y, dZ = dXw.z, w = dXw.w;
             const float *PLj = S.PL + 9 * j;
-            const float ws = w * P.rho_s_inv;
-            ax += ((PLj[0] + PLi[0]) * dX + (PLj[1] + PLi[1]) * dY + (PLj[2] + PLi[2]) * dZ) * ws;
-            ay += ((PLj[3] + PLi[3]) * dX + (PLj[4] + PLi[4]) * dY + (PLj[5] + PLi[5]) * dZ) * ws;
-            az += ((PLj[6] + PLi[6]) * dX + (PLj[7] + PLi[7]) * dY + (PLj[8] + PLi[8]) * dZ) * ws;
+            const float ws = __fmul_rn(w, P.rho_s_inv);
+            auto row3 = [&](float a0, float a1, float a2) {
+                return fmaf(a2, dZ, fmaf(a1, dY, __fmul_rn(a0, dX)));
+            };
+            ax = fmaf(row3(__fadd_rn(PLj[0], PLi[0]), __fadd_rn(PLj[1], PLi[1]), __fadd_rn(PLj[2], PLi[2])), ws, ax);
+            ay = fmaf(row3(__fadd_rn(PLj[3], PLi[3]), __fadd_rn(PLj[4], PLi[4]), __fadd_rn(PLj[5], PLi[5])), ws, ay);
+            az = fmaf(row3(__fadd_rn(PLj[6], PLi[6]), __fadd_rn(PLj[7], PLi[7]), __fadd_rn(PLj[8], PLi[8])), ws, az);
             const float4 xj = S.pos[j], vj = S.vel[j];
-            const float ddx = xj.x - xi.x, ddy = xj.y - xi.y, ddz = xj.z - xi.z;
-            const float dvdx = (vj.x - vi.x) * ddx + (vj.y - vi.y) * ddy + (vj.z - vi.z) * ddz;
-            const float nu = P.h * dvdx / (ddx * ddx + ddy * ddy + ddz * ddz + P.eps_h2);
-            const float visc = (P.alpha * nu * P.cs_s - P.beta * nu * nu) * w;
-            ax += (AVi[0] * dX + AVi[1] * dY + AVi[2] * dZ) * visc;
-            ay += (AVi[3] * dX + AVi[4] * dY + AVi[5] * dZ) * visc;
-            az += (AVi[6] * dX + AVi[7] * dY + AVi[8] * dZ) * visc;
+            const float ddx = __fsub_rn(xj.x, xi.x), ddy = __fsub_rn(xj.y, xi.y), ddz = __fsub_rn(xj.z, xi.z);
+            const float dvdx = fmaf(__fsub_rn(vj.z, vi.z), ddz,
+                                    fmaf(__fsub_rn(vj.y, vi.y), ddy, __fmul_rn(__fsub_rn(vj.x, vi.x), ddx)));
+            const float nu = __fdiv_rn(__fmul_rn(P.h, dvdx),
+                                       __fadd_rn(fmaf(ddz, ddz, fmaf(ddy, ddy, __fmul_rn(ddx, ddx))), P.eps_h2));
+            const float visc = __fmul_rn(fmaf(__fmul_rn(P.alpha, nu), P.cs_s, -__fmul_rn(__fmul_rn(P.beta, nu), nu)), w);
+            ax = fmaf(row3(AVi[0], AVi[1], AVi[2]), visc, ax);
+            ay = fmaf(row3(AVi[3], AVi[4], AVi[5]), visc, ay);
+            az = fmaf(row3(AVi[6], AVi[7], AVi[8]), visc, az);
         }
     }
     cx = group_sum(cx);
@@ -1475,9 +1512,11 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
     az = group_sum(az);
     if (!valid || g) return;
     S.couple[i] = make_float4(cx, cy, cz, 0.0f);
-    S.dudt[i] = make_float4(ax + cx, ay + cy, az + cz, 0.0f);
+    S.dudt[i] = make_float4(__fadd_rn(ax, cx), __fadd_rn(ay, cy), __fadd_rn(az, cz), 0.0f);
 }
 FSIM_BATCHED_KERNEL(kb_solid_force, SolidArgs, solid_force_body<false>, kBlock)
+FSIM_BATCHED_KERNEL(kb_solid_force_record, SolidArgs, (solid_force_body<false, 1>), kBlock)
+FSIM_BATCHED_KERNEL(kb_solid_force_listed, SolidArgs, (solid_force_body<false, 2>), kBlock)
 FSIM_BATCHED_KERNEL(kb_solid_force_mixed, SolidArgs, solid_force_body<true>, kBlock)
 
 // Kernel weight of every static solid neighbour pair (once, at creation).
@@ -2075,6 +2114,8 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
             break;
         case L_DEFORM: FSIM_LAUNCH(kb_solid_deform, SolidArgs, kBlock); break;
         case L_FORCE: FSIM_LAUNCH(kb_solid_force, SolidArgs, kBlock); break;
+        case L_FORCE_RECORD: FSIM_LAUNCH(kb_solid_force_record, SolidArgs, kBlock); break;
+        case L_FORCE_LISTED: FSIM_LAUNCH(kb_solid_force_listed, SolidArgs, kBlock); break;
         case L_UPDATE: FSIM_LAUNCH(kb_solid_update, SolidArgs, kBlock); break;
         case L_SOLID_SLOTS: FSIM_LAUNCH(kb_solid_slots, SolidArgs, kBlock); break;
         case L_HASH_M: FSIM_LAUNCH(kb_hash_mixed, HashMixedArgs, kBlock); break;
@@ -2122,7 +2163,7 @@ int launch_phase(int kind)
     case L_VIRT: case L_VIRT_M: return FSIM_PHASE_VIRT;
     case L_SWEEP: return FSIM_PHASE_FLUID;
     case L_DEFORM: case L_FORCE: case L_UPDATE: case L_DEFORM_M: case L_FORCE_M: case L_SOLID_FUSED:
-    case L_SOLID_SLOTS:
+    case L_SOLID_SLOTS: case L_FORCE_RECORD: case L_FORCE_LISTED:
         return FSIM_PHASE_SOLID;
     default: return FSIM_PHASE_CELL;
     }

@@ -80,6 +80,8 @@ struct fsim_sim {
     int *s_nbr_off = nullptr, *s_nbr_orig = nullptr; // static reference neighbours (CSR, input ids)
     float4 *s_nbr_dXw = nullptr;  // (X_j - X_i, kernel weight) per list entry
     int *s_nbr_owner = nullptr;   // input id of each entry's particle
+    int *s_fl = nullptr, *s_fl_cnt = nullptr; // solid force fluid lists (per lane) and counts
+    float4 *s_fl_org = nullptr;   // where each solid particle was when its lists were recorded
     int *s_nbr_slot = nullptr;    // per step: sorted slot of each entry's neighbour (-1: cells not adjacent)
     int s_ne = 0;                 // list entries
     int s_cur = 0;
@@ -160,6 +162,14 @@ void fill_params(fsim_sim *h)
     DevParams &P = h->P;
     std::memset(&P, 0, sizeof P);
     P.R2 = d.impact_distance_square;
+    {
+        // solid force fluid lists: a particle may move 0.1 R within a step
+        // before its list is bypassed; the list keeps candidates within
+        // 1.1 R (1 + 1e-5), which covers the FP32 rounding of both tests
+        const double R = std::sqrt((double)P.R2), dmove = 0.1 * R, rb = (R + dmove) * (1.0 + 1e-5);
+        P.fl_move2 = (float)(dmove * dmove);
+        P.fl_build2 = (float)(rb * rb);
+    }
     P.h = c.smoothing_length;
     P.h_inv2 = d.smoothing_length_inverse_square;
     P.kdiff = d.kernel_differential;
@@ -469,6 +479,9 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         S.nbr_dXw = h->s_nbr_dXw;
         S.nbr_owner = h->s_nbr_owner;
         S.nbr_slot = h->s_nbr_slot;
+        S.fl = h->s_fl;
+        S.fl_cnt = h->s_fl_cnt;
+        S.fl_org = h->s_fl_org;
         S.ne = h->s_ne;
         S.cxyz = h->s_cxyz;
         S.nsub = h->ns ? h->cfg.solid_sub_step : 0;
@@ -494,7 +507,10 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
                 tb.push_back(active ? blocks_for(h->ns, kBlock) : 0);
             }
             add_launch(pl, ab, mixed ? L_DEFORM_M : L_DEFORM, it, wb);
-            add_launch(pl, ab, mixed ? L_FORCE_M : L_FORCE, it, wb);
+            // plain form: sub-step 0 records each lane's fluid list, later sub-steps walk it
+            const bool lists = !mixed && !m[0]->cfg.solid_full_walk;
+            add_launch(pl, ab, mixed ? L_FORCE_M : !lists ? L_FORCE : k == 0 ? L_FORCE_RECORD : L_FORCE_LISTED, it,
+                       wb);
             add_launch(pl, ab, L_UPDATE, it, tb);
         }
         return;
@@ -866,7 +882,9 @@ fsim_status alloc_state(fsim_sim *h)
         (st = dalloc(h, &h->s_F, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_P, 9 * (size_t)ns)) ||
         (st = dalloc(h, &h->s_L, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_PL, 9 * (size_t)ns)) ||
         (st = dalloc(h, &h->s_AV, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_inv, ns)) ||
-        (st = dalloc(h, &h->s_cxyz, ns)))
+        (st = dalloc(h, &h->s_cxyz, ns)) ||
+        (st = dalloc(h, &h->s_fl, (size_t)kFluidListCap * kSolidGroup * ns)) ||
+        (st = dalloc(h, &h->s_fl_cnt, (size_t)kSolidGroup * ns)) || (st = dalloc(h, &h->s_fl_org, ns)))
         return st;
     // virtual
     if ((st = dalloc(h, &h->v_posr, nv)) || (st = dalloc(h, &h->v_velp, nv)) || (st = dalloc(h, &h->v_normal, nv)) ||
@@ -2243,7 +2261,8 @@ extern "C" fsim_status fsim_batch_create(fsim_handle *members, int n, fsim_batch
             return FSIM_EINVAL;
         }
         if (members[k]->mixed != members[0]->mixed ||
-            members[k]->cfg.solid_fused != members[0]->cfg.solid_fused) {
+            members[k]->cfg.solid_fused != members[0]->cfg.solid_fused ||
+            members[k]->cfg.solid_full_walk != members[0]->cfg.solid_full_walk) {
             fsim_set_error("batch members must share the precision form and the solid launch form");
             return FSIM_EINVAL;
         }
@@ -2318,7 +2337,8 @@ extern "C" fsim_status fsim_batch_add(fsim_batch_t b, fsim_handle h)
         return FSIM_EINVAL;
     }
     if (!b->members.empty() && (h->mixed != b->members[0]->mixed ||
-                                h->cfg.solid_fused != b->members[0]->cfg.solid_fused)) {
+                                h->cfg.solid_fused != b->members[0]->cfg.solid_fused ||
+                                h->cfg.solid_full_walk != b->members[0]->cfg.solid_full_walk)) {
         fsim_set_error("batch members must share the precision form and the solid launch form");
         return FSIM_EINVAL;
     }
@@ -2437,6 +2457,7 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
     if (cfg->keep_derivatives) b += nf * (sizeof(float) + sizeof(float4));
     b += ns * (2 * 3 * sizeof(float4) + 2 * 2 * sizeof(int) + 4 * sizeof(int)); // state x2, cell/key/slot/tmp
     b += ns * (3 * sizeof(float4) + 5 * 9 * sizeof(float) + 2 * sizeof(int));  // per-step products, inv, cells
+    b += ns * (kSolidGroup * (kFluidListCap + 1) * sizeof(int) + sizeof(float4)); // force fluid lists
     {
         // static solid neighbour lists (id, owner, per-step slot, dX and weight):
         // lattice count within 2h, plus slack

@@ -33,6 +33,8 @@ struct DevParams {
     float cdx[3], dlo_rel[3], dhi_rel[3];
     float dlt_min, dlt_max, p_unit, p_unit_inv;
     int mixed;
+    // solid force fluid lists: recording radius^2, allowed displacement^2
+    float fl_build2, fl_move2;
 };
 
 // per-instance error flags (device word, read by check_flags)
@@ -43,6 +45,7 @@ constexpr int kScanThreads = 1024;  // cell-count scan: threads per block
 constexpr int kScanItems = 4;       //   and counts per thread
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kMaxScanTiles = 16384; // cell grids up to 67M cells
+constexpr int kFluidListCap = 48;   // fluid list entries per solid lane
 
 __host__ __device__ inline int blocks_for(long long n, int b) { return (int)((n + b - 1) / b); }
 
@@ -169,6 +172,11 @@ struct SolidArgs {
     const int *orig, *inv, *nbr_off, *nbr_orig;
     const float4 *nbr_dXw; // (X_j - X_i, kernel weight)
     const int *nbr_owner;  // input id of each entry's particle
+    // fluid candidates of each solid lane within the recording radius (plain
+    // form, entry-major: entry e of lane t at e * (kSolidGroup * n) + t), their
+    // counts (-1: overflow) and where each particle was when they were recorded
+    int *fl, *fl_cnt;
+    float4 *fl_org;
     int *nbr_slot;         // this step: sorted slot of each entry's neighbour, -1 if its cell is not adjacent
     int ne;                // list entries
     const unsigned *cxyz;
@@ -301,7 +309,8 @@ constexpr int kShapeWarps[kSweepShapes] = {4, 4, 8}; // warps per block of sweep
 enum LaunchKind {
     L_ZERO, L_HASH, L_SCAN_REDUCE, L_SCAN_PARTIALS, L_SCAN_APPLY, L_SCATTER, L_GATHER_F, L_GATHER_S,
     L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE,
-    L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M, L_SOLID_FUSED, L_SOLID_SLOTS
+    L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M, L_SOLID_FUSED, L_SOLID_SLOTS,
+    L_FORCE_RECORD, L_FORCE_LISTED
 };
 
 struct Launch {

@@ -91,6 +91,10 @@ typedef struct fsim_config {
     int   solid_fused;              /* 1: all solid sub-steps of a step in one
                                        persistent cooperative launch (else one
                                        launch per phase per sub-step)         */
+    int   solid_full_walk;          /* 1: every solid sub-step walks the fluid
+                                       of its 27 cells (else sub-steps after
+                                       the first walk a per-lane list recorded
+                                       by the first; same results bit for bit) */
 } fsim_config;
 
 /* Derived constants, as Parameter::initiateParameter computes them in FP32

@@ -134,6 +134,48 @@ def test_sweep_shapes_bit_identical(dam):
     b.close()
 
 
+def _plate_touching_fluid(speed):
+    """tiny_box with the plate moved to one particle spacing from the fluid
+    block (inside the impact distance), moving at `speed` along x."""
+    cfg, pa = cases.make(cases.tiny_box())
+    shift = pa.solid_pos[:, 0].min() - pa.fluid_pos[:, 0].max() - cfg.particle_diameter
+    sp, sr, sv = pa.solid_pos.copy(), pa.solid_ref_pos.copy(), np.zeros_like(pa.solid_vel)
+    sp[:, 0] -= shift
+    sr[:, 0] -= shift
+    sv[:, 0] = speed
+    return cfg, api.ParticleArrays(pa.fluid_pos, pa.fluid_vel, pa.fluid_rho, pa.fluid_p, sp, sv, sr,
+                                   pa.solid_type, pa.virt_pos)
+
+
+@pytest.mark.parametrize("bypass", [False, True])
+def test_solid_fluid_lists_equal_full_walk(bypass):
+    """Solid sub-steps after the first walk a per-lane list of the fluid
+    candidates that the first recorded; the results equal the full 27-cell
+    walk of every sub-step bit for bit.  With `bypass` the plate moves more
+    than 0.1 R per sub-step, so later sub-steps fall back to the walk."""
+    cfg, pa = _plate_touching_fluid(0.0)
+    steps = 6
+    if bypass:
+        # 0.75 of the allowed displacement (0.1 R) per sub-step: sub-step 1
+        # walks the list, sub-steps 2 and 3 walk the cells; one step
+        R = float(np.sqrt(api.derive(cfg).impact_distance_square))
+        cfg, pa = _plate_touching_fluid(-0.75 * 0.1 * R / (cfg.dt / cfg.solid_sub_step))
+        steps = 1
+    full = api.Config.from_buffer_copy(cfg)
+    full.solid_full_walk = 1
+    out = []
+    for c in (cfg, full):
+        with api.Simulation(c, pa, device=0) as s:
+            s.step(steps)
+            s.sync()
+            out.append({f: s.get(f) for f in ("solid_pos", "solid_vel", "fluid_pos", "fluid_vel", "fluid_p")})
+    for f in out[0]:
+        assert np.all(np.isfinite(out[0][f])), f
+        assert np.array_equal(out[0][f], out[1][f]), f
+    if not bypass:  # the plate's free particles (type 0) felt the fluid
+        assert np.any(out[0]["solid_vel"][pa.solid_type == 0, 0] != 0.0)
+
+
 def test_deterministic_repeat(dam):
     cfg, pa = dam
     outs = []
