@@ -130,6 +130,9 @@ def test_extension_keys_ignored_by_reference_semantics():
     assert cfg.precision == api.PRECISION_MIXED and cfg.keep_derivatives == 1
     cfg = api.config_from_ini_text(text + "\n[gb300]\ngb300_solid_fused = yes\n")
     assert cfg.solid_fused == 1 and cfg.precision == api.PRECISION_FP32
+    assert api.config_from_ini_text(text).solid_full_walk == 0
+    walk = api.config_from_ini_text(text + "\n[gb300]\ngb300_solid_full_walk = yes\n")
+    assert walk.solid_full_walk == 1 and walk.solid_fused == 0
     base = api.config_from_ini_text(text)
     for k in RAW_FLOAT + RAW_INT:
         assert getattr(cfg, k) == getattr(base, k)
