@@ -2056,7 +2056,7 @@ namespace fsim_rt {
 
 // Enqueue a plan's launches; optional events around the fluid sweep.
 fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0, cudaEvent_t sweep1,
-                         const cudaEvent_t *per_launch)
+                         const cudaEvent_t *per_launch, unsigned sweep_flags)
 {
     using SweepFn = void (*)(const Item<FluidSweepArgs> *, const int *, int);
     using Sweep1Fn = void (*)(const DevParams, const FluidSweepArgs);
@@ -2098,7 +2098,7 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
         case L_COUPLE: FSIM_LAUNCH(kb_couple, CoupleArgs, kBlock); break;
         case L_VIRT: FSIM_LAUNCH(kb_virt, VirtArgs, kBlock); break;
         case L_SWEEP:
-            if (sweep0) CK(cudaEventRecord(sweep0, st));
+            if (sweep0) CK(cudaEventRecordWithFlags(sweep0, st, sweep_flags));
             {
                 const int *tbs = reinterpret_cast<const int *>(pl.arena + L.shape_table_off[shape]);
                 const int gs = L.shape_blocks[shape], thr = kShapeWarps[shape] * 32;
@@ -2110,7 +2110,7 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
                 }
             }
             CK_LAUNCH();
-            if (sweep1) CK(cudaEventRecord(sweep1, st));
+            if (sweep1) CK(cudaEventRecordWithFlags(sweep1, st, sweep_flags));
             break;
         case L_DEFORM: FSIM_LAUNCH(kb_solid_deform, SolidArgs, kBlock); break;
         case L_FORCE: FSIM_LAUNCH(kb_solid_force, SolidArgs, kBlock); break;

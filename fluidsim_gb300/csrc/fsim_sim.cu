@@ -246,6 +246,11 @@ void free_plan(Plan *pl)
 {
     if (!pl) return;
     if (pl->graph) cudaGraphExecDestroy(pl->graph);
+    for (int k = 0; k < 2; ++k) {
+        if (pl->texec[k]) cudaGraphExecDestroy(pl->texec[k]);
+        if (pl->tev[k]) cudaEventDestroy(pl->tev[k]);
+    }
+    if (pl->tgraph) cudaGraphDestroy(pl->tgraph);
     if (pl->arena) cudaFree(pl->arena);
     delete pl;
 }
@@ -589,6 +594,40 @@ fsim_status capture_plan(Plan &pl, cudaStream_t st, int shape)
         fsim_set_error("graph instantiate failed: %s", cudaGetErrorString(e));
         return FSIM_ECUDA;
     }
+    return FSIM_OK;
+}
+
+// The step graph with event nodes around the sweep (see Plan::tgraph).
+fsim_status capture_timed_plan(Plan &pl, cudaStream_t st, int shape)
+{
+    for (int k = 0; k < 2; ++k)
+        if (!pl.tev[k]) CK(cudaEventCreate(&pl.tev[k]));
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    fsim_status s = enqueue_plan(pl, st, shape, pl.tev[0], pl.tev[1], nullptr, cudaEventRecordExternal);
+    cudaError_t e = cudaStreamEndCapture(st, &pl.tgraph);
+    if (s) return s;
+    if (e != cudaSuccess) {
+        fsim_set_error("stream capture failed: %s", cudaGetErrorString(e));
+        return FSIM_ECUDA;
+    }
+    size_t n = 0;
+    CK(cudaGraphGetNodes(pl.tgraph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    CK(cudaGraphGetNodes(pl.tgraph, nodes.data(), &n));
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType type;
+        CK(cudaGraphNodeGetType(nd, &type));
+        if (type != cudaGraphNodeTypeEventRecord) continue;
+        cudaEvent_t ev = nullptr;
+        CK(cudaGraphEventRecordNodeGetEvent(nd, &ev));
+        for (int k = 0; k < 2; ++k)
+            if (ev == pl.tev[k]) pl.tnode[k] = nd;
+    }
+    if (!pl.tnode[0] || !pl.tnode[1]) {
+        fsim_set_error("the captured step graph has no event nodes around the sweep");
+        return FSIM_ECUDA;
+    }
+    for (int k = 0; k < 2; ++k) CK(cudaGraphInstantiate(&pl.texec[k], pl.tgraph, 0));
     return FSIM_OK;
 }
 
@@ -1627,12 +1666,38 @@ extern "C" fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_m
         h->sweep_events.push_back(e);
     }
     fsim_status st = FSIM_OK;
+    // once the sweep shape is tuned: the step graphs themselves (with event
+    // nodes around the sweep), else launch by launch with the tuner's shape
+    const bool graphs = h->tuner.chosen >= 0 && h->nf > 0;
+    if (graphs) {
+        // capture outside the timed region: a step flips the buffer parities
+        // the same way every time, so consecutive steps use two plans
+        const int f0 = h->f_cur, s0 = h->s_cur;
+        for (int k = 0; k < 2; ++k) {
+            Plan *pl = nullptr;
+            if ((st = handle_step_plan(h, &pl))) return st;
+            if (!pl->tgraph && (st = capture_timed_plan(*pl, h->stream, h->tuner.chosen))) return st;
+            h->f_cur = pl->pf_after;
+            h->s_cur = pl->ps_after;
+        }
+        h->f_cur = f0;
+        h->s_cur = s0;
+    }
     CK(cudaEventRecord(h->ev0, h->stream));
     for (int k = 0; k < nsteps; ++k) {
         Plan *pl = nullptr;
         if ((st = handle_step_plan(h, &pl))) return st;
-        if ((st = enqueue_plan(*pl, h->stream, h->tuner.shape(), h->sweep_events[2 * k], h->sweep_events[2 * k + 1])))
+        if (graphs) {
+            if (!pl->tgraph && (st = capture_timed_plan(*pl, h->stream, h->tuner.chosen))) return st;
+            cudaGraphExec_t ex = pl->texec[pl->tnext];
+            pl->tnext ^= 1;
+            CK(cudaGraphExecEventRecordNodeSetEvent(ex, pl->tnode[0], h->sweep_events[2 * k]));
+            CK(cudaGraphExecEventRecordNodeSetEvent(ex, pl->tnode[1], h->sweep_events[2 * k + 1]));
+            CK(cudaGraphLaunch(ex, h->stream));
+        } else if ((st = enqueue_plan(*pl, h->stream, h->tuner.shape(), h->sweep_events[2 * k],
+                                      h->sweep_events[2 * k + 1]))) {
             return st;
+        }
         after_plan(h, kAllPhases, *pl);
     }
     CK(cudaEventRecord(h->ev1, h->stream));

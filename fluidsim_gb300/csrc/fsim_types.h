@@ -332,6 +332,15 @@ struct Plan {
     std::vector<char> host; // host image of the arena (one-instance launches pass items by value)
     cudaGraphExec_t graph = nullptr;
     int sweep_index = -1;         // launch index of the fluid sweep
+    // the same step graph with event nodes around the sweep, for timing the
+    // sweep inside graph replays: two executable copies (consecutive replays
+    // alternate, so an event update never touches the copy just launched)
+    // and the nodes whose events each replay sets
+    cudaGraph_t tgraph = nullptr;
+    cudaGraphExec_t texec[2] = {nullptr, nullptr};
+    cudaGraphNode_t tnode[2] = {nullptr, nullptr};
+    cudaEvent_t tev[2] = {nullptr, nullptr}; // the events at capture
+    int tnext = 0;
 };
 
 template <class Args>
@@ -367,10 +376,12 @@ const Item<Args> &host_item(const Plan &pl, const Launch &L)
 
 // ---------------------------------------------- entry points of the kernels
 // Enqueue a plan's launches on `st`, the fluid sweep with launch shape
-// `shape`; optional events around the sweep.
+// `shape`; optional events around the sweep (recorded with sweep_flags:
+// cudaEventRecordExternal makes them event nodes of a captured graph).
 // per_launch: 2 events per launch, recorded before and after it.
 fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0 = nullptr,
-                         cudaEvent_t sweep1 = nullptr, const cudaEvent_t *per_launch = nullptr);
+                         cudaEvent_t sweep1 = nullptr, const cudaEvent_t *per_launch = nullptr,
+                         unsigned sweep_flags = cudaEventRecordDefault);
 // the FSIM_PHASE_* a launch kind belongs to
 int launch_phase(int kind);
 // CTAs of the fused solid kernel that fit on the current device at once (<= want)

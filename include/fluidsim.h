@@ -268,9 +268,10 @@ fsim_status fsim_write_vtk_binary(fsim_handle h, const char *out_dir, int file_s
 /* Device timing: run nsteps (CUDA-graph replays) on the handle's stream
  * bracketed by CUDA events recorded on that stream; *ms = elapsed device time. */
 fsim_status fsim_time_steps(fsim_handle h, int nsteps, float *ms);
-/* Instrumented timing: run nsteps launch by launch with an event pair around
- * every launch of the fluid sweep kernel; *total_ms = elapsed device time of
- * the nsteps, *sweep_ms = summed device time of the nsteps sweep launches. */
+/* Instrumented timing: run nsteps as CUDA-graph replays of the step graph
+ * with event nodes around the fluid sweep launch (launch by launch while the
+ * sweep's launch shape is still being tuned); *total_ms = elapsed device time
+ * of the nsteps, *sweep_ms = summed device time of the nsteps sweep launches. */
 fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_ms, float *sweep_ms);
 /* Per-phase device time: run nsteps launch by launch with CUDA events around
  * every launch; ms[p] = summed time of phase p (FSIM_PHASE_CELL .. SOLID) for

@@ -212,3 +212,24 @@ def test_time_phases_reports_every_phase():
         assert all(v > 0 for v in ph.values())
         sim.step(1)  # timing steps are ordinary steps
         sim.sync()
+
+
+def test_time_sweep_graph_replays_equal_plain_steps():
+    """Once the sweep shape is tuned, fsim_time_sweep replays the step graph
+    with event nodes around the sweep: the same kernels in the same order,
+    so the state equals that of ordinary steps bit for bit."""
+    cfg, pa = cases.make(cases.small_dam_break())
+    a = api.Simulation(cfg, pa, device=0)
+    b = api.Simulation(cfg, pa, device=0)
+    for s in (a, b):
+        s.step(4)  # the tuner's three steps and one graph replay
+    tot, sweep = a.time_sweep(5)
+    tot2, sweep2 = a.time_sweep(3)  # the captured timed graphs are reused
+    b.step(8)
+    a.sync()
+    b.sync()
+    assert 0 < sweep < tot and 0 < sweep2 < tot2
+    for f in ("fluid_pos", "fluid_vel", "fluid_rho", "solid_pos", "solid_vel"):
+        assert np.array_equal(a.get(f), b.get(f)), f
+    a.close()
+    b.close()
