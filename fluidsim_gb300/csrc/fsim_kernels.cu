@@ -1275,6 +1275,15 @@ __device__ __forceinline__ void solid_slots_body(const DevParams &, const SolidA
 }
 FSIM_BATCHED_KERNEL(kb_solid_slots, SolidArgs, solid_slots_body, kBlock)
 
+// Kernel weight of a reference-configuration pair from X_j - X_i.  X_j - X_i
+// is formed from the sorted reference positions (static, a few hundred KB,
+// cache-resident) instead of being stored per list entry: the same FP32
+// difference the list was built from, for 4 B per entry instead of 20.
+__device__ __forceinline__ float solid_pair_weight(const DevParams &P, float dx, float dy, float dz)
+{
+    return __fmul_rn(__expf(__fmul_rn(-dist2(dx, dy, dz), P.h_inv2)), P.kdiff);
+}
+
 // solidDeformationCalculate (src/solid.cu:10-79): F and L over the
 // reference-configuration neighbours, L^-1 (identity when singular),
 // F <- F L^-1, Green strain, St-Venant-Kirchhoff 2nd Piola, P = F S.
@@ -1290,18 +1299,18 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
 #pragma unroll
     for (int k = 0; k < 9; ++k) F.m[k] = L.m[k] = 0.0f;
     if (valid) {
-        const float4 xi = S.pos[i];
+        const float4 xi = S.pos[i], ri = S.ref[i];
         const int o = S.orig[i];
         for (int e = S.nbr_off[o] + g, ee = S.nbr_off[o + 1]; e < ee; e += kSolidGroup) {
             const int j = S.nbr_slot[e];
             if (j < 0) continue;
-            const float4 dXw = S.nbr_dXw[e];
-            const float4 xj = S.pos[j];
+            const float4 xj = S.pos[j], rj = S.ref[j];
             const float dx[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
-            const float dX[3] = {dXw.x, dXw.y, dXw.z};
+            const float dX[3] = {__fsub_rn(rj.x, ri.x), __fsub_rn(rj.y, ri.y), __fsub_rn(rj.z, ri.z)};
+            const float w = solid_pair_weight(P, dX[0], dX[1], dX[2]);
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                const float ra = dx[a] * dXw.w, la = dX[a] * dXw.w;
+                const float ra = dx[a] * w, la = dX[a] * w;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     F.m[3 * a + c] += ra * dX[c];
@@ -1478,12 +1487,14 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
             PLi[k] = S.PL[9 * i + k];
             AVi[k] = S.AV[9 * i + k];
         }
+        const float4 ri = S.ref[i];
         const int o = S.orig[i];
         for (int e = S.nbr_off[o] + g, ee = S.nbr_off[o + 1]; e < ee; e += kSolidGroup) {
             const int j = S.nbr_slot[e];
             if (j < 0) continue;
-            const float4 dXw = S.nbr_dXw[e];
-            const float dX = dXw.x, dY = dXw.y, dZ = dXw.z, w = dXw.w;
+            const float4 rj = S.ref[j];
+            const float dX = __fsub_rn(rj.x, ri.x), dY = __fsub_rn(rj.y, ri.y), dZ = __fsub_rn(rj.z, ri.z);
+            const float w = solid_pair_weight(P, dX, dY, dZ);
             const float *PLj = S.PL + 9 * j;
             const float ws = __fmul_rn(w, P.rho_s_inv);
             auto row3 = [&](float a0, float a1, float a2) {
@@ -1518,17 +1529,6 @@ FSIM_BATCHED_KERNEL(kb_solid_force, SolidArgs, solid_force_body<false>, kBlock)
 FSIM_BATCHED_KERNEL(kb_solid_force_record, SolidArgs, (solid_force_body<false, 1>), kBlock)
 FSIM_BATCHED_KERNEL(kb_solid_force_listed, SolidArgs, (solid_force_body<false, 2>), kBlock)
 FSIM_BATCHED_KERNEL(kb_solid_force_mixed, SolidArgs, solid_force_body<true>, kBlock)
-
-// Kernel weight of every static solid neighbour pair (once, at creation).
-__global__ void k_solid_pair_weights(const DevParams P, float4 *__restrict__ dXw, int n)
-{
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n) return;
-    float4 v = dXw[e];
-    const float r2 = dist2(v.x, v.y, v.z);
-    v.w = __expf(-r2 * P.h_inv2) * P.kdiff;
-    dXw[e] = v;
-}
 
 // solidUpdate (src/solid.cu:209-239)
 __device__ __forceinline__ void solid_update_body(const DevParams &P, const SolidArgs &S, int blk)
@@ -2197,11 +2197,6 @@ void launch_k_iota(int grid, cudaStream_t st, int *a, int n)
 void launch_k_virt_normal(int grid, cudaStream_t st, const DevParams P, const float4 *v_posr, const int *v_cell, const int *start_v, float4 *v_normal, int n)
 {
     k_virt_normal<<<grid, kBlock, 0, st>>>(P, v_posr, v_cell, start_v, v_normal, n);
-}
-
-void launch_k_solid_pair_weights(int grid, cudaStream_t st, const DevParams P, float4 *dXw, int n)
-{
-    k_solid_pair_weights<<<grid, kBlock, 0, st>>>(P, dXw, n);
 }
 
 void launch_k_fluid_to_mixed(int grid, cudaStream_t st, const DevParams P, float4 *posr, float4 *velp, int *cell, int n, unsigned *flags)

@@ -78,7 +78,6 @@ struct fsim_sim {
     int *s_inv = nullptr;         // sorted position of every input id (written by the gather)
     unsigned *s_cxyz = nullptr;   // packed cell coordinates, sorted order
     int *s_nbr_off = nullptr, *s_nbr_orig = nullptr; // static reference neighbours (CSR, input ids)
-    float4 *s_nbr_dXw = nullptr;  // (X_j - X_i, kernel weight) per list entry
     int *s_nbr_owner = nullptr;   // input id of each entry's particle
     int *s_fl = nullptr, *s_fl_cnt = nullptr; // solid force fluid lists (per lane) and counts
     float4 *s_fl_org = nullptr;   // where each solid particle was when its lists were recorded
@@ -481,7 +480,6 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         S.inv = h->s_inv;
         S.nbr_off = h->s_nbr_off;
         S.nbr_orig = h->s_nbr_orig;
-        S.nbr_dXw = h->s_nbr_dXw;
         S.nbr_owner = h->s_nbr_owner;
         S.nbr_slot = h->s_nbr_slot;
         S.fl = h->s_fl;
@@ -837,7 +835,6 @@ fsim_status build_solid_neighbors(fsim_sim *h, const float *ref)
         for (int i = 0; i < ns; ++i) order[fill[key[i]]++] = i; // increasing i within a bin
     }
     std::vector<int> off(ns + 1, 0), nbr;
-    std::vector<float4> dXw;
     std::vector<int> cand;
     for (int i = 0; i < ns; ++i) {
         const int bx = bin(i, 0), by = bin(i, 1), bz = bin(i, 2);
@@ -854,10 +851,7 @@ fsim_status build_solid_neighbors(fsim_sim *h, const float *ref)
             const float dx = ref[3 * j] - ref[3 * i], dy = ref[3 * j + 1] - ref[3 * i + 1],
                         dz = ref[3 * j + 2] - ref[3 * i + 2];
             const float r2 = std::fmaf(dz, dz, std::fmaf(dy, dy, dx * dx));
-            if (r2 < R2) {
-                nbr.push_back(j);
-                dXw.push_back(make_float4(dx, dy, dz, 0.0f));
-            }
+            if (r2 < R2) nbr.push_back(j);
         }
         off[i + 1] = (int)nbr.size();
     }
@@ -872,16 +866,12 @@ fsim_status build_solid_neighbors(fsim_sim *h, const float *ref)
         for (int e = off[i]; e < off[i + 1]; ++e) owner[e] = i;
     fsim_status st;
     if ((st = dalloc(h, &h->s_nbr_off, (size_t)ns + 1)) || (st = dalloc(h, &h->s_nbr_orig, ne)) ||
-        (st = dalloc(h, &h->s_nbr_dXw, ne)) || (st = dalloc(h, &h->s_nbr_owner, ne)) ||
-        (st = dalloc(h, &h->s_nbr_slot, ne)))
+        (st = dalloc(h, &h->s_nbr_owner, ne)) || (st = dalloc(h, &h->s_nbr_slot, ne)))
         return st;
     CK(cudaMemcpy(h->s_nbr_off, off.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
     if (ne) {
         CK(cudaMemcpy(h->s_nbr_orig, nbr.data(), sizeof(int) * ne, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(h->s_nbr_owner, owner.data(), sizeof(int) * ne, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(h->s_nbr_dXw, dXw.data(), sizeof(float4) * ne, cudaMemcpyHostToDevice));
-        launch_k_solid_pair_weights(blocks_for((long long)ne, kBlock), h->stream, h->P, h->s_nbr_dXw, (int)ne);
-        CK_LAUNCH();
     }
     return FSIM_OK;
 }
@@ -2524,11 +2514,11 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
     b += ns * (3 * sizeof(float4) + 5 * 9 * sizeof(float) + 2 * sizeof(int));  // per-step products, inv, cells
     b += ns * (kSolidGroup * (kFluidListCap + 1) * sizeof(int) + sizeof(float4)); // force fluid lists
     {
-        // static solid neighbour lists (id, owner, per-step slot, dX and weight):
+        // static solid neighbour lists (id, owner, per-step slot):
         // lattice count within 2h, plus slack
         const double r = std::sqrt((double)d.impact_distance_square) / (double)cfg->particle_diameter;
         const size_t per = (size_t)(4.18879 * r * r * r * 1.25) + 8;
-        b += ns * per * (3 * sizeof(int) + sizeof(float4)) + (ns + 1) * sizeof(int);
+        b += ns * per * 3 * sizeof(int) + (ns + 1) * sizeof(int);
     }
     b += nv * (3 * sizeof(float4) + 2 * sizeof(int));
     b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 3; // counts, starts

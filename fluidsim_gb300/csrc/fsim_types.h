@@ -170,7 +170,6 @@ struct SolidArgs {
     int n;
     // static reference-configuration neighbours (CSR over input ids)
     const int *orig, *inv, *nbr_off, *nbr_orig;
-    const float4 *nbr_dXw; // (X_j - X_i, kernel weight)
     const int *nbr_owner;  // input id of each entry's particle
     // fluid candidates of each solid lane within the recording radius (plain
     // form, entry-major: entry e of lane t at e * (kSolidGroup * n) + t), their
@@ -390,7 +389,6 @@ int fused_grid(bool mixed, int want);
 void launch_k_pack_f4(int grid, cudaStream_t st, const float *xyz, const float *w, int n, float wconst, float4 *out);
 void launch_k_iota(int grid, cudaStream_t st, int *a, int n);
 void launch_k_virt_normal(int grid, cudaStream_t st, const DevParams P, const float4 *v_posr, const int *v_cell, const int *start_v, float4 *v_normal, int n);
-void launch_k_solid_pair_weights(int grid, cudaStream_t st, const DevParams P, float4 *dXw, int n);
 void launch_k_fluid_to_mixed(int grid, cudaStream_t st, const DevParams P, float4 *posr, float4 *velp, int *cell, int n, unsigned *flags);
 void launch_k_offsets_in_cells(int grid, cudaStream_t st, const DevParams P, float4 *pos, const int *cell, int n);
 void launch_k_unpermute_mixed(int grid, cudaStream_t st, const DevParams P, const float4 *pos, const float4 *velp, const int *cell, const int *orig, int n, int what, float *out);
