@@ -64,15 +64,6 @@ __device__ __forceinline__ int cell_index(const DevParams &P, float x, float y, 
     return cx * P.ny * P.nz + cy * P.nz + cz;
 }
 
-// cell coordinates of a linear cell index
-__device__ __forceinline__ void cell_xyz(const DevParams &P, int c, int &cx, int &cy, int &cz)
-{
-    const int row = c / P.nz;
-    cz = c - row * P.nz;
-    cx = row / P.ny;
-    cy = row - cx * P.ny;
-}
-
 // FP32 squared distance; the oracle's neighbour counts use the same formula.
 __device__ __forceinline__ float dist2(float dx, float dy, float dz)
 {
@@ -617,40 +608,17 @@ __global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep_1(const DevPara
 // getVirtData (src/virt.cu:9-75): nearest fluid particle's rho, hydrostatically
 // corrected p and velocity mirrored about the (static) wall normal.  Ties in
 // distance go to the smaller input id.
-//
-// The 9 cell rows are walked nearest first (own row, the 4 edge rows, the 4
-// corners), and a row is skipped when its distance in x and y from the wall
-// particle -- less a margin of 1e-3 cell, far above the FP32 rounding of the
-// cell bounds -- exceeds the best squared distance found so far by a relative
-// 1e-5: no candidate there could beat or tie the best, so the winner is the
-// one a walk of all 27 cells finds.
-__constant__ int kRowOX[9] = {0, -1, 1, 0, 0, -1, -1, 1, 1};
-__constant__ int kRowOY[9] = {0, 0, 0, -1, 1, -1, 1, -1, 1};
-
 __device__ __forceinline__ void virt_body(const DevParams &P, const VirtArgs &A, int blk)
 {
     const int i = blk * blockDim.x + threadIdx.x;
     if (i >= A.n) return;
     const float4 xi = A.v_posr_in[i];
-    int cx, cy, cz;
-    cell_xyz(P, A.v_cell[i], cx, cy, cz);
-    const int z0 = max(cz - 1, 0), z1 = min(cz + 1, P.nz - 1) + 1;
-    const float mx = 1e-3f * P.cdx[0], my = 1e-3f * P.cdx[1];
-    // gaps to the rows on either side: the faces of the wall particle's cell column
-    const float gxl = fmaxf(xi.x - fmaf((float)cx, P.cdx[0], P.cmin[0]) - mx, 0.0f);
-    const float gxh = fmaxf(fmaf((float)(cx + 1), P.cdx[0], P.cmin[0]) - xi.x - mx, 0.0f);
-    const float gyl = fmaxf(xi.y - fmaf((float)cy, P.cdx[1], P.cmin[1]) - my, 0.0f);
-    const float gyh = fmaxf(fmaf((float)(cy + 1), P.cdx[1], P.cmin[1]) - xi.y - my, 0.0f);
+    Rows rows;
+    neighbor_rows(P, A.v_cell[i], rows);
     float best = FSIM_LARGE_FLOAT;
     int best_j = -1, best_orig = INT_MAX;
-    for (int r = 0; r < 9; ++r) {
-        const int ox = kRowOX[r], oy = kRowOY[r];
-        const int x = cx + ox, y = cy + oy;
-        if (x < 0 || x >= P.nx || y < 0 || y >= P.ny) continue;
-        const float gx = ox < 0 ? gxl : ox > 0 ? gxh : 0.0f, gy = oy < 0 ? gyl : oy > 0 ? gyh : 0.0f;
-        if (fmaf(gx, gx, gy * gy) > best * 1.00001f) continue;
-        const int base = (x * P.ny + y) * P.nz;
-        for (int j = A.start_f[base + z0], je = A.start_f[base + z1]; j < je; ++j) {
+    for (int r = 0; r < rows.count; ++r) {
+        for (int j = A.start_f[rows.base[r] + rows.z0], je = A.start_f[rows.base[r] + rows.z1]; j < je; ++j) {
             const float4 q = A.fposr[j];
             const float d2 = dist2(q.x - xi.x, q.y - xi.y, q.z - xi.z);
             if (d2 < best) {
@@ -821,6 +789,13 @@ constexpr float kDeltaUnit = 1.0f / 1024.0f;
 __device__ __forceinline__ float eos_delta(const DevParams &P, float d)
 {
     return fmaxf(__fmul_rn(P.rho2p, expm1f(__fmul_rn(P.gamma, log1pf(d)))), P.min_p);
+}
+__device__ __forceinline__ void cell_xyz(const DevParams &P, int c, int &cx, int &cy, int &cz)
+{
+    const int row = c / P.nz;
+    cz = c - row * P.nz;
+    cx = row / P.ny;
+    cy = row - cx * P.ny;
 }
 __device__ __forceinline__ unsigned half2_bits(float a, float b)
 {
