@@ -393,8 +393,8 @@ def link_bandwidth(dev, nbytes, reps=5):
 
 
 def run_mixed(dev, steps):
-    """BASELINE config 2: the 4M FSI case with +-0.01 dx position jitter (seed
-    12345) in the plain FP32 form and in the mixed form, same input.  Device
+    """The mixed-precision workload: the 4M FSI case with +-0.01 dx position
+    jitter (seed 12345) in the plain FP32 form and in the mixed form, same input.  Device
     time of `steps` graph steps each; the per-field error of both forms against
     the FP64 oracle is measured separately (tests/accuracy_report.py)."""
     from fluidsim_gb300 import api, cases
@@ -416,7 +416,7 @@ def run_mixed(dev, steps):
 
 
 def run_ensemble(dev, steps):
-    """BASELINE config 3: 64 seeded dam-break instances (8k-250k fluid
+    """The ensemble workload: 64 seeded dam-break instances (8k-250k fluid
     particles, plate E log-uniform 1e5-1e7 Pa, nu 0.3-0.45, gate 0.6-1.0 m),
     advanced (a) one instance after another in the plain form and (b) all at
     once by batched launches.  Returns aggregate particle-updates/s of both."""
@@ -464,10 +464,10 @@ def run_ensemble(dev, steps):
 
 
 def run_served(dev):
-    """BASELINE config 4, shortened in request count only: a seeded Poisson
-    stream (20 requests/s) of config-3-style scenarios with the config's
-    distributions (fluid 10k-1M log-uniform, solid 1k-27k, 200-2000 steps),
-    served with continuous batching under a 150 GB budget, and the same stream
+    """The served workload, shortened in request count only: a seeded Poisson
+    stream (20 requests/s) of ensemble-style dam-break scenarios (fluid 10k-1M
+    log-uniform, solid 1k-27k, 200-2000 steps), served with continuous
+    batching under a 150 GB budget, and the same stream
     served one request at a time.  Request data is generated before the clock
     starts.  24 requests keep the run to tens of seconds; at 20 requests/s the
     stream saturates the GPU, as the 2000-request stream does."""
@@ -483,8 +483,8 @@ def run_served(dev):
         q.data, q.particles = r.data, r.particles
     plain = serve.serve_one_by_one(again, device=dev)
     return {"workload": "Poisson stream, %d requests at %g/s (seed 7), fluid %d-%d log-uniform, solid %d-%d, "
-                        "steps %d-%d uniform, dx=0.01, 150 GB HBM budget and a 6M-particle work budget; the config's "
-                        "2000 requests shortened to %d"
+                        "steps %d-%d uniform, dx=0.01, 150 GB HBM budget and a 6M-particle work budget; a "
+                        "2000-request stream shortened to %d"
                         % (spec["n"], spec["rate"], spec["fluid_range"][0], spec["fluid_range"][1],
                            spec["solid_range"][0], spec["solid_range"][1], spec["steps_range"][0],
                            spec["steps_range"][1], spec["n"]),

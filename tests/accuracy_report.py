@@ -2,7 +2,7 @@
 oracle, at chosen step counts, from the same initial state.
 
     python tests/accuracy_report.py --case fsi_4m_jitter --steps 1,200,1000 \
-        --json gpurun_out/accuracy.json
+        --json out/accuracy.json
 
 Errors per field (fluid and solid), with d = gpu - fp64:
   max_rel = |d|_inf / |fp64|_inf            (the normalised max error of the tests)
