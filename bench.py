@@ -26,7 +26,7 @@ virtual walls, fused fluid sweep + update, 4 solid sub-steps) over the
   against the measured HBM bandwidth, with the algorithmic 64 B per fluid
   particle-step; ``roofline_fp32`` against the measured FP32 FMA peak.
 * ``cpu_baseline``: the FP64 CPU oracle on this host's cores, 2 steps of the
-  same workload.
+  same workload; ``single_thread``: one step of it on one thread.
 
 ``--impl reference`` times the CPU restatement of the reference path (FP32
 oracle, all host threads): the reference itself is a CUDA program with no CPU
@@ -307,6 +307,11 @@ def run_gb300(args, dist):
         rate, dt = cpu_oracle_rate(cfg, pa, "f64", args.cpu_steps, cores)
         cpu = {"value": rate, "unit": "particle-updates/s", "cores": cores, "kind": "port",
                "sample": "%d fluid steps of the full workload in the FP64 oracle (%.1f s)" % (args.cpu_steps, dt)}
+        if cores > 1:
+            rate1, dt1 = cpu_oracle_rate(cfg, pa, "f64", 1, 1)
+            cpu["single_thread"] = {"value": rate1, "unit": "particle-updates/s", "cores": 1,
+                                    "sample": "1 fluid step of the full workload in the FP64 oracle on one "
+                                              "thread (%.1f s)" % dt1}
 
     if dist.rank == 0:
         line = {
