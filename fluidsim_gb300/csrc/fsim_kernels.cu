@@ -1378,9 +1378,12 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
         S.F[9 * i + k] = F.m[k];
         S.Pk[9 * i + k] = Pk.m[k];
         S.L[9 * i + k] = Linv.m[k];
-        S.PL[9 * i + k] = PL.m[k];
         S.AV[9 * i + k] = AV.m[k];
     }
+    float4 *pl = reinterpret_cast<float4 *>(S.PL + kPLStride * i);
+    pl[0] = make_float4(PL.m[0], PL.m[1], PL.m[2], PL.m[3]);
+    pl[1] = make_float4(PL.m[4], PL.m[5], PL.m[6], PL.m[7]);
+    pl[2] = make_float4(PL.m[8], 0.0f, 0.0f, 0.0f);
 }
 FSIM_BATCHED_KERNEL(kb_solid_deform, SolidArgs, solid_deform_body<false>, kBlock)
 FSIM_BATCHED_KERNEL(kb_solid_deform_mixed, SolidArgs, solid_deform_body<true>, kBlock)
@@ -1484,7 +1487,7 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
         float PLi[9], AVi[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
-            PLi[k] = S.PL[9 * i + k];
+            PLi[k] = S.PL[kPLStride * i + k];
             AVi[k] = S.AV[9 * i + k];
         }
         const float4 ri = S.ref[i];
@@ -1495,7 +1498,9 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
             const float4 rj = S.ref[j];
             const float dX = __fsub_rn(rj.x, ri.x), dY = __fsub_rn(rj.y, ri.y), dZ = __fsub_rn(rj.z, ri.z);
             const float w = solid_pair_weight(P, dX, dY, dZ);
-            const float *PLj = S.PL + 9 * j;
+            const float4 *plj = reinterpret_cast<const float4 *>(S.PL + kPLStride * j);
+            const float4 q0 = plj[0], q1 = plj[1], q2 = plj[2];
+            const float PLj[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
             const float ws = __fmul_rn(w, P.rho_s_inv);
             auto row3 = [&](float a0, float a1, float a2) {
                 return fmaf(a2, dZ, fmaf(a1, dY, __fmul_rn(a0, dX)));

@@ -909,7 +909,7 @@ fsim_status alloc_state(fsim_sim *h)
         (st = dalloc(h, &h->s_tmp, ns)) || (st = dalloc(h, &h->s_cnt, nc)) || (st = dalloc(h, &h->s_start, nc + 1)) ||
         (st = dalloc(h, &h->s_np, ns)) || (st = dalloc(h, &h->s_dudt, ns)) || (st = dalloc(h, &h->s_couple, ns)) ||
         (st = dalloc(h, &h->s_F, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_P, 9 * (size_t)ns)) ||
-        (st = dalloc(h, &h->s_L, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_PL, 9 * (size_t)ns)) ||
+        (st = dalloc(h, &h->s_L, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_PL, (size_t)kPLStride * ns)) ||
         (st = dalloc(h, &h->s_AV, 9 * (size_t)ns)) || (st = dalloc(h, &h->s_inv, ns)) ||
         (st = dalloc(h, &h->s_cxyz, ns)) ||
         (st = dalloc(h, &h->s_fl, (size_t)kFluidListCap * kSolidGroup * ns)) ||
@@ -2511,7 +2511,7 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
     b += nf * (2 * 2 * sizeof(float4) + 2 * sizeof(int) + 4 * sizeof(int)); // state x2, orig x2, cell/key/slot/tmp
     if (cfg->keep_derivatives) b += nf * (sizeof(float) + sizeof(float4));
     b += ns * (2 * 3 * sizeof(float4) + 2 * 2 * sizeof(int) + 4 * sizeof(int)); // state x2, cell/key/slot/tmp
-    b += ns * (3 * sizeof(float4) + 5 * 9 * sizeof(float) + 2 * sizeof(int));  // per-step products, inv, cells
+    b += ns * (3 * sizeof(float4) + (4 * 9 + kPLStride) * sizeof(float) + 2 * sizeof(int)); // per-step products, inv, cells
     b += ns * (kSolidGroup * (kFluidListCap + 1) * sizeof(int) + sizeof(float4)); // force fluid lists
     {
         // static solid neighbour lists (id, owner, per-step slot):

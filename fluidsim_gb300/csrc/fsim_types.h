@@ -46,6 +46,7 @@ constexpr int kScanItems = 4;       //   and counts per thread
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kMaxScanTiles = 16384; // cell grids up to 67M cells
 constexpr int kFluidListCap = 48;   // fluid list entries per solid lane
+constexpr int kPLStride = 12;       // floats per particle of the solid's P L^-1 array (16-byte rows)
 
 __host__ __device__ inline int blocks_for(long long n, int b) { return (int)((n + b - 1) / b); }
 
@@ -163,7 +164,8 @@ struct SolidArgs {
     const float4 *ref;
     const int *type, *cell, *start_s;
     const float4 *np;
-    float *F, *Pk, *L, *PL, *AV; // 9 floats per particle, row-major
+    float *F, *Pk, *L, *AV; // 9 floats per particle, row-major
+    float *PL;              // kPLStride floats per particle (9 used): three 16-byte loads per neighbour
     float4 *dudt, *couple;
     const float4 *fposr, *fvelp;
     const int *start_f;
