@@ -1289,7 +1289,9 @@ __device__ __forceinline__ float solid_pair_weight(const DevParams &P, float dx,
 // F <- F L^-1, Green strain, St-Venant-Kirchhoff 2nd Piola, P = F S.
 // Also stores P L^-1 and cof(F) L^-1 (= det(F) F^-T L^-1) for the force sweep.
 // MIXED: L^-1 is formed in FP64 (cofactors, determinant, division) and rounded.
-template <bool MIXED>
+// RESOLVE (the step's first sub-step): each list entry's neighbour slot is
+// resolved here, as kb_solid_slots would, and stored for the later sub-steps.
+template <bool MIXED, bool RESOLVE = false>
 __device__ __forceinline__ void solid_deform_body(const DevParams &P, const SolidArgs &S, int blk)
 {
     const int t = blk * blockDim.x + threadIdx.x;
@@ -1301,8 +1303,16 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
     if (valid) {
         const float4 xi = S.pos[i], ri = S.ref[i];
         const int o = S.orig[i];
+        const unsigned ci = RESOLVE ? S.cxyz[i] : 0u;
         for (int e = S.nbr_off[o] + g, ee = S.nbr_off[o + 1]; e < ee; e += kSolidGroup) {
-            const int j = S.nbr_slot[e];
+            int j;
+            if (RESOLVE) {
+                const int jj = S.inv[S.nbr_orig[e]];
+                j = cells_adjacent(ci, S.cxyz[jj]) ? jj : -1;
+                S.nbr_slot[e] = j;
+            } else {
+                j = S.nbr_slot[e];
+            }
             if (j < 0) continue;
             const float4 xj = S.pos[j], rj = S.ref[j];
             const float dx[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
@@ -1310,11 +1320,12 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
             const float w = solid_pair_weight(P, dX[0], dX[1], dX[2]);
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                const float ra = dx[a] * w, la = dX[a] * w;
+                // roundings spelled out: the instantiations compute alike
+                const float ra = __fmul_rn(dx[a], w), la = __fmul_rn(dX[a], w);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    F.m[3 * a + c] += ra * dX[c];
-                    L.m[3 * a + c] += la * dX[c];
+                    F.m[3 * a + c] = fmaf(ra, dX[c], F.m[3 * a + c]);
+                    L.m[3 * a + c] = fmaf(la, dX[c], L.m[3 * a + c]);
                 }
             }
         }
@@ -1387,6 +1398,8 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
 }
 FSIM_BATCHED_KERNEL(kb_solid_deform, SolidArgs, solid_deform_body<false>, kBlock)
 FSIM_BATCHED_KERNEL(kb_solid_deform_mixed, SolidArgs, solid_deform_body<true>, kBlock)
+FSIM_BATCHED_KERNEL(kb_solid_deform_resolve, SolidArgs, (solid_deform_body<false, true>), kBlock)
+FSIM_BATCHED_KERNEL(kb_solid_deform_mixed_resolve, SolidArgs, (solid_deform_body<true, true>), kBlock)
 
 // solidForceCalculate (src/solid.cu:81-207): fluid traction over the fluid
 // neighbours (current configuration, fluid already advanced; candidates from
@@ -2123,6 +2136,8 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
         case L_FORCE_LISTED: FSIM_LAUNCH(kb_solid_force_listed, SolidArgs, kBlock); break;
         case L_UPDATE: FSIM_LAUNCH(kb_solid_update, SolidArgs, kBlock); break;
         case L_SOLID_SLOTS: FSIM_LAUNCH(kb_solid_slots, SolidArgs, kBlock); break;
+        case L_DEFORM_R: FSIM_LAUNCH(kb_solid_deform_resolve, SolidArgs, kBlock); break;
+        case L_DEFORM_M_R: FSIM_LAUNCH(kb_solid_deform_mixed_resolve, SolidArgs, kBlock); break;
         case L_HASH_M: FSIM_LAUNCH(kb_hash_mixed, HashMixedArgs, kBlock); break;
         case L_CELLREF: FSIM_LAUNCH(kb_cell_ref, CellRefArgs, kBlock); break;
         case L_COUPLE_M: FSIM_LAUNCH(kb_couple_mixed, CoupleArgs, kBlock); break;
@@ -2168,7 +2183,7 @@ int launch_phase(int kind)
     case L_VIRT: case L_VIRT_M: return FSIM_PHASE_VIRT;
     case L_SWEEP: return FSIM_PHASE_FLUID;
     case L_DEFORM: case L_FORCE: case L_UPDATE: case L_DEFORM_M: case L_FORCE_M: case L_SOLID_FUSED:
-    case L_SOLID_SLOTS: case L_FORCE_RECORD: case L_FORCE_LISTED:
+    case L_SOLID_SLOTS: case L_FORCE_RECORD: case L_FORCE_LISTED: case L_DEFORM_R: case L_DEFORM_M_R:
         return FSIM_PHASE_SOLID;
     default: return FSIM_PHASE_CELL;
     }

@@ -494,11 +494,6 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         tt[q + 1] = tt[q] + (h->ns ? blocks_for(h->ns, kBlock) : 0);
     }
     const bool mixed = !m.empty() && m[0]->mixed;
-    {
-        std::vector<int> eb;
-        for (fsim_sim *h : m) eb.push_back(h->ns ? blocks_for(h->s_ne, kBlock) : 0);
-        add_launch(pl, ab, L_SOLID_SLOTS, it, eb);
-    }
     if (m.empty() || !m[0]->cfg.solid_fused) {
         // one batched launch per phase per sub-step; an instance takes part in
         // the sub-steps it has
@@ -509,7 +504,9 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
                 wb.push_back(active ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
                 tb.push_back(active ? blocks_for(h->ns, kBlock) : 0);
             }
-            add_launch(pl, ab, mixed ? L_DEFORM_M : L_DEFORM, it, wb);
+            // sub-step 0 also resolves the step's list slots for the later sub-steps
+            add_launch(pl, ab, mixed ? (k == 0 ? L_DEFORM_M_R : L_DEFORM_M) : (k == 0 ? L_DEFORM_R : L_DEFORM), it,
+                       wb);
             // plain form: sub-step 0 records each lane's fluid list, later sub-steps walk it
             const bool lists = !mixed && !m[0]->cfg.solid_full_walk;
             add_launch(pl, ab, mixed ? L_FORCE_M : !lists ? L_FORCE : k == 0 ? L_FORCE_RECORD : L_FORCE_LISTED, it,
@@ -517,6 +514,11 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
             add_launch(pl, ab, L_UPDATE, it, tb);
         }
         return;
+    }
+    {
+        std::vector<int> eb;
+        for (fsim_sim *h : m) eb.push_back(h->ns ? blocks_for(h->s_ne, kBlock) : 0);
+        add_launch(pl, ab, L_SOLID_SLOTS, it, eb);
     }
     Launch L{};
     L.kind = L_SOLID_FUSED;

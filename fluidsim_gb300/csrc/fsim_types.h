@@ -311,7 +311,7 @@ enum LaunchKind {
     L_ZERO, L_HASH, L_SCAN_REDUCE, L_SCAN_PARTIALS, L_SCAN_APPLY, L_SCATTER, L_GATHER_F, L_GATHER_S,
     L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE,
     L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M, L_SOLID_FUSED, L_SOLID_SLOTS,
-    L_FORCE_RECORD, L_FORCE_LISTED
+    L_FORCE_RECORD, L_FORCE_LISTED, L_DEFORM_R, L_DEFORM_M_R
 };
 
 struct Launch {
