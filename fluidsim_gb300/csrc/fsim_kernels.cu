@@ -518,7 +518,7 @@ __device__ __forceinline__ void flush_list(const DevParams &P, const FluidSweepA
     cnt = 0;
 }
 
-template <int SP, bool CHECK_Z, int VISCID, class SH, bool KAHAN = false>
+template <int SP, bool CHECK_Z, int VISCID, class SH, bool KAHAN = false, bool BITS = false>
 __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
                                                int &cnt, bool in, int cz, int cx, int cy, int z0, int z1, float4 pr,
                                                float4 vp, PairAcc &acc)
@@ -537,17 +537,44 @@ __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSw
             while (j < je) {
                 if (__reduce_max_sync(kFull, cnt) > SH::cap - SH::chunk)
                     flush_list<SP, VISCID, KAHAN>(P, A, lst, lane, cnt, pr, vp, acc);
-                const int jend = min(j + SH::chunk, je);
-#pragma unroll 4
-                for (; j < jend; ++j) {
-                    const float4 q = pos[j]; // same address in every lane: a broadcast
-                    const float r2 = dist2(q.x - pr.x, q.y - pr.y, q.z - pr.z);
-                    bool hit = in && r2 < P.R2;
-                    if (CHECK_Z && hit) {
-                        const int czj = (int)__fmul_rn(__fsub_rn(q.z, P.cmin[2]), P.cinv[2]);
-                        hit = abs(czj - cz) <= 1;
+                if (BITS && j + SH::chunk <= je) {
+                    // BITS (the batched sweep): a full chunk's hits as bits,
+                    // appended afterwards in candidate order -- one predicated
+                    // OR per candidate instead of a predicated append; the same
+                    // list.  Measured faster in the batched kernel (ensemble step
+                    // 5.67 -> 5.55 ms) and slower in the one-instance kernel,
+                    // whose 16-candidate chunk then needs 62 registers.
+                    unsigned bits = 0;
+#pragma unroll
+                    for (int c = 0; c < SH::chunk; ++c) {
+                        const float4 q = pos[j + c]; // same address in every lane: a broadcast
+                        const float r2 = dist2(q.x - pr.x, q.y - pr.y, q.z - pr.z);
+                        bool hit = in && r2 < P.R2;
+                        if (CHECK_Z && hit) {
+                            const int czj = (int)__fmul_rn(__fsub_rn(q.z, P.cmin[2]), P.cinv[2]);
+                            hit = abs(czj - cz) <= 1;
+                        }
+                        if (hit) bits |= 1u << c;
                     }
-                    if (hit) lst[cnt++][lane] = j;
+                    while (bits) {
+                        const int c = __ffs(bits) - 1;
+                        bits &= bits - 1;
+                        lst[cnt++][lane] = j + c;
+                    }
+                    j += SH::chunk;
+                } else {
+                    const int jend = min(j + SH::chunk, je);
+#pragma unroll 4
+                    for (; j < jend; ++j) {
+                        const float4 q = pos[j]; // same address in every lane: a broadcast
+                        const float r2 = dist2(q.x - pr.x, q.y - pr.y, q.z - pr.z);
+                        bool hit = in && r2 < P.R2;
+                        if (CHECK_Z && hit) {
+                            const int czj = (int)__fmul_rn(__fsub_rn(q.z, P.cmin[2]), P.cinv[2]);
+                            hit = abs(czj - cz) <= 1;
+                        }
+                        if (hit) lst[cnt++][lane] = j;
+                    }
                 }
             }
         }
@@ -555,7 +582,7 @@ __device__ __forceinline__ void gather_species(const DevParams &P, const FluidSw
     flush_list<SP, VISCID, KAHAN>(P, A, lst, lane, cnt, pr, vp, acc);
 }
 
-template <bool CHECK_Z, int VISCID, class SH>
+template <bool CHECK_Z, int VISCID, class SH, bool BITS = false>
 __device__ __forceinline__ void fluid_sweep_body(const DevParams &P, const FluidSweepArgs &A, int blk)
 {
     __shared__ int lists[SH::warps][SH::cap][32];
@@ -580,9 +607,12 @@ __device__ __forceinline__ void fluid_sweep_body(const DevParams &P, const Fluid
         const int zhi = __reduce_max_sync(kFull, in ? cz : INT_MIN);
         const int z0 = max(zlo - 1, 0), z1 = min(zhi + 1, P.nz - 1) + 1;
         const int cx = grow / P.ny, cy = grow - cx * P.ny;
-        gather_species<kFluid, CHECK_Z, VISCID, SH>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
-        gather_species<kVirt, CHECK_Z, VISCID, SH>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
-        gather_species<kSolid, CHECK_Z, VISCID, SH>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp, acc);
+        gather_species<kFluid, CHECK_Z, VISCID, SH, false, BITS>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp,
+                                                                acc);
+        gather_species<kVirt, CHECK_Z, VISCID, SH, false, BITS>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp,
+                                                               acc);
+        gather_species<kSolid, CHECK_Z, VISCID, SH, false, BITS>(P, A, lst, lane, cnt, in, cz, cx, cy, z0, z1, pr, vp,
+                                                                acc);
     }
     if (valid) fluid_update_store(P, A, i, pr, vp, acc);
 }
@@ -593,7 +623,7 @@ __global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep(const Item<Flui
 {
     const int inst = locate_instance(bstart, ninst, blockIdx.x);
     const DevParams P = items[inst].P;
-    fluid_sweep_body<CHECK_Z, VISCID, SH>(P, items[inst].A, (int)blockIdx.x - bstart[inst]);
+    fluid_sweep_body<CHECK_Z, VISCID, SH, true>(P, items[inst].A, (int)blockIdx.x - bstart[inst]);
 }
 
 // The one-instance sweep takes {params, args} by value: kernel parameters live
