@@ -634,6 +634,17 @@ __global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep_1(const DevPara
     fluid_sweep_body<CHECK_Z, VISCID, SH>(P, A, (int)blockIdx.x);
 }
 
+// The batched sweep with its instances' {params, args} passed by value: one
+// kernel parameter block (in the constant bank, like the one-instance
+// sweep's), up to kSweepParamItems instances.
+template <bool CHECK_Z, int VISCID, class SH>
+__global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep_p(const __grid_constant__ SweepBatchParams B)
+{
+    const int inst = locate_instance(B.bstart, B.n, blockIdx.x);
+    const Item<FluidSweepArgs> &it = B.it[inst];
+    fluid_sweep_body<CHECK_Z, VISCID, SH, true>(it.P, it.A, (int)blockIdx.x - B.bstart[inst]);
+}
+
 // ------------------------------------------------------- virtual particles
 // getVirtData (src/virt.cu:9-75): nearest fluid particle's rho, hydrostatically
 // corrected p and velocity mirrored about the (static) wall normal.  Ties in
@@ -2108,6 +2119,14 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
 {
     using SweepFn = void (*)(const Item<FluidSweepArgs> *, const int *, int);
     using Sweep1Fn = void (*)(const DevParams, const FluidSweepArgs);
+    using SweepPFn = void (*)(const SweepBatchParams);
+    static const SweepPFn sweepsp[6][kSweepShapes] = {
+        {kb_fluid_sweep_p<false, 0, Shape0>, kb_fluid_sweep_p<false, 0, Shape1>, kb_fluid_sweep_p<false, 0, Shape2>},
+        {kb_fluid_sweep_p<false, 1, Shape0>, kb_fluid_sweep_p<false, 1, Shape1>, kb_fluid_sweep_p<false, 1, Shape2>},
+        {kb_fluid_sweep_p<false, 2, Shape0>, kb_fluid_sweep_p<false, 2, Shape1>, kb_fluid_sweep_p<false, 2, Shape2>},
+        {kb_fluid_sweep_p<true, 0, Shape0>, kb_fluid_sweep_p<true, 0, Shape1>, kb_fluid_sweep_p<true, 0, Shape2>},
+        {kb_fluid_sweep_p<true, 1, Shape0>, kb_fluid_sweep_p<true, 1, Shape1>, kb_fluid_sweep_p<true, 1, Shape2>},
+        {kb_fluid_sweep_p<true, 2, Shape0>, kb_fluid_sweep_p<true, 2, Shape1>, kb_fluid_sweep_p<true, 2, Shape2>}};
     // [variant][shape]; variants 0-5: plain (CHECK_Z, VISCID); 6-8: mixed (VISCID)
     static const SweepFn sweeps[9][kSweepShapes] = {
         {kb_fluid_sweep<false, 0, Shape0>, kb_fluid_sweep<false, 0, Shape1>, kb_fluid_sweep<false, 0, Shape2>},
@@ -2153,6 +2172,12 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
                 if (n == 1) {
                     const Item<FluidSweepArgs> &it = host_item<FluidSweepArgs>(pl, L);
                     sweeps1[L.variant][shape]<<<gs, thr, 0, st>>>(it.P, it.A);
+                } else if (L.variant < 6 && n <= kSweepParamItems) {
+                    static thread_local SweepBatchParams B;
+                    B.n = n;
+                    std::memcpy(B.bstart, pl.host.data() + L.shape_table_off[shape], sizeof(int) * (n + 1));
+                    std::memcpy(B.it, pl.host.data() + L.items_off, sizeof(Item<FluidSweepArgs>) * n);
+                    sweepsp[L.variant][shape]<<<gs, thr, 0, st>>>(B);
                 } else {
                     sweeps[L.variant][shape]<<<gs, thr, 0, st>>>(items_of<FluidSweepArgs>(pl, L), tbs, n);
                 }

@@ -185,6 +185,16 @@ struct SolidArgs {
     unsigned *flags;       // this instance's error flags
 };
 
+// the batched sweep's instances passed by value as one kernel parameter block
+// (at most 32,764 bytes of kernel parameters)
+constexpr int kSweepParamItems = 72;
+struct SweepBatchParams {
+    int n;
+    int bstart[kSweepParamItems + 1];
+    Item<FluidSweepArgs> it[kSweepParamItems];
+};
+static_assert(sizeof(SweepBatchParams) <= 32764, "kernel parameter limit");
+
 // ---- device case generator (fsim_create_case): lattice rows and their bases
 struct CaseGeom {
     int T[3], FN[3], SL[3], SN[3];
