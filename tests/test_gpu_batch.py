@@ -57,6 +57,28 @@ def test_batch_members_equal_standalone(steps):
         s.close()
 
 
+def test_large_batch_uses_the_item_array_sweep_and_equals_standalone():
+    """A plain-form batch larger than the sweep's by-value parameter block (72
+    instances) reads its items from global memory: the same results as each
+    member alone, bit for bit."""
+    members = [cases.make(cases.tiny_box(jitter=0.01, seed=100 + k, fluid=(8 + k % 5, 10, 8))) for k in range(80)]
+    alone = []
+    for cfg, pa in members:
+        with api.Simulation(cfg, pa, device=0) as s:
+            s.step(4)
+            s.sync()
+            alone.append({f: s.get(f) for f in ("fluid_pos", "fluid_vel", "fluid_p", "solid_pos")})
+    sims = [api.Simulation(cfg, pa, device=0) for cfg, pa in members]
+    with api.Batch(sims) as b:
+        b.step(4)
+        b.sync()
+        for k, s in enumerate(sims):
+            for f, want in alone[k].items():
+                assert np.array_equal(s.get(f), want), (k, f)
+    for s in sims:
+        s.close()
+
+
 def test_batch_rejects_misuse():
     (cfg, pa), = _members()[:1]
     s = api.Simulation(cfg, pa, device=0)
