@@ -189,14 +189,16 @@ def run_reference(args, dist):
         return 0
     cfg, pa = workload(args)
     cores = os.cpu_count() or 1
-    # one untimed warm-up step sizes the sample: at most K steps and about 45 s
-    _, t1 = cpu_oracle_rate(cfg, pa, "f32", 1, cores)
-    steps = max(1, min(args.steps, int(45.0 / max(t1, 1e-3))))
+    # W untimed warm-up steps (at most 5, so the CPU arm stays within minutes);
+    # their time sizes the sample: at most K steps and about 45 s
+    warm = max(1, min(args.warmup, 5))
+    _, tw = cpu_oracle_rate(cfg, pa, "f32", warm, cores)
+    steps = max(1, min(args.steps, int(45.0 / max(tw / warm, 1e-3))))
     rate, dt = cpu_oracle_rate(cfg, pa, "f32", steps, cores)
     desc = workload_desc(cfg, pa)
     line = {
         "impl": "reference", "metric": "particle-updates/s", "value": rate, "unit": "particle-updates/s",
-        "n_gpus": args.gpus, "steps": steps, "warmup": 1, "ms_per_step": dt * 1e3 / steps,
+        "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": dt * 1e3 / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": desc,
         "cpu_baseline": {"value": rate, "unit": "particle-updates/s", "cores": cores, "kind": "port",
