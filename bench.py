@@ -203,7 +203,8 @@ def run_reference(args, dist):
         "config": desc,
         "cpu_baseline": {"value": rate, "unit": "particle-updates/s", "cores": cores, "kind": "port",
                          "sample": "%d fluid steps of the full workload (oracle FP32 restatement of the "
-                                   "reference CUDA path, OpenMP), sized to ~45 s" % steps},
+                                   "reference CUDA path, OpenMP) in %.1f s: at most --steps, about 45 s at most"
+                                   % (steps, dt)},
         "e2e": {"value": rate, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference is a CUDA-only program; its CUDA sources need the unvendored glm library and are "
                 "not built here, so the reference arm is the CPU restatement of its algorithm",
