@@ -123,6 +123,22 @@ __device__ __forceinline__ int locate_instance(const int *__restrict__ bstart, i
         BODY(P, A, (int)blockIdx.x - bstart[inst]);                                                       \
     }
 
+// The same kernel in two more launch forms whose parameters sit in the constant
+// bank: one instance by value (NAME_1), and up to ParamBlock<ARGS>::kMax
+// instances as one __grid_constant__ parameter block (NAME_p).  Only for
+// bodies whose arithmetic spells out every rounding, so that all forms agree.
+#define FSIM_BATCHED_KERNEL_P(NAME, ARGS, BODY, BOUNDS)                                                    \
+    FSIM_BATCHED_KERNEL(NAME, ARGS, BODY, BOUNDS)                                                         \
+    __global__ void __launch_bounds__(BOUNDS) NAME##_1(const DevParams P, const ARGS A)                   \
+    {                                                                                                     \
+        BODY(P, A, (int)blockIdx.x);                                                                      \
+    }                                                                                                     \
+    __global__ void __launch_bounds__(BOUNDS) NAME##_p(const __grid_constant__ ParamBlock<ARGS> B)        \
+    {                                                                                                     \
+        const int inst = locate_instance(B.bstart, B.n, blockIdx.x);                                      \
+        BODY(B.it[inst].P, B.it[inst].A, (int)blockIdx.x - B.bstart[inst]);                               \
+    }
+
 // ------------------------------------------------------- counting sort
 // A slot in cell c's count: lanes of a warp with the same cell share one
 // atomic (particles arrive sorted by their previous cell, so a warp holds few
@@ -1584,9 +1600,9 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
     S.couple[i] = make_float4(cx, cy, cz, 0.0f);
     S.dudt[i] = make_float4(__fadd_rn(ax, cx), __fadd_rn(ay, cy), __fadd_rn(az, cz), 0.0f);
 }
-FSIM_BATCHED_KERNEL(kb_solid_force, SolidArgs, solid_force_body<false>, kBlock)
-FSIM_BATCHED_KERNEL(kb_solid_force_record, SolidArgs, (solid_force_body<false, 1>), kBlock)
-FSIM_BATCHED_KERNEL(kb_solid_force_listed, SolidArgs, (solid_force_body<false, 2>), kBlock)
+FSIM_BATCHED_KERNEL_P(kb_solid_force, SolidArgs, solid_force_body<false>, kBlock)
+FSIM_BATCHED_KERNEL_P(kb_solid_force_record, SolidArgs, (solid_force_body<false, 1>), kBlock)
+FSIM_BATCHED_KERNEL_P(kb_solid_force_listed, SolidArgs, (solid_force_body<false, 2>), kBlock)
 FSIM_BATCHED_KERNEL(kb_solid_force_mixed, SolidArgs, solid_force_body<true>, kBlock)
 
 // solidUpdate (src/solid.cu:209-239)
@@ -2112,6 +2128,20 @@ __global__ void __launch_bounds__(kBlock) k_conservation_solid(const DevParams P
 namespace fsim_rt {
 
 #define FSIM_LAUNCH(KB, ARGS, THREADS) KB<<<g, THREADS, 0, st>>>(items_of<ARGS>(pl, L), tb, n)
+// one instance by value; up to ParamBlock<ARGS>::kMax as a parameter block; else the item array
+#define FSIM_LAUNCH_P(KB, ARGS, THREADS)                                                                    \
+    if (n == 1) {                                                                                          \
+        const Item<ARGS> &it1 = host_item<ARGS>(pl, L);                                                    \
+        KB##_1<<<g, THREADS, 0, st>>>(it1.P, it1.A);                                                       \
+    } else if (n <= ParamBlock<ARGS>::kMax) {                                                              \
+        static thread_local ParamBlock<ARGS> B;                                                            \
+        B.n = n;                                                                                           \
+        std::memcpy(B.bstart, pl.host.data() + L.table_off, sizeof(int) * (n + 1));                        \
+        std::memcpy(B.it, pl.host.data() + L.items_off, sizeof(Item<ARGS>) * n);                           \
+        KB##_p<<<g, THREADS, 0, st>>>(B);                                                                  \
+    } else {                                                                                               \
+        KB<<<g, THREADS, 0, st>>>(items_of<ARGS>(pl, L), tb, n);                                           \
+    }
 
 // Enqueue a plan's launches; optional events around the fluid sweep.
 fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0, cudaEvent_t sweep1,
@@ -2186,9 +2216,9 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
             if (sweep1) CK(cudaEventRecordWithFlags(sweep1, st, sweep_flags));
             break;
         case L_DEFORM: FSIM_LAUNCH(kb_solid_deform, SolidArgs, kBlock); break;
-        case L_FORCE: FSIM_LAUNCH(kb_solid_force, SolidArgs, kBlock); break;
-        case L_FORCE_RECORD: FSIM_LAUNCH(kb_solid_force_record, SolidArgs, kBlock); break;
-        case L_FORCE_LISTED: FSIM_LAUNCH(kb_solid_force_listed, SolidArgs, kBlock); break;
+        case L_FORCE: { FSIM_LAUNCH_P(kb_solid_force, SolidArgs, kBlock); } break;
+        case L_FORCE_RECORD: { FSIM_LAUNCH_P(kb_solid_force_record, SolidArgs, kBlock); } break;
+        case L_FORCE_LISTED: { FSIM_LAUNCH_P(kb_solid_force_listed, SolidArgs, kBlock); } break;
         case L_UPDATE: FSIM_LAUNCH(kb_solid_update, SolidArgs, kBlock); break;
         case L_SOLID_SLOTS: FSIM_LAUNCH(kb_solid_slots, SolidArgs, kBlock); break;
         case L_DEFORM_R: FSIM_LAUNCH(kb_solid_deform_resolve, SolidArgs, kBlock); break;
@@ -2335,3 +2365,5 @@ void launch_k_case_generate(int grid, cudaStream_t st, const CaseGenArgs A)
 }
 
 } // namespace fsim_rt
+static_assert(sizeof(fsim_rt::ParamBlock<fsim_rt::SolidArgs>) <= 32764, "parameter block size");
+static_assert(fsim_rt::ParamBlock<fsim_rt::SolidArgs>::kMax >= 64, "a 64-instance ensemble fits");

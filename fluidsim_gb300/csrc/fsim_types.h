@@ -185,6 +185,16 @@ struct SolidArgs {
     unsigned *flags;       // this instance's error flags
 };
 
+// a batched kernel's instances passed by value as one kernel parameter block
+// (at most 32,764 bytes of kernel parameters)
+template <class ARGS>
+struct ParamBlock {
+    static constexpr int kMax = (32764 - 16) / (int)(sizeof(Item<ARGS>) + sizeof(int));
+    int n;
+    int bstart[kMax + 1];
+    Item<ARGS> it[kMax];
+};
+
 // the batched sweep's instances passed by value as one kernel parameter block
 // (at most 32,764 bytes of kernel parameters)
 constexpr int kSweepParamItems = 72;
