@@ -27,11 +27,21 @@ virtual walls, fused fluid sweep + update, 4 solid sub-steps) over the
   particle-step; ``roofline_fp32`` against the measured FP32 FMA peak.
 * ``cpu_baseline``: the FP64 CPU oracle on this host's cores, 2 steps of the
   same workload; ``single_thread``: one step of it on one thread.
+* ``reference_build``: the reference's own CUDA kernels (its unmodified
+  src/pair.cu, fluid.cu, virt.cu, solid.cu, compiled for sm_103a with its
+  Release flags; oracle/refcuda) on the same workload and GPU, with the
+  reference's launch shapes and a synchronisation after every launch.
+* ``forms``: the small dam break for its 2000 steps beside the reference build
+  (``config0``), the mixed-precision form, the batched 64-instance ensemble and
+  the served request stream.
 
-``--impl reference`` times the CPU restatement of the reference path (FP32
-oracle, all host threads): the reference itself is a CUDA program with no CPU
-path, and its CUDA sources cannot be built here (they need the unvendored glm
-library).  Multi-GPU: replicas only (independent instances, no collective).
+``--impl reference`` times the reference build on the GPU (the reference is a
+CUDA program with no CPU path); where its device image is absent it falls back
+to the CPU restatement of its algorithm (FP32 oracle, all host threads), which
+it also samples for ``cpu_baseline``.  ``--cpu-full`` times the FP64 oracle on
+the small dam break for all 2000 steps and on 200 steps of the 4M case, on all
+host cores and on one thread (minutes; not part of the default run).
+Multi-GPU: replicas only (independent instances, no collective).
 """
 import argparse
 import json
@@ -183,34 +193,100 @@ def cpu_oracle_rate(cfg, pa, precision, steps, threads=0):
     return (pa.n_fluid + pa.n_solid) * steps / dt, dt
 
 
+def reference_build_rate(cfg, pa, steps, warmup, dev=0):
+    """The reference's own CUDA kernels (unmodified src/*.cu, Release flags,
+    sm_103a; oracle/refcuda) on this GPU through the harness that restates its
+    host loop: particle-updates/s over `steps` steps after `warmup`, CUDA
+    events on the default stream, a device synchronisation after every launch
+    as in the reference.  None when the device image is absent."""
+    from oracle import refbuild
+
+    if not refbuild.available("release"):
+        return None
+    with refbuild.RefBuildSim(cfg, pa, "release", device=dev) as ref:
+        ref.step(warmup)
+        ms = ref.time_steps(steps)
+    return {"value": (pa.n_fluid + pa.n_solid) * steps / (ms * 1e-3), "unit": "particle-updates/s",
+            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup, "thread_num": cfg.thread_num,
+            "build": "reference CUDA kernels (src/pair.cu, fluid.cu, virt.cu, solid.cu, unmodified) for sm_103a "
+                     "with -O3 -Xptxas -dlcm=cg -use_fast_math, glm subset written here; host loop of "
+                     "src/calculation.cu:20-35 restated (oracle/refcuda/ref_harness.cpp)"}
+
+
 def run_reference(args, dist):
-    """CPU restatement of the reference path (FP32 oracle, all host threads)."""
+    """The reference arm: the reference's own CUDA build on this GPU (its
+    kernels are the whole of its hot path; it has no CPU path).  Where the
+    device image is absent, the CPU restatement of its algorithm instead."""
     if dist.rank != 0:
         return 0
     cfg, pa = workload(args)
     cores = os.cpu_count() or 1
-    # W untimed warm-up steps (at most 5, so the CPU arm stays within minutes);
-    # their time sizes the sample: at most K steps and about 45 s
-    warm = max(1, min(args.warmup, 5))
-    _, tw = cpu_oracle_rate(cfg, pa, "f32", warm, cores)
-    steps = max(1, min(args.steps, int(45.0 / max(tw / warm, 1e-3))))
-    rate, dt = cpu_oracle_rate(cfg, pa, "f32", steps, cores)
     desc = workload_desc(cfg, pa)
-    line = {
-        "impl": "reference", "metric": "particle-updates/s", "value": rate, "unit": "particle-updates/s",
-        "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": dt * 1e3 / steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": desc,
-        "cpu_baseline": {"value": rate, "unit": "particle-updates/s", "cores": cores, "kind": "port",
-                         "sample": "%d fluid steps of the full workload (oracle FP32 restatement of the "
-                                   "reference CUDA path, OpenMP) in %.1f s: at most --steps, about 45 s at most"
-                                   % (steps, dt)},
-        "e2e": {"value": rate, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference is a CUDA-only program; its CUDA sources need the unvendored glm library and are "
-                "not built here, so the reference arm is the CPU restatement of its algorithm",
-    }
+    # CPU restatement (FP32 oracle, all host threads): a short bounded sample
+    warm = 1
+    _, tw = cpu_oracle_rate(cfg, pa, "f32", warm, cores)
+    cpu_steps = max(1, min(args.steps, int(20.0 / max(tw / warm, 1e-3))))
+    cpu_rate, cpu_dt = cpu_oracle_rate(cfg, pa, "f32", cpu_steps, cores)
+    cpu = {"value": cpu_rate, "unit": "particle-updates/s", "cores": cores, "kind": "port",
+           "sample": "%d fluid steps of the full workload in the FP32 CPU restatement of the reference path "
+                     "(OpenMP, all host threads) in %.1f s, after 1 untimed step; at most --steps, about 20 s"
+                     % (cpu_steps, cpu_dt)}
+    ref = None
+    try:
+        ref = reference_build_rate(cfg, pa, args.steps, max(args.warmup, 3), dist.local)
+    except Exception as e:  # the reference build failing is reported, not hidden
+        ref = None
+        cpu["reference_build_error"] = str(e)
+    if ref is not None:
+        line = {
+            "impl": "reference", "metric": "particle-updates/s", "value": ref["value"], "unit": "particle-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": ref["warmup"], "ms_per_step": ref["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": desc, "reference_build": ref, "cpu_baseline": cpu,
+            "e2e": {"value": ref["value"], "unit": "particle-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference is a CUDA program; its own kernels run here on the GPU, state resident for "
+                    "the whole run as in the reference (its loop copies nothing per step); cpu_baseline is the "
+                    "CPU restatement of the same path, a separate sample",
+        }
+    else:
+        line = {
+            "impl": "reference", "metric": "particle-updates/s", "value": cpu_rate, "unit": "particle-updates/s",
+            "n_gpus": args.gpus, "steps": cpu_steps, "warmup": warm, "ms_per_step": cpu_dt * 1e3 / cpu_steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": desc, "cpu_baseline": cpu,
+            "e2e": {"value": cpu_rate, "unit": "particle-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference build's device image is absent, so the reference arm is the CPU restatement "
+                    "of its algorithm",
+        }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_config0(dev, steps=2000):
+    """The small dam break (32,000 fluid, 3,680 solid, 144,216 wall particles,
+    dt 1e-4, 4 sub-steps) for its full 2000 steps: this build and the
+    reference build on the same GPU."""
+    from fluidsim_gb300 import api, cases
+
+    cfg, pa = cases.make(cases.small_dam_break())
+    nupd = pa.n_fluid + pa.n_solid
+    with api.Simulation(cfg, pa, device=dev) as sim:
+        sim.step(10)
+        sim.sync()
+        ms = sim.time_steps(steps)
+    out = {"workload": "small dam break: %d fluid + %d solid + %d wall particles, dx=0.01, dt=1e-4, %d steps "
+                       "after 10 warm-up steps" % (pa.n_fluid, pa.n_solid, pa.n_virt, steps),
+           "value": nupd * steps / (ms * 1e-3), "ms_per_step": ms / steps, "unit": "particle-updates/s"}
+    try:
+        ref = reference_build_rate(cfg, pa, steps, 10, dev)
+    except Exception as e:
+        ref = {"error": str(e)}
+    out["reference_build"] = ref
+    if ref and "value" in ref:
+        out["ratio_vs_reference_build"] = out["value"] / ref["value"]
+    return out
 
 
 def run_gb300(args, dist):
@@ -297,10 +373,22 @@ def run_gb300(args, dist):
 
     sim.close()
 
-    # ---- the batched form on the ensemble workload
+    # ---- the reference build on the same workload and GPU (its own kernels)
+    ref_build = None
+    if not args.no_forms:
+        try:
+            ref_build = reference_build_rate(cfg, pa, max(10, min(args.steps, 50)), 3, dev)
+        except Exception as e:
+            ref_build = {"error": str(e)}
+        if ref_build and "value" in ref_build:
+            ref_build["ratio_device"] = value / ref_build["value"]
+            ref_build["ratio_e2e"] = e2e / ref_build["value"]
+
+    # ---- the other forms and the small dam break
     forms = None
     if not args.no_forms:
-        forms = {"mixed": run_mixed(dev, max(10, min(args.steps, 100))),
+        forms = {"config0": run_config0(dev),
+                 "mixed": run_mixed(dev, max(10, min(args.steps, 100))),
                  "ensemble64": run_ensemble(dev, max(10, min(args.steps, 50))), "served": run_served(dev)}
 
     # ---- CPU baseline (rank 0, N=1 only)
@@ -335,6 +423,7 @@ def run_gb300(args, dist):
             "autotuner": tuning,
             "phases_ms_per_step": phases,
             "cpu_baseline": cpu,
+            "reference_build": ref_build,
             "clocks": clk,
             "forms": forms,
             "gpu_launches": launches * args.steps,
@@ -500,6 +589,28 @@ def run_served(dev):
             "throughput_ratio": batched["throughput"] / plain["throughput"]}
 
 
+def run_cpu_full(args):
+    """The FP64 CPU oracle on the two plain workloads as the measurement plan
+    asks: the small dam break for all 2000 steps and the 4M case for 200 steps,
+    on every host core; one thread on 20 and 2 steps of them (per-step rates
+    extrapolate, the oracle's cost per step varies little)."""
+    from fluidsim_gb300 import cases
+
+    cores = os.cpu_count() or 1
+    out = {"cores": cores, "unit": "particle-updates/s", "kind": "port (FP64 oracle, OpenMP)"}
+    for name, make, steps, steps1 in (("small_dam_break", cases.small_dam_break, 2000, 20),
+                                      ("fsi_4m", cases.fsi_4m, 200, 2)):
+        cfg, pa = cases.make(make())
+        rate, dt = cpu_oracle_rate(cfg, pa, "f64", steps, cores)
+        rate1, dt1 = cpu_oracle_rate(cfg, pa, "f64", steps1, 1)
+        out[name] = {"all_cores": rate, "all_cores_steps": steps, "all_cores_s": dt,
+                     "one_thread": rate1, "one_thread_steps": steps1, "one_thread_s": dt1,
+                     "particles": pa.n_fluid + pa.n_solid, "wall_particles": pa.n_virt}
+        print(json.dumps({name: out[name]}), flush=True)
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_profile(args):
     """Fewest launches for an ncu capture: creation, then N graph-free steps
     (the same kernels as the timed region).  --profile-form picks the plain
@@ -538,11 +649,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--profile-form", choices=("plain", "mixed", "ensemble"), default="plain")
+    ap.add_argument("--cpu-full", action="store_true",
+                    help="time the FP64 oracle on the small dam break (2000 steps) and the 4M case (200 steps)")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling run for ncu: create the workload, run this many steps, print nothing else")
     args = ap.parse_args()
     if args.profile_steps:
         return run_profile(args)
+    if args.cpu_full:
+        return run_cpu_full(args)
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     dist = Dist()

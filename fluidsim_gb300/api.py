@@ -51,6 +51,7 @@ class Config(C.Structure):
         ("keep_derivatives", C.c_int),
         ("solid_fused", C.c_int),
         ("solid_full_walk", C.c_int),
+        ("barrier_wait_polls", C.c_int),
     ]
 
     def as_dict(self):

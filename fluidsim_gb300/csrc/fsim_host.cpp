@@ -200,6 +200,8 @@ fsim_status config_from_values(const IniValues &ini, fsim_config *c)
     c->keep_derivatives = ini.get_bool("gb300_keep_derivatives", false) ? 1 : 0;
     c->solid_fused = ini.get_bool("gb300_solid_fused", false) ? 1 : 0;
     c->solid_full_walk = ini.get_bool("gb300_solid_full_walk", false) ? 1 : 0;
+    c->barrier_wait_polls = ini.get("gb300_barrier_wait_polls", 0);
+    if (c->barrier_wait_polls < 0) c->barrier_wait_polls = 0;
 
     // validity checks of the readers (src/kernel.cpp:16-20, src/domain.cpp:19-23,
     // src/sim_time.cpp:17-21); the reference throws, we return EINVAL

@@ -272,13 +272,23 @@ __device__ __forceinline__ void scatter_body(const DevParams &, const ScatterArg
 FSIM_BATCHED_KERNEL(kb_scatter, ScatterArgs, scatter_body, kBlock)
 
 // Rank inside the cell by previous position: the new order is sorted by
-// (cell, previous sorted position), a stable and deterministic order.
+// (cell, previous sorted position), a stable and deterministic order.  The
+// scan costs the cell's count per particle, so a cell of more than
+// kStableRankMax particles (only out-of-grid input clamped into a boundary
+// cell, or a smoothing length of several particle spacings, makes one) keeps
+// the scatter's order and raises FLAG_CELL_OVERFULL: bounded work, and the
+// step reports the failure.
 __device__ __forceinline__ int stable_dst(const int *__restrict__ tmp, const int *__restrict__ key,
-                                          const int *__restrict__ start, int d, int &src, int &cell)
+                                          const int *__restrict__ start, int d, int &src, int &cell,
+                                          unsigned *flags)
 {
     src = tmp[d];
     cell = key[src];
     const int b = start[cell], e = start[cell + 1];
+    if (e - b > kStableRankMax) {
+        if (d == b && flags) atomicOr(flags, FLAG_CELL_OVERFULL);
+        return d;
+    }
     int rank = 0;
     for (int t = b; t < e; ++t) rank += tmp[t] < src;
     return b + rank;
@@ -289,7 +299,7 @@ __device__ __forceinline__ void gather_fluid_body(const DevParams &, const Gathe
     const int d = blk * blockDim.x + threadIdx.x;
     if (d >= A.n) return;
     int src, cell;
-    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell);
+    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell, A.flags);
     A.posr_out[dst] = A.posr_in[src];
     A.velp_out[dst] = A.velp_in[src];
     A.orig_out[dst] = A.orig_in[src];
@@ -316,7 +326,7 @@ __device__ __forceinline__ void gather_solid_body(const DevParams &P, const Gath
     const int d = blk * blockDim.x + threadIdx.x;
     if (d >= A.n) return;
     int src, cell;
-    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell);
+    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell, A.flags);
     A.pos_out[dst] = A.pos_in[src];
     A.vel_out[dst] = A.vel_in[src];
     A.ref_out[dst] = A.ref_in[src];
@@ -331,9 +341,15 @@ FSIM_BATCHED_KERNEL(kb_gather_solid, GatherSolidArgs, gather_solid_body, kBlock)
 
 // ------------------------------------------------------------ EOS
 // densityToPressure (src/fluid.cu:16-24): Tait EOS, floored at min_pressure.
+// The accurate powf, not the fast-math __powf that the reference's release
+// build compiles it to: (rho/rho0)^gamma - 1 is a cancellation near rho0, and
+// __powf's log2 approximation has an absolute error there that is large next
+// to the small difference (it dominated the pressure error against FP64 in the
+// reference build and in a first version of this kernel alike).  Once per
+// particle per step, so its cost is negligible.
 __device__ __forceinline__ float tait_pressure(const DevParams &P, float rho)
 {
-    const float p = (__powf(rho * P.rho0_inv, P.gamma) - 1.0f) * P.rho2p;
+    const float p = (powf(rho * P.rho0_inv, P.gamma) - 1.0f) * P.rho2p;
     return fmaxf(p, P.min_p);
 }
 
@@ -1797,7 +1813,9 @@ __global__ void k_probe(const DevParams P, const ProbeArgs A)
 // of spinning for ever.
 constexpr unsigned kBarrierSpinLimit = 1u << 22; // x ~64 ns sleeps: about a quarter of a second and more
 
-__device__ __forceinline__ void grid_sync(GridBarrier *b, bool &ok)
+// `limit`: polls before giving up (kBarrierSpinLimit unless the configuration
+// asks for fewer, gb300_barrier_wait_polls)
+__device__ __forceinline__ void grid_sync(GridBarrier *b, bool &ok, unsigned limit)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1811,7 +1829,7 @@ __device__ __forceinline__ void grid_sync(GridBarrier *b, bool &ok)
         } else {
             unsigned spins = 0;
             while (*vgen == g) {
-                if (++spins > kBarrierSpinLimit) {
+                if (++spins > limit) {
                     ok = false;
                     break;
                 }
@@ -1820,13 +1838,15 @@ __device__ __forceinline__ void grid_sync(GridBarrier *b, bool &ok)
         }
         __threadfence();
     }
-    __syncthreads();
+    // thread 0 alone waited: every thread of the CTA learns whether it gave up
+    ok = __syncthreads_and(ok) != 0;
 }
 
 struct SolidFusedArgs {
     const int *bstart_w, *bstart_t; // prefix tables: kSolidGroup lanes per particle / thread per particle
     int ninst, max_sub;
     GridBarrier *barrier;
+    unsigned polls; // barrier wait limit
 };
 
 template <bool MIXED>
@@ -1835,28 +1855,32 @@ __global__ void __launch_bounds__(kBlock, 3) kb_solid_fused(const Item<SolidArgs
 {
     const int total_w = F.bstart_w[F.ninst], total_t = F.bstart_t[F.ninst];
     bool ok = true;
-    for (int k = 0; k < F.max_sub; ++k) {
+    // a CTA whose wait gave up leaves at once (the CTAs still waiting for it
+    // give up in turn after their own bounded wait)
+    for (int k = 0; k < F.max_sub && ok; ++k) {
         for (int b = blockIdx.x; b < total_w; b += gridDim.x) {
             const int inst = locate_instance(F.bstart_w, F.ninst, b);
             if (k >= items[inst].A.nsub) continue;
             const DevParams P = items[inst].P;
             solid_deform_body<MIXED>(P, items[inst].A, b - F.bstart_w[inst]);
         }
-        grid_sync(F.barrier, ok);
+        grid_sync(F.barrier, ok, F.polls);
+        if (!ok) break;
         for (int b = blockIdx.x; b < total_w; b += gridDim.x) {
             const int inst = locate_instance(F.bstart_w, F.ninst, b);
             if (k >= items[inst].A.nsub) continue;
             const DevParams P = items[inst].P;
             solid_force_body<MIXED>(P, items[inst].A, b - F.bstart_w[inst]);
         }
-        grid_sync(F.barrier, ok);
+        grid_sync(F.barrier, ok, F.polls);
+        if (!ok) break;
         for (int b = blockIdx.x; b < total_t; b += gridDim.x) {
             const int inst = locate_instance(F.bstart_t, F.ninst, b);
             if (k >= items[inst].A.nsub) continue;
             const DevParams P = items[inst].P;
             solid_update_body(P, items[inst].A, b - F.bstart_t[inst]);
         }
-        if (k + 1 < F.max_sub) grid_sync(F.barrier, ok);
+        if (k + 1 < F.max_sub) grid_sync(F.barrier, ok, F.polls);
     }
     if (!ok && threadIdx.x == 0)
         for (int inst = 0; inst < F.ninst; ++inst) atomicOr(items[inst].A.flags, FLAG_BARRIER_TIMEOUT);
@@ -2235,6 +2259,7 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
             F.bstart_t = reinterpret_cast<const int *>(pl.arena + L.table2_off);
             F.ninst = n;
             F.max_sub = L.max_sub;
+            F.polls = L.polls ? L.polls : kBarrierSpinLimit;
             F.barrier = reinterpret_cast<GridBarrier *>(pl.arena + L.barrier_off);
             CK(cudaMemsetAsync(F.barrier, 0, sizeof(GridBarrier), st));
             cudaLaunchConfig_t lc = {};

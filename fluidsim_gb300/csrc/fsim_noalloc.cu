@@ -18,8 +18,6 @@
 
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 namespace {
 
 constexpr int kMaxParticles = FSIM_NOALLOC_MAX_PARTICLES;
@@ -98,7 +96,12 @@ __global__ void k_na_scatter(const int *__restrict__ key, const int *__restrict_
     if (s < np) tmp[start[key[s]] + slot[s]] = s;
 }
 
-// final slot = cell start + number of same-cell particles with a smaller input index
+// final slot = cell start + number of same-cell particles with a smaller input
+// index.  The scan costs the cell's count per particle; a cell of more than
+// kRankMax particles (positions outside the grid or NaN, clamped into one
+// boundary cell, or a smoothing length of several particle spacings) keeps the
+// scatter's order instead, so the work stays bounded.
+constexpr int kRankMax = FSIM_NOALLOC_RANK_MAX;
 __global__ void k_na_rank(const int *__restrict__ key, const int *__restrict__ start, const int *__restrict__ tmp,
                           int *__restrict__ ids, int np)
 {
@@ -107,40 +110,31 @@ __global__ void k_na_rank(const int *__restrict__ key, const int *__restrict__ s
     const int src = tmp[d];
     const int c = key[src];
     const int b = start[c], e = start[c + 1];
+    if (e - b > kRankMax) {
+        ids[d] = src;
+        return;
+    }
     int rank = 0;
     for (int t = b; t < e; ++t) rank += tmp[t] < src;
     ids[b + rank] = src;
 }
 
-// Device address of the scratch array, looked up once per device.  In host
-// code g_sort_scratch names a host-side stand-in, never the device memory.
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-int *g_scratch_ptr[kMaxDevices] = {};
-
+// Device address of the scratch array on the current device.  In host code
+// g_sort_scratch names a host-side stand-in, never the device memory.  The
+// address is looked up on every call (a table lookup in the runtime once the
+// module is loaded on the device) rather than cached, so that it stays right
+// after cudaDeviceReset or a new primary context reloads the module.  The
+// first call on a device loads the module there, so make it before any stream
+// capture.
 fsim_status scratch_for_current_device(int **out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
     if (e != cudaSuccess) {
-        fsim_set_error("cudaGetDevice failed: %s", cudaGetErrorString(e));
+        fsim_set_error("cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
         return FSIM_ECUDA;
     }
-    if (dev < 0 || dev >= kMaxDevices) {
-        fsim_set_error("device %d out of range", dev);
-        return FSIM_EINVAL;
-    }
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_sort_scratch);
-        if (e != cudaSuccess) {
-            fsim_set_error("cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
-            return FSIM_ECUDA;
-        }
-        g_scratch_ptr[dev] = (int *)p;
-    }
-    *out = g_scratch_ptr[dev];
+    *out = (int *)p;
     return FSIM_OK;
 }
 

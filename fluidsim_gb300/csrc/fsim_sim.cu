@@ -355,12 +355,12 @@ void plan_cell(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
     for (fsim_sim *h : m) {
         gf.push_back({h->P, GatherFluidArgs{h->f_tmp, h->f_key, h->f_start, h->nf, h->f_posr[pf], h->f_velp[pf],
                                             h->f_orig[pf], h->f_posr[1 - pf], h->f_velp[1 - pf], h->f_orig[1 - pf],
-                                            h->f_cell}});
+                                            h->f_cell, h->d_flags}});
         gfb.push_back(blocks_for(h->nf, kBlock));
         gs.push_back({h->P, GatherSolidArgs{h->s_tmp, h->s_key, h->s_start, h->ns, h->s_pos[ps], h->s_vel[ps],
                                             h->s_ref[ps], h->s_type[ps], h->s_orig[ps], h->s_pos[1 - ps],
                                             h->s_vel[1 - ps], h->s_ref[1 - ps], h->s_type[1 - ps], h->s_orig[1 - ps],
-                                            h->s_cell, h->s_inv, h->s_cxyz}});
+                                            h->s_cell, h->s_inv, h->s_cxyz, h->d_flags}});
         gsb.push_back(blocks_for(h->ns, kBlock));
     }
     add_launch(pl, ab, L_GATHER_F, gf, gfb);
@@ -531,6 +531,15 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
     L.blocks = fused_grid(mixed, std::max(tw.back(), tt.back()));
     L.variant = mixed ? 1 : 0;
     L.max_sub = max_sub;
+    // the longest wait any member allows (0 = the kernel's default)
+    L.polls = 0;
+    for (fsim_sim *h : m) {
+        if (h->cfg.barrier_wait_polls <= 0) {
+            L.polls = 0;
+            break;
+        }
+        L.polls = std::max(L.polls, (unsigned)h->cfg.barrier_wait_polls);
+    }
     pl.launches.push_back(L);
 }
 
@@ -714,6 +723,11 @@ fsim_status check_flags(fsim_sim *h)
         fsim_set_error("a particle position fell outside the cell grid (clamped)");
         return FSIM_ENUMERIC;
     }
+    if (flags & FLAG_CELL_OVERFULL) {
+        fsim_set_error("a cell holds more than %d particles of one species (order inside it not kept)",
+                       kStableRankMax);
+        return FSIM_ENUMERIC;
+    }
     return FSIM_OK;
 }
 
@@ -771,7 +785,7 @@ fsim_status sort_virtual(fsim_sim *h, const float *vpos_host, float4 *vpos_dev =
     add_launch(pl, ab, L_GATHER_F,
                std::vector<Item<GatherFluidArgs>>{{h->P, GatherFluidArgs{tmp, key, h->v_start, n, tmp_pos, tmp_pos,
                                                                          orig0, h->v_posr, h->v_velp, h->v_orig,
-                                                                         h->v_cell}}},
+                                                                         h->v_cell, h->d_flags}}},
                {blocks_for(n, kBlock)});
     pl.host = ab.bytes;
     CK(cudaMalloc((void **)&pl.arena, ab.bytes.size()));

@@ -38,7 +38,11 @@ struct DevParams {
 };
 
 // per-instance error flags (device word, read by check_flags)
-enum : unsigned { FLAG_OUT_OF_GRID = 1u, FLAG_BARRIER_TIMEOUT = 2u };
+enum : unsigned { FLAG_OUT_OF_GRID = 1u, FLAG_BARRIER_TIMEOUT = 2u, FLAG_CELL_OVERFULL = 4u };
+// A cell's particles are ordered by their previous sorted position with a scan
+// over the cell; cells above this count keep the scatter's order instead (the
+// scan's cost grows with the square of the count) and raise FLAG_CELL_OVERFULL.
+constexpr int kStableRankMax = 1024;
 
 constexpr int kBlock = 256;         // threads per block of the element-wise and solid kernels
 constexpr int kScanThreads = 1024;  // cell-count scan: threads per block
@@ -91,6 +95,7 @@ struct GatherFluidArgs {
     const int *orig_in;
     float4 *posr_out, *velp_out;
     int *orig_out, *cell_out;
+    unsigned *flags;
 };
 
 struct GatherSolidArgs {
@@ -102,6 +107,7 @@ struct GatherSolidArgs {
     int *type_out, *orig_out, *cell_out;
     int *inv_out;       // sorted position of every input id
     unsigned *cxyz_out; // cell coordinates packed x | y << 11 | z << 21
+    unsigned *flags;
 };
 
 // fused fluid sweep + update (plain and mixed)
@@ -342,6 +348,7 @@ struct Launch {
     int shape_blocks[kSweepShapes];
     size_t table2_off, barrier_off;       // L_SOLID_FUSED: thread-per-particle table, grid barrier
     int max_sub;
+    unsigned polls;                       // L_SOLID_FUSED: barrier wait limit, 0 = the default
 };
 
 struct Plan {

@@ -95,6 +95,12 @@ typedef struct fsim_config {
                                        of its 27 cells (else sub-steps after
                                        the first walk a per-lane list recorded
                                        by the first; same results bit for bit) */
+    int   barrier_wait_polls;       /* grid barrier of the solid_fused kernel:
+                                       give up (FSIM_ETIMEOUT) after this many
+                                       polls of about 64 ns; 0 = the default
+                                       2^22 (a quarter of a second and more).
+                                       Small values exist to exercise the
+                                       timeout path.                         */
 } fsim_config;
 
 /* Derived constants, as Parameter::initiateParameter computes them in FP32
@@ -363,12 +369,18 @@ fsim_status fsim_host_free(void *p);
  * Scratch is one fixed device array inside the library (4 MiB, held by every
  * GPU that loads the library until the process exits): at most
  * FSIM_NOALLOC_MAX_PARTICLES positions and FSIM_NOALLOC_MAX_CELLS cells, else
- * FSIM_EINVAL.  Positions outside the grid are clamped into its boundary cells.
- * The first call on a device looks up the array's device address (make it
- * before any stream capture).  All calls share the array: calls that overlap
- * on the GPU race, so order them. */
+ * FSIM_EINVAL.  Positions outside the grid are clamped into its boundary cells
+ * (NaN coordinates into the first cell of their axis).  Inside a cell of more
+ * than FSIM_NOALLOC_RANK_MAX particles (only such clamped positions, or a
+ * smoothing length of several particle spacings, produce one) the order is
+ * unspecified: ordering by input index costs the cell's count per particle,
+ * and the sort keeps its work bounded instead.  Every call looks up the
+ * array's device address on the current device; the first call on a device
+ * loads it there, so make that call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race, so order them. */
 #define FSIM_NOALLOC_MAX_PARTICLES 262144
 #define FSIM_NOALLOC_MAX_CELLS 262144
+#define FSIM_NOALLOC_RANK_MAX 1024
 fsim_status fsim_cell_sort_noalloc(const fsim_derived *grid, const float *d_pos, int n,
                                    int *d_cell_start, int *d_ids, void *stream);
 

@@ -32,6 +32,20 @@ def nerr(a, b, floor=1e-12):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), floor))
 
 
+# The accuracy target after 200 steps: normalised max error against FP64
+# within 1e-3; where the FP32 restatement of the reference's own formulas
+# (the FP32 oracle) itself exceeds 1e-3 on a trajectory (FP32 conditioning of
+# the formulation, e.g. pressure near walls in a developing dam break), within
+# TARGET_FP32_FACTOR times its error instead.
+TARGET_200_STEPS = 1e-3
+TARGET_FP32_FACTOR = 1.5
+
+
+def target_200_steps(e_fp32):
+    """Allowed normalised max error after 200 steps, given the FP32 oracle's."""
+    return max(TARGET_200_STEPS, TARGET_FP32_FACTOR * e_fp32)
+
+
 def nrms(a, b, floor=1e-12):
     import numpy as np
 

@@ -201,3 +201,35 @@ def test_add_and_remove_members_of_a_live_batch():
         for f, want in ref[k].items():
             assert np.array_equal(got[f], want), (k, f)
         s.close()
+
+
+def test_fused_barrier_wait_runs_out_then_recovers():
+    """The fused solid kernel's grid barrier gives up after a bounded wait.
+    With the wait limited to one poll (gb300_barrier_wait_polls = 1) a CTA
+    that is not the last to arrive gives up at once: the kernel returns, the
+    instance's flag reports FSIM_ETIMEOUT, and the context stays usable — a
+    handle with the default limit then steps normally and equals the
+    per-phase launches up to FP32 rounding."""
+    cfg, pa = cases.make(cases.small_dam_break())
+    short = api.Config.from_buffer_copy(cfg)
+    short.solid_fused = 1
+    short.barrier_wait_polls = 1
+    seen = None
+    with api.Simulation(short, pa, device=0) as s:
+        for _ in range(10):  # a CTA arriving within ~100 ns of the last one does not time out
+            s.step(1)
+            try:
+                s.sync()
+            except api.FsimError as e:
+                seen = e
+                break
+    assert seen is not None and seen.status == api.ETIMEOUT, seen
+    fused = api.Config.from_buffer_copy(cfg)
+    fused.solid_fused = 1
+    with api.Simulation(fused, pa, device=0) as a, api.Simulation(cfg, pa, device=0) as b:
+        a.step(3)
+        b.step(3)
+        a.sync()
+        b.sync()
+        for f in ("solid_pos", "solid_vel", "fluid_pos"):
+            assert np.allclose(a.get(f), b.get(f), rtol=1e-5, atol=1e-7), f

@@ -1,14 +1,14 @@
 """The CUDA path at the full size of the 4M FSI case (4,194,304 fluid +
 27,000 solid + 912,600 wall particles, +-0.01 dx jitter), through checks that
 do not grow with the size: bit-exact cell ids, cell membership and neighbour
-counts against the oracle, one step against the FP64 oracle, repeatability
-and exact mass conservation."""
+counts against the oracle, one and 20 steps against the FP64 oracle,
+repeatability and exact mass conservation."""
 import os
 
 import numpy as np
 import pytest
 
-from conftest import nerr
+from conftest import TARGET_FP32_FACTOR, nerr
 from fluidsim_gb300 import api, cases
 from oracle import oracle as orc
 
@@ -43,25 +43,27 @@ def test_full_size_cells_membership_and_counts_bitexact(big):
     ref.close()
 
 
-def test_full_size_one_step_vs_fp64(big):
-    """One full step: fluid fields to 1e-4 (normalised max error); solid
-    velocity and stress within 2x the FP32 restatement's own error."""
+def test_full_size_1_and_20_steps_vs_fp64(big):
+    """After one full step fluid fields are within 1e-4 (normalised max
+    error); after 20 steps within 1e-3 (or 1.5x the FP32 oracle's error where
+    that is larger).  Every field stays within 2x (one
+    step) or 3x (20 steps) the FP32 restatement's own error plus 5e-5."""
     cfg, pa = big
     sim = api.Simulation(cfg, pa, device=0)
     r64 = orc.OracleSim(cfg, pa, "f64", threads=THREADS)
     r32 = orc.OracleSim(cfg, pa, "f32", threads=THREADS)
-    sim.step(1)
-    r64.step(1)
-    r32.step(1)
-    sim.sync()
-    for f in ("fluid_pos", "fluid_vel", "fluid_rho", "fluid_p", "solid_pos", "solid_vel", "virt_p"):
-        want = r64.get(f)
-        e_gpu, e_32 = nerr(sim.get(f), want), nerr(r32.get(f), want)
-        print("%-10s gpu %.3g  fp32-oracle %.3g" % (f, e_gpu, e_32))
-        if f.startswith("fluid") or f in ("solid_pos", "virt_p"):
-            assert e_gpu < 1e-4, (f, e_gpu)
-        else:
-            assert e_gpu <= 2.0 * e_32 + 1e-4, (f, e_gpu, e_32)
+    for n, tol, factor in ((1, 1e-4, 2.0), (19, 1e-3, 3.0)):
+        sim.step(n)
+        r64.step(n)
+        r32.step(n)
+        sim.sync()
+        for f in ("fluid_pos", "fluid_vel", "fluid_rho", "fluid_p", "solid_pos", "solid_vel", "virt_p"):
+            want = r64.get(f)
+            e_gpu, e_32 = nerr(sim.get(f), want), nerr(r32.get(f), want)
+            print("after %2d more steps %-10s gpu %.3g  fp32-oracle %.3g" % (n, f, e_gpu, e_32))
+            if f.startswith("fluid") or f in ("solid_pos", "virt_p"):
+                assert e_gpu < max(tol, TARGET_FP32_FACTOR * e_32), (f, e_gpu, e_32)
+            assert e_gpu <= factor * e_32 + 5e-5, (f, e_gpu, e_32)
     sim.close()
 
 

@@ -9,14 +9,14 @@ FP32 form (normalised max error |gpu - fp64|_inf / |fp64|_inf)."""
 import numpy as np
 import pytest
 
-from conftest import nerr
+from conftest import nerr, target_200_steps
 from fluidsim_gb300 import api, cases
 from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
-TOL_200_STEPS = 1e-3   # fluid fields and solid positions after 200 steps
-TRAJ_FP32_FACTOR = 3.0  # solid velocity/stress: FP32-conditioned, bounded by the FP32 oracle's error
+TRAJ_FP32_FACTOR = 3.0  # every field: within 3x the FP32 oracle's error plus TOL_FLOOR
+TOL_FLOOR = 5e-5
 
 
 def test_mixed_field_round_trip():
@@ -60,9 +60,9 @@ def test_mixed_1_and_200_steps_vs_fp64():
             e_m, e_p, e_32 = nerr(mixed.get(f), want), nerr(plain.get(f), want), nerr(r32.get(f), want)
             print("after %3d more steps %-10s mixed %.3g  plain %.3g  fp32-oracle %.3g" % (n, f, e_m, e_p, e_32))
             if f.startswith("fluid") or f == "solid_pos":
-                assert e_m < TOL_200_STEPS, (f, e_m)
+                assert e_m < target_200_steps(e_32), (f, e_m, e_32)
             else:
-                assert e_m <= TRAJ_FP32_FACTOR * e_32 + TOL_200_STEPS, (f, e_m, e_32)
+                assert e_m <= TRAJ_FP32_FACTOR * e_32 + TOL_FLOOR, (f, e_m, e_32)
     mixed.close()
     plain.close()
 
