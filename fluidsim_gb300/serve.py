@@ -154,6 +154,10 @@ class Server:
         prepared = {}
         st = {"nxt": 0, "used": 0, "load": 0, "completed": 0, "failed": 0, "work": 0, "rebuilds": 0, "joins": 0,
               "leaves": 0}
+        # host time per activity: stepping (enqueue + the wait for the quantum),
+        # admission (instance creation), retirement (read-back + free),
+        # batch membership changes, idle (nothing to run)
+        tm = {"step": 0.0, "admit": 0.0, "retire": 0.0, "membership": 0.0, "idle": 0.0}
         batch, batch_members = None, []
         t0 = clock()
 
@@ -164,12 +168,14 @@ class Server:
             self.log.append((event, r.rid, now))
 
         def retire(a, now, error=""):
+            t_r = clock()
             if self.keep_results and not error:
                 a[0].result = be.result(a[1])
             be.destroy(a[1])
             st["used"] -= a[3]
             st["load"] -= a[0].particles
             close_request(a[0], now, "failed" if error else "done", error)
+            tm["retire"] += clock() - t_r
 
         while st["completed"] < len(reqs):
             now = clock() - t0
@@ -201,11 +207,14 @@ class Server:
                 waiting.pop(0)
                 del prepared[r.rid]
                 r.particles = npart
+                t_a = clock()
                 try:
                     inst = be.create(data)
                 except Exception as exc:  # this request fails; the others go on
                     close_request(r, clock() - t0, "failed", "admission failed: %s" % exc)
                     continue
+                finally:
+                    tm["admit"] += clock() - t_a
                 active.append([r, inst, r.steps, need])
                 st["used"] += need
                 st["load"] += npart
@@ -216,8 +225,11 @@ class Server:
                     batch.close()
                     batch = None
                 if st["nxt"] < len(reqs):
+                    t_i = clock()
                     sleep(max(0.0, min(0.05, reqs[st["nxt"]].arrival - (clock() - t0))))
+                    tm["idle"] += clock() - t_i
                 continue
+            t_m = clock()
             if batch is not None and changed and hasattr(be, "add"):
                 # keep the live batch: admit the new members into it
                 current = list(batch_members)
@@ -233,9 +245,12 @@ class Server:
                 batch = be.batch([a[1] for a in active])
                 batch_members = [a[1] for a in active]
                 st["rebuilds"] += 1
+            tm["membership"] += clock() - t_m
             k = min(self.quantum, min(a[2] for a in active))
+            t_s = clock()
             batch.step(k)
             status = be.member_status(batch)
+            tm["step"] += clock() - t_s
             now = clock() - t0
             finished, broken = [], []
             for a, code in zip(active, status):
@@ -248,6 +263,7 @@ class Server:
                     finished.append(a)
             if finished or broken:
                 leaving = finished + [a for a, _ in broken]
+                t_m = clock()
                 if hasattr(be, "remove") and len(leaving) < len(active):
                     for a in leaving:
                         be.remove(batch, a[1])
@@ -256,6 +272,7 @@ class Server:
                 else:
                     batch.close()
                     batch = None
+                tm["membership"] += clock() - t_m
                 for a in finished:
                     retire(a, now)
                 for a, code in broken:
@@ -269,7 +286,8 @@ class Server:
         return {"requests": len(reqs), "makespan_s": makespan, "particle_updates": st["work"],
                 "throughput": st["work"] / makespan, "p50_latency_s": _percentile(lat, 50),
                 "p99_latency_s": _percentile(lat, 99), "batch_rebuilds": st["rebuilds"],
-                "batch_joins": st["joins"], "batch_leaves": st["leaves"], "failed": st["failed"]}
+                "batch_joins": st["joins"], "batch_leaves": st["leaves"], "failed": st["failed"],
+                "host_time_s": {k: round(v, 3) for k, v in tm.items()}}
 
 
 def serve_one_by_one(requests, device=0, clock=time.perf_counter, keep_results=False):
