@@ -545,7 +545,26 @@ def run_ensemble(dev, steps):
         fused_launches = b.launches_per_step()
     for sm in sims:
         sm.close()
+    # the reference build, one instance after another (how the reference runs an ensemble)
+    ref_ms, ref_err = 0.0, None
+    try:
+        from oracle import refbuild
+
+        if refbuild.available("release"):
+            for cfg, pa in members:
+                cfg.solid_fused = 0
+                with refbuild.RefBuildSim(cfg, pa, "release", device=dev) as r:
+                    r.step(3)
+                    ref_ms += r.time_steps(steps)
+        else:
+            ref_err = "reference device image absent"
+    except Exception as e:
+        ref_err = str(e)
+    ref_rate = total * steps / (ref_ms * 1e-3) if ref_ms > 0 and not ref_err else None
     return {
+        "reference_build_one_by_one": ref_rate,
+        "ratio_batched_vs_reference_build": (total * steps / (batched_ms * 1e-3)) / ref_rate if ref_rate else None,
+        "reference_build_error": ref_err,
         "workload": "ensemble of 64 dam-break instances (seed 2024), %d fluid+solid particles in total, "
                     "dx=0.01, dt=1e-4, 4-5 solid sub-steps" % total,
         "steps": steps,
