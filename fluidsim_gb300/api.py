@@ -52,6 +52,7 @@ class Config(C.Structure):
         ("solid_fused", C.c_int),
         ("solid_full_walk", C.c_int),
         ("barrier_wait_polls", C.c_int),
+        ("neighbor_skin", C.c_float),
     ]
 
     def as_dict(self):
@@ -140,6 +141,9 @@ def load():
         "fsim_get_field": (C.c_int, [P, C.c_int, P, C.c_size_t]),
         "fsim_set_field": (C.c_int, [P, C.c_int, P, C.c_size_t]),
         "fsim_neighbor_counts": (C.c_int, [P, P, C.c_size_t]),
+        "fsim_list_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int)]),
+        "fsim_list_counts": (C.c_int, [P, P, C.c_size_t]),
         "fsim_get_cells": (C.c_int, [P, C.c_int, P, C.c_size_t, P, C.c_size_t]),
         "fsim_write_vtk": (C.c_int, [P, C.c_char_p, C.c_int]),
         "fsim_time_steps": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
@@ -198,7 +202,7 @@ EXPORTED = [
     "fsim_snapshot_save", "fsim_snapshot_load", "fsim_snapshot_write", "fsim_snapshot_read", "fsim_probe",
     "fsim_write_vtk_binary", "fsim_batch_sync_members", "fsim_create_case", "fsim_case_counts",
     "fsim_get_fields", "fsim_set_fields", "fsim_batch_add", "fsim_batch_remove",
-    "fsim_time_phases",
+    "fsim_time_phases", "fsim_list_stats", "fsim_list_counts",
 ]
 SWEEP_SHAPES = ((4, 48), (4, 32), (8, 32))  # (warps per block, list capacity) per shape index
 
@@ -492,6 +496,18 @@ class Simulation:
         out = np.empty((self.n["fluid"], 3), np.int32)
         check(self.lib.fsim_neighbor_counts(self.h, out.ctypes.data, out.nbytes))
         return out
+
+    def list_counts(self):
+        """Neighbour-list entries within the impact distance per fluid particle."""
+        out = np.empty((self.n["fluid"], 3), np.int32)
+        check(self.lib.fsim_list_counts(self.h, out.ctypes.data, out.nbytes))
+        return out
+
+    def list_stats(self):
+        """{"enabled", "builds", "capacity", "check"} of the fluid neighbour lists."""
+        v = [C.c_int() for _ in range(4)]
+        check(self.lib.fsim_list_stats(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("enabled", "builds", "capacity", "check"), (x.value for x in v)))
 
     def cells(self, species):
         d = self.derived()

@@ -22,7 +22,10 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_UNITS = ["fsim_kernels.cu", "fsim_sim.cu", "fsim_noalloc.cu", "fsim_probe.cu"]
 HOST_UNITS = ["fsim_host.cpp"]
-HEADERS = ["fsim_internal.h"]
+HEADERS = ["fsim_internal.h", "fsim_types.h"]
+# FSIM_DEVICE_CHECKS=1 in the environment compiles the kernels' index checks
+# in (a debugging build; see FSIM_DCHECK in fsim_kernels.cu)
+DEBUG_FLAGS = ["-DFSIM_DEVICE_CHECKS"] if os.environ.get("FSIM_DEVICE_CHECKS") == "1" else []
 
 
 def _deps():
@@ -61,8 +64,8 @@ def build(force=False, verbose=False):
         objs.append(obj)
         if force or _stale(obj, [src] + deps):
             cmds.append([NVCC] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-                                         "-Xptxas", "-v" if verbose else "-O3",
-                                         "-I", INCLUDE, "-c", src, "-o", obj])
+                                         "-Xptxas", "-v" if verbose else "-O3"] + DEBUG_FLAGS +
+                        ["-I", INCLUDE, "-c", src, "-o", obj])
     for u in HOST_UNITS:
         src = os.path.join(CSRC, u)
         obj = os.path.join(BUILD, u + ".o")

@@ -202,6 +202,11 @@ fsim_status config_from_values(const IniValues &ini, fsim_config *c)
     c->solid_full_walk = ini.get_bool("gb300_solid_full_walk", false) ? 1 : 0;
     c->barrier_wait_polls = ini.get("gb300_barrier_wait_polls", 0);
     if (c->barrier_wait_polls < 0) c->barrier_wait_polls = 0;
+    c->neighbor_skin = ini.get("gb300_neighbor_skin", c->neighbor_skin);
+    if (!(c->neighbor_skin >= 0.0f && c->neighbor_skin <= 1.0f)) {
+        fsim_set_error("gb300_neighbor_skin must lie in [0, 1]");
+        return FSIM_EINVAL;
+    }
 
     // validity checks of the readers (src/kernel.cpp:16-20, src/domain.cpp:19-23,
     // src/sim_time.cpp:17-21); the reference throws, we return EINVAL
@@ -240,6 +245,7 @@ extern "C" fsim_status fsim_config_defaults(fsim_config *c)
     c->impact_length_hsml_ratio = 3.0f;
     c->thread_num = 32;
     c->precision = FSIM_PRECISION_FP32;
+    c->neighbor_skin = 0.1f;
     return FSIM_OK;
 }
 

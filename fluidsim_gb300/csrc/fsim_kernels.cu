@@ -40,6 +40,20 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu; // all lanes of a warp
 
+// Device-side index checks, compiled in only with -DFSIM_DEVICE_CHECKS (a
+// debugging build): a failed check records its site bit in g_check_sites and
+// skips the access instead of reading or writing out of bounds.
+#ifdef FSIM_DEVICE_CHECKS
+__device__ unsigned g_check_sites;
+#define FSIM_DCHECK(cond, bit, skip)                                                                          \
+    if (!(cond)) {                                                                                            \
+        atomicOr(&g_check_sites, (bit));                                                                      \
+        skip;                                                                                                 \
+    }
+#else
+#define FSIM_DCHECK(cond, bit, skip)
+#endif
+
 // ------------------------------------------------------------- cell math
 // findPositionCell (src/pair.cu:8-24): per-axis truncation of the FP32
 // (p - min) * inv.  Out-of-grid indices (impossible for clamped positions)
@@ -158,6 +172,7 @@ __device__ __forceinline__ int cell_slot(int *cnt, int c, bool active)
 
 __device__ __forceinline__ void hash_body(const DevParams &P, const HashArgs &A, int blk)
 {
+    if (A.gate && !*A.gate) return; // uniform per block
     const int s = blk * blockDim.x + threadIdx.x;
     const bool active = s < A.n;
     int c = 0;
@@ -173,6 +188,7 @@ FSIM_BATCHED_KERNEL(kb_hash, HashArgs, hash_body, kBlock)
 
 __device__ __forceinline__ void zero_body(const DevParams &, const ZeroArgs &A, int blk)
 {
+    if (A.gate && !*A.gate) return;
     const int s = blk * blockDim.x + threadIdx.x;
     if (s < A.n) A.p[s] = 0;
 }
@@ -214,6 +230,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *total)
 // scan pass 1: per-tile sums (one block per 4096-entry tile)
 __device__ __forceinline__ void scan_reduce_body(const DevParams &, const ScanArgs &J, int blk)
 {
+    if (J.gate && !*J.gate) return; // uniform per block
     const int base = blk * kScanTile + threadIdx.x * kScanItems;
     int s = 0;
 #pragma unroll
@@ -228,6 +245,7 @@ FSIM_BATCHED_KERNEL(kb_scan_reduce, ScanArgs, scan_reduce_body, kScanThreads)
 // scan pass 2: exclusive scan of the tile sums (one block per array)
 __device__ __forceinline__ void scan_partials_body(const DevParams &, const ScanArgs &J, int)
 {
+    if (J.gate && !*J.gate) return;
     const int tiles = blocks_for(J.n, kScanTile);
     int carry = 0;
     for (int b0 = 0; b0 < tiles; b0 += kScanThreads) {
@@ -245,6 +263,7 @@ FSIM_BATCHED_KERNEL(kb_scan_partials, ScanArgs, scan_partials_body, kScanThreads
 // scan pass 3: scan inside each tile plus its offset
 __device__ __forceinline__ void scan_apply_body(const DevParams &, const ScanArgs &J, int blk)
 {
+    if (J.gate && !*J.gate) return;
     const int base = blk * kScanTile + threadIdx.x * kScanItems;
     int v[kScanItems];
     int s = 0;
@@ -265,8 +284,10 @@ FSIM_BATCHED_KERNEL(kb_scan_apply, ScanArgs, scan_apply_body, kScanThreads)
 
 __device__ __forceinline__ void scatter_body(const DevParams &, const ScatterArgs &A, int blk)
 {
+    if (A.gate && !*A.gate) return;
     const int s = blk * blockDim.x + threadIdx.x;
     if (s >= A.n) return;
+    FSIM_DCHECK(A.start[A.key[s]] + A.slot[s] >= 0 && A.start[A.key[s]] + A.slot[s] < A.n, 8192u, return);
     A.tmp[A.start[A.key[s]] + A.slot[s]] = s;
 }
 FSIM_BATCHED_KERNEL(kb_scatter, ScatterArgs, scatter_body, kBlock)
@@ -280,9 +301,15 @@ FSIM_BATCHED_KERNEL(kb_scatter, ScatterArgs, scatter_body, kBlock)
 // step reports the failure.
 __device__ __forceinline__ int stable_dst(const int *__restrict__ tmp, const int *__restrict__ key,
                                           const int *__restrict__ start, int d, int &src, int &cell,
-                                          unsigned *flags)
+                                          unsigned *flags, int n)
 {
     src = tmp[d];
+    FSIM_DCHECK(src >= 0 && src < n, 4096u, {
+        src = d;
+        cell = key[d];
+        return d;
+    });
+    (void)n;
     cell = key[src];
     const int b = start[cell], e = start[cell + 1];
     if (e - b > kStableRankMax) {
@@ -298,12 +325,23 @@ __device__ __forceinline__ void gather_fluid_body(const DevParams &, const Gathe
 {
     const int d = blk * blockDim.x + threadIdx.x;
     if (d >= A.n) return;
+    if (A.gate && !*A.gate) {
+        // neighbour-list step without a rebuild: the order stays, the state
+        // moves to the other buffer unpermuted
+        A.posr_out[d] = A.posr_in[d];
+        A.velp_out[d] = A.velp_in[d];
+        A.orig_out[d] = A.orig_in[d];
+        return;
+    }
     int src, cell;
-    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell, A.flags);
-    A.posr_out[dst] = A.posr_in[src];
+    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell, A.flags, A.n);
+    FSIM_DCHECK(dst >= 0 && dst < A.n && src >= 0 && src < A.n, 8u, return);
+    const float4 p = A.posr_in[src];
+    A.posr_out[dst] = p;
     A.velp_out[dst] = A.velp_in[src];
     A.orig_out[dst] = A.orig_in[src];
     A.cell_out[dst] = cell;
+    if (A.x0_out) A.x0_out[dst] = p;
 }
 FSIM_BATCHED_KERNEL(kb_gather_fluid, GatherFluidArgs, gather_fluid_body, kBlock)
 
@@ -325,9 +363,19 @@ __device__ __forceinline__ void gather_solid_body(const DevParams &P, const Gath
 {
     const int d = blk * blockDim.x + threadIdx.x;
     if (d >= A.n) return;
+    if (A.gate && !*A.gate) { // no rebuild: unpermuted copy (inv stays valid)
+        A.pos_out[d] = A.pos_in[d];
+        A.vel_out[d] = A.vel_in[d];
+        A.ref_out[d] = A.ref_in[d];
+        A.type_out[d] = A.type_in[d];
+        A.orig_out[d] = A.orig_in[d];
+        return;
+    }
     int src, cell;
-    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell, A.flags);
-    A.pos_out[dst] = A.pos_in[src];
+    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell, A.flags, A.n);
+    FSIM_DCHECK(dst >= 0 && dst < A.n && src >= 0 && src < A.n, 16u, return);
+    const float4 p = A.pos_in[src];
+    A.pos_out[dst] = p;
     A.vel_out[dst] = A.vel_in[src];
     A.ref_out[dst] = A.ref_in[src];
     A.type_out[dst] = A.type_in[src];
@@ -335,9 +383,26 @@ __device__ __forceinline__ void gather_solid_body(const DevParams &P, const Gath
     A.orig_out[dst] = o;
     A.cell_out[dst] = cell;
     A.inv_out[o] = dst;
-    A.cxyz_out[dst] = pack_cell(P, cell);
+    if (A.cxyz_out) A.cxyz_out[dst] = pack_cell(P, cell);
+    if (A.x0_out) A.x0_out[dst] = p;
 }
 FSIM_BATCHED_KERNEL(kb_gather_solid, GatherSolidArgs, gather_solid_body, kBlock)
+
+// Neighbour-list instances: the per-step cell index.  Slot d of the scatter
+// holds particle slot src = tmp[d] of cell `cell`; its rank among the cell's
+// slots (in increasing slot order, as stable_dst ranks) places it in ids.
+__device__ __forceinline__ void rank_body(const DevParams &P, const RankArgs &A, int blk)
+{
+    const int d = blk * blockDim.x + threadIdx.x;
+    if (d >= A.n) return;
+    int src, cell;
+    const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell, A.flags, A.n);
+    FSIM_DCHECK(dst >= 0 && dst < A.n && src >= 0 && src < A.n, 4u, return);
+    A.ids[dst] = src;
+    A.cell_out[src] = cell;
+    if (A.cxyz_out) A.cxyz_out[src] = pack_cell(P, cell);
+}
+FSIM_BATCHED_KERNEL(kb_rank, RankArgs, rank_body, kBlock)
 
 // ------------------------------------------------------------ EOS
 // densityToPressure (src/fluid.cu:16-24): Tait EOS, floored at min_pressure.
@@ -446,8 +511,8 @@ __device__ __forceinline__ void riemann_pair(const DevParams &P, float dx, float
 // fluidUpdate (src/fluid.cu:234-269) applied to the sums of one particle: NaN
 // scrub, Euler step with the old velocity, density clamp, EOS, position clamp,
 // speed cap; writes the integrated state into the other buffer.
-__device__ __forceinline__ void fluid_update_store(const DevParams &P, const FluidSweepArgs &A, int i, float4 pr,
-                                                   float4 vp, const PairAcc &acc)
+__device__ __forceinline__ float4 fluid_update_store(const DevParams &P, const FluidSweepArgs &A, int i, float4 pr,
+                                                     float4 vp, const PairAcc &acc)
 {
     const float rho_inv = __fdividef(1.0f, pr.w);
     float drho = 2.0f * pr.w * acc.drho;
@@ -469,13 +534,15 @@ __device__ __forceinline__ void fluid_update_store(const DevParams &P, const Flu
         uy *= s;
         uz *= s;
     }
-    A.posr_out[i] = make_float4(x, y, z, rho);
+    const float4 xr = make_float4(x, y, z, rho);
+    A.posr_out[i] = xr;
     A.velp_out[i] = make_float4(ux, uy, uz, p);
     A.orig_out[i] = A.orig_in[i];
     if (A.keep) {
         A.drho_out[i] = drho;
         A.dudt_out[i] = make_float4(ax, ay, az, 0.0f);
     }
+    return xr;
 }
 
 // findFluidPair + fluidUpdate (src/fluid.cu:169-269), fused: the sweep reads
@@ -677,6 +744,226 @@ __global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep_p(const __grid_
     fluid_sweep_body<CHECK_Z, VISCID, SH, true>(it.P, it.A, (int)blockIdx.x - B.bstart[inst]);
 }
 
+// ------------------------------------------------------- fluid neighbour lists
+// Neighbour-list instances advance the fluid with per-particle lists that
+// are kept for many steps (a Verlet list): the list of particle i holds every
+// fluid, wall and solid particle within the list radius Rs = R + skin of i
+// when the list was built.  While no particle has moved more than (Rs - R) / 2
+// since the build, every pair within the impact distance R is in the lists,
+// so the sweep finds exactly the reference's pair set (src/fluid.cu:169-232:
+// 27 cells of side >= R, then r^2 < R^2) with no cell walk.  The particles
+// keep the order of the last build between builds; the other phases walk a
+// per-step cell index (kb_rank) instead.
+
+// One block per instance at the start of every step: rebuild when forced or
+// when the largest displacement since the last build (fluid: accumulated by
+// the last sweep; solid: measured here) exceeds the allowance.
+__device__ __forceinline__ void nl_decide_body(const DevParams &, const NlDecideArgs &A, int)
+{
+    __shared__ unsigned wmax[kBlock / 32];
+    unsigned m = 0;
+    for (int i = threadIdx.x; i < A.ns; i += blockDim.x) {
+        const float4 p = A.s_pos[i], o = A.s_x0[i];
+        m = max(m, __float_as_uint(dist2(p.x - o.x, p.y - o.y, p.z - o.z)));
+    }
+    m = __reduce_max_sync(kFull, m);
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x) return;
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, wmax[w]);
+    NlState &S = *A.nl;
+    const float d2 = __uint_as_float(max(m, S.maxd2)); // NaN bits compare above every distance
+    const int rb = S.force || !(d2 <= A.move2);
+    S.rebuild = rb;
+    S.force = 0;
+    S.maxd2 = 0u; // this step's sweep accumulates afresh (against the new x0 if rebuilt)
+    if (rb) {
+        S.builds += 1;
+        S.overflow = 0;
+    }
+}
+FSIM_BATCHED_KERNEL(kb_nl_decide, NlDecideArgs, nl_decide_body, kBlock)
+
+// The list build: the sweep's warp-uniform candidate stream (a warp's lanes of
+// one cell row walk the union of their 9 neighbour rows) over the list grid,
+// testing r^2 < Rs^2; hits collect in a per-lane shared-memory list that is
+// appended to the lane's global list in candidate order.  Per particle: its
+// fluid, then wall, then solid candidates, in row order -- the order in which
+// the stream sweep sums them.
+constexpr int kNlBuildWarps = kNlBuildThreads / 32, kNlBuildCap = 32, kNlBuildChunk = 8;
+
+__device__ __forceinline__ void nl_flush(const NlBuildArgs &A, int (*lst)[32], int lane, int i, int &cnt, int &tot)
+{
+    const int m = __reduce_max_sync(kFull, cnt);
+    for (int k = 0; k < m; ++k) {
+        const int e = tot + k;
+        if (k < cnt && e < A.cap) A.list[(size_t)e * A.n + i] = lst[k][lane];
+    }
+    tot += cnt;
+    cnt = 0;
+}
+
+template <int SP>
+__device__ __forceinline__ void nl_gather(const DevParams &P, const NlBuildArgs &A, int (*lst)[32], int lane, int i,
+                                          int &cnt, int &tot, bool in, int cx, int cy, int z0, int z1, float4 pr)
+{
+    const int *start = SP == 0 ? A.start_f : SP == 1 ? A.start_v : A.start_s;
+    const float4 *pos = SP == 0 ? A.posr : SP == 1 ? A.v_posr : A.s_pos;
+    const int tag = (int)((unsigned)SP << kNlSpeciesShift);
+    for (int ox = -1; ox <= 1; ++ox) {
+        const int x = cx + ox;
+        if (x < 0 || x >= P.nx) continue;
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int y = cy + oy;
+            if (y < 0 || y >= P.ny) continue;
+            const int base = (x * P.ny + y) * P.nz;
+            int j = start[base + z0];
+            const int je = start[base + z1];
+            while (j < je) {
+                if (__reduce_max_sync(kFull, cnt) > kNlBuildCap - kNlBuildChunk) nl_flush(A, lst, lane, i, cnt, tot);
+                const int jend = min(j + kNlBuildChunk, je);
+#pragma unroll 4
+                for (; j < jend; ++j) {
+                    FSIM_DCHECK(j < (SP == 0 ? A.n : SP == 1 ? A.nv : A.ns), 2u, continue);
+                    const float4 q = pos[j]; // same address in every lane: a broadcast
+                    const float r2 = dist2(q.x - pr.x, q.y - pr.y, q.z - pr.z);
+                    if (in && r2 < A.R2s) lst[cnt++][lane] = j | tag;
+                }
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void nl_build_body(const DevParams &P, const NlBuildArgs &A, int blk)
+{
+    if (!A.nl->rebuild) return; // uniform per block
+    __shared__ int lists[kNlBuildWarps][kNlBuildCap][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = (blk * kNlBuildWarps + warp) * 32 + lane;
+    const bool valid = i < A.n;
+    int(*lst)[32] = lists[warp];
+    const float4 pr = valid ? A.posr[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const int cell = valid ? A.cell_f[i] : 0;
+    const int row = cell / P.nz, cz = cell - row * P.nz;
+    int cnt = 0, tot = 0;
+    unsigned remaining = __ballot_sync(kFull, valid);
+    while (remaining) {
+        const int leader = __ffs(remaining) - 1;
+        const int grow = __shfl_sync(kFull, row, leader);
+        const unsigned grp = __ballot_sync(kFull, valid && row == grow);
+        remaining &= ~grp;
+        const bool in = (grp >> lane) & 1u;
+        const int zlo = __reduce_min_sync(kFull, in ? cz : INT_MAX);
+        const int zhi = __reduce_max_sync(kFull, in ? cz : INT_MIN);
+        const int z0 = max(zlo - 1, 0), z1 = min(zhi + 1, P.nz - 1) + 1;
+        const int cx = grow / P.ny, cy = grow - cx * P.ny;
+        nl_gather<0>(P, A, lst, lane, i, cnt, tot, in, cx, cy, z0, z1, pr);
+        nl_gather<1>(P, A, lst, lane, i, cnt, tot, in, cx, cy, z0, z1, pr);
+        nl_gather<2>(P, A, lst, lane, i, cnt, tot, in, cx, cy, z0, z1, pr);
+    }
+    nl_flush(A, lst, lane, i, cnt, tot);
+    if (valid) {
+        A.cnt[i] = tot;
+        if (tot > A.cap) {
+            atomicAdd(&A.nl->overflow, 1);
+            atomicOr(A.flags, FLAG_LIST_OVERFLOW);
+        }
+    }
+}
+FSIM_BATCHED_KERNEL(kb_nl_build, NlBuildArgs, nl_build_body, kNlBuildWarps * 32)
+
+// The list sweep: one thread per particle walks its list, tests r^2 < R^2
+// and sums the Riemann pair terms in list order (fluid, then wall, then solid
+// candidates, as the stream sweep sums them), then fluidUpdate
+// (src/fluid.cu:234-269) as in the stream sweep; the particle's squared
+// displacement since the build goes into the instance's running maximum.
+template <int VISCID, bool CHECK>
+__device__ __forceinline__ void fluid_sweep_nl_pairs(const DevParams &P, const FluidSweepArgs &A, int i, float4 pr,
+                                                     float4 vp, PairAcc &acc)
+{
+    const int m = min(A.nl_cnt[i], A.nl_cap);
+    const int *__restrict__ l = A.nl_list + i;
+    const size_t stride = (size_t)A.n;
+    const unsigned ci = CHECK ? A.nl_cxyz_f[i] : 0u;
+    for (int k = 0; k < m; ++k) {
+        const unsigned e = (unsigned)__ldg(l + (size_t)k * stride);
+        const int sp = (int)(e >> kNlSpeciesShift), j = (int)(e & kNlIndexMask);
+        FSIM_DCHECK(sp == 0 ? j < A.n : sp == 1 ? j < A.nl_nv : sp == 2 && j < A.nl_ns, 1u, continue);
+        if (sp == 2) {
+            const float4 q = A.s_pos[j];
+            const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2 && (!CHECK || cells_adjacent(ci, A.nl_cxyz_s[j]))) {
+                const float4 np = A.s_np[j], sv = A.s_vel[j];
+                const float k2 = 2.0f * ((vp.x - sv.x) * np.x + (vp.y - sv.y) * np.y + (vp.z - sv.z) * np.z);
+                riemann_pair<false, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, vp.x - k2 * np.x,
+                                            vp.y - k2 * np.y, vp.z - k2 * np.z, pr.w, np.w, false, acc);
+            }
+        } else {
+            const float4 q = sp ? A.v_posr[j] : A.posr[j];
+            const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
+            const float r2 = dist2(dx, dy, dz);
+            if (r2 < P.R2 && (!CHECK || cells_adjacent(ci, sp ? A.nl_cxyz_v[j] : A.nl_cxyz_f[j]))) {
+                const float4 u = sp ? A.v_velp[j] : A.velp[j];
+                riemann_pair<true, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q.w,
+                                           u.w, sp == 1, acc);
+            }
+        }
+    }
+}
+
+template <int VISCID>
+__device__ __forceinline__ void fluid_sweep_nl_body(const DevParams &P, const FluidSweepArgs &A, int blk)
+{
+    const int i = blk * blockDim.x + threadIdx.x;
+    const bool valid = i < A.n;
+    unsigned d2bits = 0u;
+    if (valid) {
+        const float4 pr = A.posr[i], vp = A.velp[i];
+        PairAcc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        if (A.nl_cxyz_f) fluid_sweep_nl_pairs<VISCID, true>(P, A, i, pr, vp, acc);
+        else fluid_sweep_nl_pairs<VISCID, false>(P, A, i, pr, vp, acc);
+        const float4 x = fluid_update_store(P, A, i, pr, vp, acc);
+        const float4 o = A.x0[i];
+        d2bits = __float_as_uint(dist2(x.x - o.x, x.y - o.y, x.z - o.z));
+    }
+    const unsigned wmax = __reduce_max_sync(kFull, d2bits);
+    if ((threadIdx.x & 31) == 0 && wmax) atomicMax(&A.nl->maxd2, wmax);
+}
+
+// launch shapes of the list sweep: threads per block, minimum blocks per SM
+template <int BS, int MINB>
+struct NlShape {
+    static constexpr int threads = BS, min_blocks = MINB;
+};
+using NlShape0 = NlShape<128, 1>;
+using NlShape1 = NlShape<128, 12>; // at most 40 registers: 12 blocks (48 warps) per SM
+using NlShape2 = NlShape<256, 1>;
+static_assert(kShapeWarps[0] * 32 == NlShape0::threads && kShapeWarps[1] * 32 == NlShape1::threads &&
+                  kShapeWarps[2] * 32 == NlShape2::threads,
+              "list-sweep shapes follow the block sizes of fsim_types.h");
+
+template <int VISCID, class SH>
+__global__ void __launch_bounds__(SH::threads, SH::min_blocks) kb_fluid_sweep_nl_1(const DevParams P,
+                                                                                   const FluidSweepArgs A)
+{
+    fluid_sweep_nl_body<VISCID>(P, A, (int)blockIdx.x);
+}
+template <int VISCID, class SH>
+__global__ void __launch_bounds__(SH::threads, SH::min_blocks)
+    kb_fluid_sweep_nl(const Item<FluidSweepArgs> *__restrict__ items, const int *__restrict__ bstart, int ninst)
+{
+    const int inst = locate_instance(bstart, ninst, blockIdx.x);
+    fluid_sweep_nl_body<VISCID>(items[inst].P, items[inst].A, (int)blockIdx.x - bstart[inst]);
+}
+template <int VISCID, class SH>
+__global__ void __launch_bounds__(SH::threads, SH::min_blocks) kb_fluid_sweep_nl_p(const __grid_constant__ SweepBatchParams B)
+{
+    const int inst = locate_instance(B.bstart, B.n, blockIdx.x);
+    const Item<FluidSweepArgs> &it = B.it[inst];
+    fluid_sweep_nl_body<VISCID>(it.P, it.A, (int)blockIdx.x - B.bstart[inst]);
+}
+
 // ------------------------------------------------------- virtual particles
 // getVirtData (src/virt.cu:9-75): nearest fluid particle's rho, hydrostatically
 // corrected p and velocity mirrored about the (static) wall normal.  Ties in
@@ -691,7 +978,9 @@ __device__ __forceinline__ void virt_body(const DevParams &P, const VirtArgs &A,
     float best = FSIM_LARGE_FLOAT;
     int best_j = -1, best_orig = INT_MAX;
     for (int r = 0; r < rows.count; ++r) {
-        for (int j = A.start_f[rows.base[r] + rows.z0], je = A.start_f[rows.base[r] + rows.z1]; j < je; ++j) {
+        for (int t = A.start_f[rows.base[r] + rows.z0], te = A.start_f[rows.base[r] + rows.z1]; t < te; ++t) {
+            const int j = A.ids_f ? A.ids_f[t] : t;
+            FSIM_DCHECK(j >= 0 && j < A.nf, 32u, continue);
             const float4 q = A.fposr[j];
             const float d2 = dist2(q.x - xi.x, q.y - xi.y, q.z - xi.z);
             if (d2 < best) {
@@ -799,7 +1088,9 @@ __device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs
         neighbor_rows(P, A.s_cell[i], rows);
         for (int r = 0; r < rows.count; ++r) {
             const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-            for (int j = A.start_f[c0] + g, je = A.start_f[c1]; j < je; j += kSolidGroup) {
+            for (int tf = A.start_f[c0] + g, te = A.start_f[c1]; tf < te; tf += kSolidGroup) {
+                const int j = A.ids_f ? A.ids_f[tf] : tf;
+                FSIM_DCHECK(j >= 0 && j < A.nf, 64u, continue);
                 const float4 q = A.fposr[j];
                 const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
                 const float r2 = dist2(dx, dy, dz);
@@ -809,7 +1100,9 @@ __device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs
                     psum += A.fvelp[j].w * w;
                 }
             }
-            for (int j = A.start_s[c0] + g, je = A.start_s[c1]; j < je; j += kSolidGroup) {
+            for (int ts = A.start_s[c0] + g, te = A.start_s[c1]; ts < te; ts += kSolidGroup) {
+                const int j = A.ids_s ? A.ids_s[ts] : ts;
+                FSIM_DCHECK(j >= 0 && j < A.n, 128u, continue);
                 const float4 q = A.s_pos[j];
                 const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
                 const float r2 = dist2(dx, dy, dz);
@@ -1381,6 +1674,10 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
             int j;
             if (RESOLVE) {
                 const int jj = S.inv[S.nbr_orig[e]];
+                FSIM_DCHECK(jj >= 0 && jj < S.n, 512u, {
+                    S.nbr_slot[e] = -1;
+                    continue;
+                });
                 j = cells_adjacent(ci, S.cxyz[jj]) ? jj : -1;
                 S.nbr_slot[e] = j;
             } else {
@@ -1534,6 +1831,7 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
                 walk = false;
                 for (int e = 0; e < c; ++e) {
                     const int j = S.fl[(size_t)e * T + t];
+                    FSIM_DCHECK(j >= 0 && j < S.nf, 1024u, continue);
                     const float4 q = S.fposr[j];
                     const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
                     const float r2 = dist2(dx, dy, dz);
@@ -1550,7 +1848,9 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
             int nrec = 0;
             for (int r = 0; r < rows.count; ++r) {
                 const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-                for (int j = S.start_f[c0] + g, je = S.start_f[c1]; j < je; j += kSolidGroup) {
+                for (int tf = S.start_f[c0] + g, te = S.start_f[c1]; tf < te; tf += kSolidGroup) {
+                    const int j = S.ids_f ? S.ids_f[tf] : tf;
+                    FSIM_DCHECK(j >= 0 && j < S.nf, 256u, continue);
                     const float4 q = S.fposr[j];
                     const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
                     const float r2 = dist2(dx, dy, dz);
@@ -1581,6 +1881,7 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
         for (int e = S.nbr_off[o] + g, ee = S.nbr_off[o + 1]; e < ee; e += kSolidGroup) {
             const int j = S.nbr_slot[e];
             if (j < 0) continue;
+            FSIM_DCHECK(j < S.n, 2048u, continue);
             const float4 rj = S.ref[j];
             const float dX = __fsub_rn(rj.x, ri.x), dY = __fsub_rn(rj.y, ri.y), dZ = __fsub_rn(rj.z, ri.z);
             const float w = solid_pair_weight(P, dX, dY, dZ);
@@ -1762,12 +2063,14 @@ __global__ void k_probe(const DevParams P, const ProbeArgs A)
         for (int r = 0; r < rows.count; ++r) {
             const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
             if (!P.mixed) {
-                for (int j = A.start_f[c0] + lane, je = A.start_f[c1]; j < je; j += 32) {
+                for (int t = A.start_f[c0] + lane, te = A.start_f[c1]; t < te; t += 32) {
+                    const int j = A.ids_f ? A.ids_f[t] : t;
                     const float4 q = A.fposr[j];
                     fluid(j, q.x - xi.x, q.y - xi.y, q.z - xi.z);
                 }
             }
-            for (int j = A.start_s[c0] + lane, je = A.start_s[c1]; j < je; j += 32) {
+            for (int t = A.start_s[c0] + lane, te = A.start_s[c1]; t < te; t += 32) {
+                const int j = A.ids_s ? A.ids_s[t] : t;
                 const float4 q = A.s_pos[j];
                 const float r2 = dist2(q.x - xi.x, q.y - xi.y, q.z - xi.z);
                 if (r2 < P.R2) {
@@ -1887,10 +2190,16 @@ __global__ void __launch_bounds__(kBlock, 3) kb_solid_fused(const Item<SolidArgs
 }
 
 // ------------------------------------------------------- neighbour counts
-__global__ void k_neighbor_counts(const DevParams P, const float4 *__restrict__ fposr, const int *__restrict__ cell_f,
-                                  const int *__restrict__ start_f, const float4 *__restrict__ s_pos,
-                                  const int *__restrict__ start_s, const float4 *__restrict__ v_posr,
-                                  const int *__restrict__ start_v, int *__restrict__ out, int n)
+// Per fluid particle: fluid, solid and wall particles within the impact
+// distance in its 27 cells.  Neighbour-list instances pass their per-step cell
+// indices (ids_f, ids_s) and the list grid Pv of the walls, whose cells are
+// then located from the particle's position.
+__global__ void k_neighbor_counts(const DevParams P, const DevParams Pv, const float4 *__restrict__ fposr,
+                                  const int *__restrict__ cell_f, const int *__restrict__ start_f,
+                                  const int *__restrict__ ids_f, const float4 *__restrict__ s_pos,
+                                  const int *__restrict__ start_s, const int *__restrict__ ids_s,
+                                  const float4 *__restrict__ v_posr, const int *__restrict__ start_v,
+                                  int *__restrict__ out, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -1900,14 +2209,19 @@ __global__ void k_neighbor_counts(const DevParams P, const float4 *__restrict__ 
     int cf = 0, cs = 0, cv = 0;
     for (int r = 0; r < rows.count; ++r) {
         const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-        for (int j = start_f[c0]; j < start_f[c1]; ++j) {
-            const float4 q = fposr[j];
+        for (int t = start_f[c0]; t < start_f[c1]; ++t) {
+            const float4 q = fposr[ids_f ? ids_f[t] : t];
             cf += dist2(q.x - p.x, q.y - p.y, q.z - p.z) < P.R2;
         }
-        for (int j = start_s[c0]; j < start_s[c1]; ++j) {
-            const float4 q = s_pos[j];
+        for (int t = start_s[c0]; t < start_s[c1]; ++t) {
+            const float4 q = s_pos[ids_s ? ids_s[t] : t];
             cs += dist2(q.x - p.x, q.y - p.y, q.z - p.z) < P.R2;
         }
+    }
+    Rows vrows;
+    neighbor_rows(Pv, ids_f ? cell_index(Pv, p.x, p.y, p.z, nullptr) : cell_f[i], vrows);
+    for (int r = 0; r < vrows.count; ++r) {
+        const int c0 = vrows.base[r] + vrows.z0, c1 = vrows.base[r] + vrows.z1;
         for (int j = start_v[c0]; j < start_v[c1]; ++j) {
             const float4 q = v_posr[j];
             cv += dist2(q.x - p.x, q.y - p.y, q.z - p.z) < P.R2;
@@ -1916,6 +2230,56 @@ __global__ void k_neighbor_counts(const DevParams P, const float4 *__restrict__ 
     out[3 * i] = cf;
     out[3 * i + 1] = cs;
     out[3 * i + 2] = cv;
+}
+
+// The same counts of a neighbour-list instance, from its lists (which hold
+// every pair within the impact distance while no rebuild is due).
+__global__ void k_neighbor_counts_nl(const DevParams P, const float4 *__restrict__ fposr, const int *__restrict__ list,
+                                     const int *__restrict__ cnt, int cap, const float4 *__restrict__ s_pos,
+                                     const float4 *__restrict__ v_posr, int *__restrict__ out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = fposr[i];
+    int c[3] = {0, 0, 0};
+    const int m = min(cnt[i], cap);
+    for (int k = 0; k < m; ++k) {
+        const unsigned e = (unsigned)list[(size_t)k * n + i];
+        const int sp = (int)(e >> kNlSpeciesShift), j = (int)(e & kNlIndexMask);
+        const float4 q = sp == 0 ? fposr[j] : sp == 1 ? v_posr[j] : s_pos[j];
+        if (dist2(q.x - p.x, q.y - p.y, q.z - p.z) < P.R2) ++c[sp == 0 ? 0 : sp == 2 ? 1 : 2];
+    }
+    out[3 * i] = c[0];
+    out[3 * i + 1] = c[1];
+    out[3 * i + 2] = c[2];
+}
+
+// Positions set from the host: fold their squared displacement since the last
+// list build into the instance's running maximum (the next step's decision).
+__global__ void k_nl_displacement(const float4 *__restrict__ posr, const float4 *__restrict__ x0, int n,
+                                  NlState *__restrict__ nl)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned d2 = 0u;
+    if (i < n) {
+        const float4 p = posr[i], o = x0[i];
+        d2 = __float_as_uint(dist2(p.x - o.x, p.y - o.y, p.z - o.z));
+    }
+    d2 = __reduce_max_sync(kFull, d2);
+    if ((threadIdx.x & 31) == 0 && d2) atomicMax(&nl->maxd2, d2);
+}
+
+// cell index of every position (the wall particles' impact-grid cells), and
+// optionally its packed coordinates
+__global__ void k_cells_of(const DevParams P, const float4 *__restrict__ pos, int n, int *__restrict__ out,
+                           unsigned *__restrict__ packed)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    const int c = cell_index(P, p.x, p.y, p.z, nullptr);
+    out[i] = c;
+    if (packed) packed[i] = pack_cell(P, c);
 }
 
 // --------------------------------------------------- (un)permutation
@@ -2168,8 +2532,9 @@ namespace fsim_rt {
     }
 
 // Enqueue a plan's launches; optional events around the fluid sweep.
-fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0, cudaEvent_t sweep1,
-                         const cudaEvent_t *per_launch, unsigned sweep_flags)
+fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape_arg, cudaEvent_t sweep0, cudaEvent_t sweep1,
+                         const cudaEvent_t *per_launch, unsigned sweep_flags, const cudaEvent_t *tune_ev,
+                         int tune_rounds)
 {
     using SweepFn = void (*)(const Item<FluidSweepArgs> *, const int *, int);
     using Sweep1Fn = void (*)(const DevParams, const FluidSweepArgs);
@@ -2202,6 +2567,19 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
         {kb_fluid_sweep_m1<0, Shape0>, kb_fluid_sweep_m1<0, Shape1>, kb_fluid_sweep_m1<0, Shape2>},
         {kb_fluid_sweep_m1<1, Shape0>, kb_fluid_sweep_m1<1, Shape1>, kb_fluid_sweep_m1<1, Shape2>},
         {kb_fluid_sweep_m1<2, Shape0>, kb_fluid_sweep_m1<2, Shape1>, kb_fluid_sweep_m1<2, Shape2>}};
+    // list sweep [VISCID][shape], the variants kSweepNlVariant + VISCID
+    static const Sweep1Fn nl1[3][kSweepShapes] = {
+        {kb_fluid_sweep_nl_1<0, NlShape0>, kb_fluid_sweep_nl_1<0, NlShape1>, kb_fluid_sweep_nl_1<0, NlShape2>},
+        {kb_fluid_sweep_nl_1<1, NlShape0>, kb_fluid_sweep_nl_1<1, NlShape1>, kb_fluid_sweep_nl_1<1, NlShape2>},
+        {kb_fluid_sweep_nl_1<2, NlShape0>, kb_fluid_sweep_nl_1<2, NlShape1>, kb_fluid_sweep_nl_1<2, NlShape2>}};
+    static const SweepPFn nlp[3][kSweepShapes] = {
+        {kb_fluid_sweep_nl_p<0, NlShape0>, kb_fluid_sweep_nl_p<0, NlShape1>, kb_fluid_sweep_nl_p<0, NlShape2>},
+        {kb_fluid_sweep_nl_p<1, NlShape0>, kb_fluid_sweep_nl_p<1, NlShape1>, kb_fluid_sweep_nl_p<1, NlShape2>},
+        {kb_fluid_sweep_nl_p<2, NlShape0>, kb_fluid_sweep_nl_p<2, NlShape1>, kb_fluid_sweep_nl_p<2, NlShape2>}};
+    static const SweepFn nlb[3][kSweepShapes] = {
+        {kb_fluid_sweep_nl<0, NlShape0>, kb_fluid_sweep_nl<0, NlShape1>, kb_fluid_sweep_nl<0, NlShape2>},
+        {kb_fluid_sweep_nl<1, NlShape0>, kb_fluid_sweep_nl<1, NlShape1>, kb_fluid_sweep_nl<1, NlShape2>},
+        {kb_fluid_sweep_nl<2, NlShape0>, kb_fluid_sweep_nl<2, NlShape1>, kb_fluid_sweep_nl<2, NlShape2>}};
     for (size_t k = 0; k < pl.launches.size(); ++k) {
         const Launch &L = pl.launches[k];
         const int *tb = reinterpret_cast<const int *>(pl.arena + L.table_off);
@@ -2216,14 +2594,34 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
         case L_SCATTER: FSIM_LAUNCH(kb_scatter, ScatterArgs, kBlock); break;
         case L_GATHER_F: FSIM_LAUNCH(kb_gather_fluid, GatherFluidArgs, kBlock); break;
         case L_GATHER_S: FSIM_LAUNCH(kb_gather_solid, GatherSolidArgs, kBlock); break;
+        case L_RANK_F:
+        case L_RANK_S: FSIM_LAUNCH(kb_rank, RankArgs, kBlock); break;
+        case L_NL_DECIDE: FSIM_LAUNCH(kb_nl_decide, NlDecideArgs, kBlock); break;
+        case L_NL_BUILD: FSIM_LAUNCH(kb_nl_build, NlBuildArgs, kNlBuildWarps * 32); break;
         case L_COUPLE: FSIM_LAUNCH(kb_couple, CoupleArgs, kBlock); break;
         case L_VIRT: FSIM_LAUNCH(kb_virt, VirtArgs, kBlock); break;
         case L_SWEEP:
             if (sweep0) CK(cudaEventRecordWithFlags(sweep0, st, sweep_flags));
-            {
+            for (int tr = 0; tr < (tune_ev ? tune_rounds * kSweepShapes : 1); ++tr) {
+                const int shape = tune_ev ? tr % kSweepShapes : shape_arg;
+                if (tune_ev) CK(cudaEventRecord(tune_ev[2 * tr], st));
                 const int *tbs = reinterpret_cast<const int *>(pl.arena + L.shape_table_off[shape]);
                 const int gs = L.shape_blocks[shape], thr = kShapeWarps[shape] * 32;
-                if (n == 1) {
+                if (L.variant >= kSweepNlVariant) {
+                    const int v = L.variant - kSweepNlVariant;
+                    if (n == 1) {
+                        const Item<FluidSweepArgs> &it = host_item<FluidSweepArgs>(pl, L);
+                        nl1[v][shape]<<<gs, thr, 0, st>>>(it.P, it.A);
+                    } else if (n <= kSweepParamItems) {
+                        static thread_local SweepBatchParams B;
+                        B.n = n;
+                        std::memcpy(B.bstart, pl.host.data() + L.shape_table_off[shape], sizeof(int) * (n + 1));
+                        std::memcpy(B.it, pl.host.data() + L.items_off, sizeof(Item<FluidSweepArgs>) * n);
+                        nlp[v][shape]<<<gs, thr, 0, st>>>(B);
+                    } else {
+                        nlb[v][shape]<<<gs, thr, 0, st>>>(items_of<FluidSweepArgs>(pl, L), tbs, n);
+                    }
+                } else if (n == 1) {
                     const Item<FluidSweepArgs> &it = host_item<FluidSweepArgs>(pl, L);
                     sweeps1[L.variant][shape]<<<gs, thr, 0, st>>>(it.P, it.A);
                 } else if (L.variant < 6 && n <= kSweepParamItems) {
@@ -2235,8 +2633,9 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t
                 } else {
                     sweeps[L.variant][shape]<<<gs, thr, 0, st>>>(items_of<FluidSweepArgs>(pl, L), tbs, n);
                 }
+                CK_LAUNCH();
+                if (tune_ev) CK(cudaEventRecord(tune_ev[2 * tr + 1], st));
             }
-            CK_LAUNCH();
             if (sweep1) CK(cudaEventRecordWithFlags(sweep1, st, sweep_flags));
             break;
         case L_DEFORM: FSIM_LAUNCH(kb_solid_deform, SolidArgs, kBlock); break;
@@ -2369,9 +2768,24 @@ void launch_k_probe(int grid, cudaStream_t st, const DevParams P, const ProbeArg
     k_probe<<<grid, kBlock, 0, st>>>(P, A);
 }
 
-void launch_k_neighbor_counts(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *cell_f, const int *start_f, const float4 *s_pos, const int *start_s, const float4 *v_posr, const int *start_v, int *out, int n)
+void launch_k_neighbor_counts(int grid, cudaStream_t st, const DevParams P, const DevParams Pv, const float4 *fposr, const int *cell_f, const int *start_f, const int *ids_f, const float4 *s_pos, const int *start_s, const int *ids_s, const float4 *v_posr, const int *start_v, int *out, int n)
 {
-    k_neighbor_counts<<<grid, kBlock, 0, st>>>(P, fposr, cell_f, start_f, s_pos, start_s, v_posr, start_v, out, n);
+    k_neighbor_counts<<<grid, kBlock, 0, st>>>(P, Pv, fposr, cell_f, start_f, ids_f, s_pos, start_s, ids_s, v_posr, start_v, out, n);
+}
+
+void launch_k_neighbor_counts_nl(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *list, const int *cnt, int cap, const float4 *s_pos, const float4 *v_posr, int *out, int n)
+{
+    k_neighbor_counts_nl<<<grid, kBlock, 0, st>>>(P, fposr, list, cnt, cap, s_pos, v_posr, out, n);
+}
+
+void launch_k_nl_displacement(int grid, cudaStream_t st, const float4 *posr, const float4 *x0, int n, NlState *nl)
+{
+    k_nl_displacement<<<grid, kBlock, 0, st>>>(posr, x0, n, nl);
+}
+
+void launch_k_cells_of(int grid, cudaStream_t st, const DevParams P, const float4 *pos, int n, int *out, unsigned *packed)
+{
+    k_cells_of<<<grid, kBlock, 0, st>>>(P, pos, n, out, packed);
 }
 
 void launch_k_conservation_fluid(int grid, cudaStream_t st, const DevParams P, const float4 *posr, const float4 *velp, const int *cell, int n, double vol, double *partials)
@@ -2390,5 +2804,16 @@ void launch_k_case_generate(int grid, cudaStream_t st, const CaseGenArgs A)
 }
 
 } // namespace fsim_rt
+
+#ifdef FSIM_DEVICE_CHECKS
+// debugging build only: the check sites that failed since the last call (bit
+// per site, see FSIM_DCHECK), cleared by the call
+extern "C" int fsim_debug_check_sites(unsigned *out)
+{
+    unsigned zero = 0;
+    if (cudaMemcpyFromSymbol(out, g_check_sites, sizeof(unsigned)) != cudaSuccess) return 1;
+    return cudaMemcpyToSymbol(g_check_sites, &zero, sizeof(unsigned)) != cudaSuccess;
+}
+#endif
 static_assert(sizeof(fsim_rt::ParamBlock<fsim_rt::SolidArgs>) <= 32764, "parameter block size");
 static_assert(fsim_rt::ParamBlock<fsim_rt::SolidArgs>::kMax >= 64, "a 64-instance ensemble fits");

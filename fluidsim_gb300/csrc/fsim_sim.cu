@@ -31,17 +31,19 @@ struct NvtxRange {
 namespace {
 
 // Online autotuner of the fluid sweep's launch shape (see run_plan_step).
+constexpr int kTuneRounds = 2; // each shape is timed this many times; the fastest time counts
 struct SweepTuner {
     int chosen = -1; // shape index once tuned
-    int next = 0;    // next shape to time
+    int next = 0;    // shapes timed
     float ms[kSweepShapes] = {};
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEvent_t ev[2 * kSweepShapes * kTuneRounds] = {};
     int shape() const { return chosen >= 0 ? chosen : 0; }
     void release()
     {
-        if (e0) cudaEventDestroy(e0);
-        if (e1) cudaEventDestroy(e1);
-        e0 = e1 = nullptr;
+        for (cudaEvent_t &e : ev) {
+            if (e) cudaEventDestroy(e);
+            e = nullptr;
+        }
     }
 };
 }
@@ -90,6 +92,23 @@ struct fsim_sim {
     // virtual
     float4 *v_posr = nullptr, *v_velp = nullptr, *v_normal = nullptr;
     int *v_orig = nullptr, *v_cell = nullptr, *v_start = nullptr;
+    // fluid neighbour lists (nl): particles sorted on the list grid Pl (cells of
+    // at least the list radius) at every list build and left in that order in
+    // between; per step an index of the impact grid (f_start/f_ids, s_start/
+    // s_ids; f_cell/s_cell/s_cxyz per slot) serves the other phases.  Walls are
+    // sorted on the list grid (v_cell, v_start); v_icell is their impact-grid cell.
+    bool nl = false;
+    bool nl_check = false;        // pairs also need neighbouring impact-grid cells (f_cxyz, v_icxyz, s_cxyz)
+    unsigned *f_cxyz = nullptr, *v_icxyz = nullptr;
+    DevParams Pl;                 // the list grid's parameters (else unused)
+    int ncell_l = 0, nl_cap = 0;
+    float nl_R2s = 0.0f, nl_move2 = 0.0f;
+    int *nl_list = nullptr, *nl_cnt = nullptr;
+    NlState *nl_state = nullptr;
+    float4 *f_x0 = nullptr, *s_x0 = nullptr;
+    int *f_ids = nullptr, *f_lcell = nullptr, *f_lcnt = nullptr, *f_lstart = nullptr;
+    int *s_ids = nullptr, *s_lcell = nullptr, *s_lcnt = nullptr, *s_lstart = nullptr;
+    int *v_icell = nullptr;
     // misc
     int *scan_partials = nullptr; // 2 * kMaxScanTiles
     unsigned *d_flags = nullptr;
@@ -305,9 +324,151 @@ void add_sweep_launch(Plan &pl, ArenaBuilder &ab, const std::vector<Item<FluidSw
     pl.launches.push_back(L);
 }
 
+// The cell phase of neighbour-list instances (parity pf -> 1-pf, ps -> 1-ps):
+// the list decision; on a rebuild, the counting sort of fluid and solid on the
+// list grid, else an unpermuted copy; the per-step impact-grid index; on a
+// rebuild, the list build.
+void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
+{
+    std::vector<Item<NlDecideArgs>> di;
+    std::vector<int> db;
+    for (fsim_sim *h : m) {
+        NlDecideArgs a{h->nl_state, h->s_pos[ps], h->s_x0, h->ns, h->nl_move2};
+        Item<NlDecideArgs> it{h->P, a};
+        di.push_back(it);
+        db.push_back(1);
+    }
+    add_launch(pl, ab, L_NL_DECIDE, di, db);
+    // list-grid sort, run only when the decision says rebuild
+    std::vector<Item<ZeroArgs>> zi;
+    std::vector<Item<HashArgs>> hi;
+    std::vector<Item<ScanArgs>> si;
+    std::vector<Item<ScatterArgs>> ci;
+    std::vector<int> zb, hb, sb, sp, cb;
+    for (fsim_sim *h : m) {
+        const int *gate = &h->nl_state->rebuild;
+        for (int s_ = 0; s_ < 2; ++s_) {
+            const int n = s_ ? h->ns : h->nf;
+            int *lcnt = s_ ? h->s_lcnt : h->f_lcnt, *lstart = s_ ? h->s_lstart : h->f_lstart;
+            const Item<ZeroArgs> z{h->Pl, ZeroArgs{lcnt, n ? h->ncell_l : 0, gate}};
+            zi.push_back(z);
+            zb.push_back(blocks_for(z.A.n, kBlock));
+            const HashArgs ha = s_ ? HashArgs{h->s_pos[ps], h->ns, h->s_key, h->s_slot, lcnt, h->d_flags, gate}
+                                   : HashArgs{h->f_posr[pf], h->nf, h->f_key, h->f_slot, lcnt, h->d_flags, gate};
+            const Item<HashArgs> hh{h->Pl, ha};
+            hi.push_back(hh);
+            hb.push_back(blocks_for(n, kBlock));
+            const Item<ScanArgs> sc{h->Pl,
+                                    ScanArgs{lcnt, lstart, h->ncell_l, h->scan_partials + (s_ ? kMaxScanTiles : 0), gate}};
+            si.push_back(sc);
+            sb.push_back(n ? blocks_for(h->ncell_l, kScanTile) : 0);
+            sp.push_back(n ? 1 : 0);
+            const ScatterArgs ca = s_ ? ScatterArgs{h->s_key, h->s_slot, lstart, h->s_tmp, h->ns, gate}
+                                      : ScatterArgs{h->f_key, h->f_slot, lstart, h->f_tmp, h->nf, gate};
+            const Item<ScatterArgs> cc{h->Pl, ca};
+            ci.push_back(cc);
+            cb.push_back(blocks_for(n, kBlock));
+        }
+    }
+    add_launch(pl, ab, L_ZERO, zi, zb);
+    add_launch(pl, ab, L_HASH, hi, hb);
+    add_launch(pl, ab, L_SCAN_REDUCE, si, sb);
+    add_launch(pl, ab, L_SCAN_PARTIALS, si, sp);
+    add_launch(pl, ab, L_SCAN_APPLY, si, sb);
+    add_launch(pl, ab, L_SCATTER, ci, cb);
+    std::vector<Item<GatherFluidArgs>> gf;
+    std::vector<Item<GatherSolidArgs>> gs;
+    std::vector<int> gfb, gsb;
+    for (fsim_sim *h : m) {
+        const int *gate = &h->nl_state->rebuild;
+        const GatherFluidArgs fa{h->f_tmp, h->f_key, h->f_lstart, h->nf, h->f_posr[pf], h->f_velp[pf], h->f_orig[pf],
+                                 h->f_posr[1 - pf], h->f_velp[1 - pf], h->f_orig[1 - pf], h->f_lcell, h->d_flags,
+                                 gate, h->f_x0};
+        const Item<GatherFluidArgs> fi{h->Pl, fa};
+        gf.push_back(fi);
+        gfb.push_back(blocks_for(h->nf, kBlock));
+        const GatherSolidArgs sa{h->s_tmp, h->s_key, h->s_lstart, h->ns, h->s_pos[ps], h->s_vel[ps], h->s_ref[ps],
+                                 h->s_type[ps], h->s_orig[ps], h->s_pos[1 - ps], h->s_vel[1 - ps], h->s_ref[1 - ps],
+                                 h->s_type[1 - ps], h->s_orig[1 - ps], h->s_lcell, h->s_inv, nullptr, h->d_flags,
+                                 gate, h->s_x0};
+        const Item<GatherSolidArgs> sg{h->Pl, sa};
+        gs.push_back(sg);
+        gsb.push_back(blocks_for(h->ns, kBlock));
+    }
+    add_launch(pl, ab, L_GATHER_F, gf, gfb);
+    add_launch(pl, ab, L_GATHER_S, gs, gsb);
+    // the per-step impact-grid index of the particles as they now lie
+    zi.clear();
+    hi.clear();
+    si.clear();
+    ci.clear();
+    zb.clear();
+    hb.clear();
+    sb.clear();
+    sp.clear();
+    cb.clear();
+    std::vector<Item<RankArgs>> ri;
+    std::vector<int> rb;
+    for (fsim_sim *h : m) {
+        for (int s_ = 0; s_ < 2; ++s_) {
+            const int n = s_ ? h->ns : h->nf;
+            int *cnt = s_ ? h->s_cnt : h->f_cnt, *start = s_ ? h->s_start : h->f_start;
+            const Item<ZeroArgs> z{h->P, ZeroArgs{cnt, n ? h->ncell : 0, nullptr}};
+            zi.push_back(z);
+            zb.push_back(blocks_for(z.A.n, kBlock));
+            const HashArgs ha = s_ ? HashArgs{h->s_pos[1 - ps], h->ns, h->s_key, h->s_slot, cnt, h->d_flags, nullptr}
+                                   : HashArgs{h->f_posr[1 - pf], h->nf, h->f_key, h->f_slot, cnt, h->d_flags, nullptr};
+            const Item<HashArgs> hh{h->P, ha};
+            hi.push_back(hh);
+            hb.push_back(blocks_for(n, kBlock));
+            const Item<ScanArgs> sc{h->P,
+                                    ScanArgs{cnt, start, h->ncell, h->scan_partials + (s_ ? kMaxScanTiles : 0), nullptr}};
+            si.push_back(sc);
+            sb.push_back(n ? blocks_for(h->ncell, kScanTile) : 0);
+            sp.push_back(n ? 1 : 0);
+            const ScatterArgs ca = s_ ? ScatterArgs{h->s_key, h->s_slot, start, h->s_tmp, h->ns, nullptr}
+                                      : ScatterArgs{h->f_key, h->f_slot, start, h->f_tmp, h->nf, nullptr};
+            const Item<ScatterArgs> cc{h->P, ca};
+            ci.push_back(cc);
+            cb.push_back(blocks_for(n, kBlock));
+            const RankArgs ra = s_ ? RankArgs{h->s_tmp, h->s_key, start, h->ns, h->s_ids, h->s_cell, h->s_cxyz,
+                                              h->d_flags}
+                                   : RankArgs{h->f_tmp, h->f_key, start, h->nf, h->f_ids, h->f_cell, h->f_cxyz,
+                                              h->d_flags};
+            const Item<RankArgs> rr{h->P, ra};
+            ri.push_back(rr);
+            rb.push_back(blocks_for(n, kBlock));
+        }
+    }
+    add_launch(pl, ab, L_ZERO, zi, zb);
+    add_launch(pl, ab, L_HASH, hi, hb);
+    add_launch(pl, ab, L_SCAN_REDUCE, si, sb);
+    add_launch(pl, ab, L_SCAN_PARTIALS, si, sp);
+    add_launch(pl, ab, L_SCAN_APPLY, si, sb);
+    add_launch(pl, ab, L_SCATTER, ci, cb);
+    add_launch(pl, ab, L_RANK_F, ri, rb);
+    // the list build (runs only on a rebuild)
+    std::vector<Item<NlBuildArgs>> bi;
+    std::vector<int> bb;
+    for (fsim_sim *h : m) {
+        const NlBuildArgs ba{h->f_x0,   h->f_lcell,  h->f_lstart, h->v_posr,  h->v_start,
+                             h->s_x0,   h->s_lstart, h->nf,       h->nl_cap,  h->nl_list,
+                             h->nl_cnt, h->nl_state, h->d_flags,  h->nl_R2s,  h->nv,
+                             h->ns};
+        const Item<NlBuildArgs> bt{h->Pl, ba};
+        bi.push_back(bt);
+        bb.push_back(blocks_for(h->nf, kNlBuildThreads));
+    }
+    add_launch(pl, ab, L_NL_BUILD, bi, bb);
+}
+
 // The cell phase: counting sort of fluid and solid (parity pf -> 1-pf, ps -> 1-ps).
 void plan_cell(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
 {
+    if (!m.empty() && m[0]->nl) {
+        plan_cell_nl(pl, ab, m, pf, ps);
+        return;
+    }
     std::vector<Item<ZeroArgs>> zi;
     std::vector<Item<HashArgs>> hi;
     std::vector<Item<HashMixedArgs>> hmi;
@@ -380,8 +541,11 @@ void plan_couple(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, i
     std::vector<Item<CoupleArgs>> it;
     std::vector<int> nb;
     for (fsim_sim *h : m) {
-        it.push_back({h->P, CoupleArgs{h->s_pos[ps], h->s_cell, h->s_start, h->f_posr[pf], h->f_velp[pf], h->f_start,
-                                       h->s_np, h->ns}});
+        const CoupleArgs ca{h->s_pos[ps], h->s_cell,  h->s_start, h->f_posr[pf], h->f_velp[pf],
+                            h->f_start,   h->s_np,    h->ns,      h->nf,         h->nl ? h->f_ids : nullptr,
+                            h->nl ? h->s_ids : nullptr};
+        const Item<CoupleArgs> ci{h->P, ca};
+        it.push_back(ci);
         nb.push_back(h->nf && h->ns ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
     }
     add_launch(pl, ab, m.empty() || !m[0]->mixed ? L_COUPLE : L_COUPLE_M, it, nb);
@@ -392,8 +556,10 @@ void plan_virt(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
     std::vector<Item<VirtArgs>> it;
     std::vector<int> nb;
     for (fsim_sim *h : m) {
-        it.push_back({h->P, VirtArgs{h->v_posr, h->v_normal, h->v_cell, h->f_posr[pf], h->f_velp[pf], h->f_orig[pf],
-                                     h->f_start, h->v_posr, h->v_velp, h->nv}});
+        const VirtArgs va{h->v_posr,  h->v_normal, h->nl ? h->v_icell : h->v_cell, h->f_posr[pf], h->f_velp[pf],
+                          h->f_orig[pf], h->f_start, h->v_posr, h->v_velp, h->nv, h->nf, h->nl ? h->f_ids : nullptr};
+        const Item<VirtArgs> vi{h->P, va};
+        it.push_back(vi);
         nb.push_back(blocks_for(h->nv, kBlock));
     }
     add_launch(pl, ab, m.empty() || !m[0]->mixed ? L_VIRT : L_VIRT_M, it, nb);
@@ -428,6 +594,16 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         A.n = h->nf;
         A.keep = h->keep ? 1 : 0;
         A.cm = h->f_cm;
+        A.nl_list = h->nl_list;
+        A.nl_cnt = h->nl_cnt;
+        A.nl_cap = h->nl_cap;
+        A.nl_nv = h->nv;
+        A.nl_ns = h->ns;
+        A.x0 = h->f_x0;
+        A.nl = h->nl_state;
+        A.nl_cxyz_f = h->nl_check ? h->f_cxyz : nullptr;
+        A.nl_cxyz_v = h->nl_check ? h->v_icxyz : nullptr;
+        A.nl_cxyz_s = h->nl_check ? h->s_cxyz : nullptr;
         it.push_back({h->P, A});
         for (int sh = 0; sh < kSweepShapes; ++sh) nb[sh].push_back(blocks_for(h->nf, kShapeWarps[sh] * 32));
         if (h->nf) {
@@ -438,8 +614,9 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
     const int n_active = (int)std::count_if(m.begin(), m.end(), [](fsim_sim *h) { return h->nf > 0; });
     const int visc_mode = nvisc == 0 ? 0 : nvisc == n_active ? 1 : 2;
     const size_t before = pl.launches.size();
-    const bool mixed = !m.empty() && m[0]->mixed;
-    add_sweep_launch(pl, ab, it, nb, mixed ? 6 + visc_mode : (any_check ? 3 : 0) + visc_mode);
+    const bool mixed = !m.empty() && m[0]->mixed, nl = !m.empty() && m[0]->nl;
+    add_sweep_launch(pl, ab, it, nb,
+                     nl ? kSweepNlVariant + visc_mode : mixed ? 6 + visc_mode : (any_check ? 3 : 0) + visc_mode);
     if (pl.launches.size() > before) pl.sweep_index = (int)before;
 }
 
@@ -463,7 +640,6 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         S.ref = h->s_ref[ps];
         S.type = h->s_type[ps];
         S.cell = h->s_cell;
-        S.start_s = h->s_start;
         S.np = h->s_np;
         S.F = h->s_F;
         S.Pk = h->s_P;
@@ -476,6 +652,7 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         S.fvelp = h->f_velp[pf];
         S.start_f = h->f_start;
         S.n = h->ns;
+        S.nf = h->nf;
         S.orig = h->s_orig[ps];
         S.inv = h->s_inv;
         S.nbr_off = h->s_nbr_off;
@@ -489,6 +666,7 @@ void plan_solid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         S.cxyz = h->s_cxyz;
         S.nsub = h->ns ? h->cfg.solid_sub_step : 0;
         S.flags = h->d_flags;
+        S.ids_f = h->nl ? h->f_ids : nullptr;
         it.push_back({h->P, S});
         tw[q + 1] = tw[q] + (h->ns ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
         tt[q + 1] = tt[q] + (h->ns ? blocks_for(h->ns, kBlock) : 0);
@@ -668,26 +846,33 @@ fsim_status handle_step_plan(fsim_sim *h, Plan **out)
 }
 
 // One step of a plan: while the sweep's launch shape is untuned, run launch
-// by launch with the next candidate shape and time its sweep (CUDA events on
-// the stream, waited for on the host); once every shape has been timed, keep
-// the fastest and run the plan as a CUDA graph captured with it.
+// by launch and, in place of the one sweep, sweep kTuneRounds times with every
+// candidate shape, timing each (CUDA events on the stream, waited for on the
+// host).  A sweep is a pure function of its input buffer (it writes the other
+// buffer; its running displacement maximum is idempotent) and the shapes give
+// bit-identical results, so the step's outcome is the same.  Then keep the
+// fastest shape and run the plan as a CUDA graph captured with it.
 fsim_status run_plan_step(Plan &pl, cudaStream_t st, SweepTuner &t)
 {
     if (t.chosen < 0 && pl.sweep_index >= 0) {
-        if (!t.e0) {
-            CK(cudaEventCreate(&t.e0));
-            CK(cudaEventCreate(&t.e1));
-        }
-        const int s = t.next;
-        fsim_status r = enqueue_plan(pl, st, s, t.e0, t.e1);
+        for (cudaEvent_t &e : t.ev)
+            if (!e) CK(cudaEventCreate(&e));
+        fsim_status r = enqueue_plan(pl, st, 0, nullptr, nullptr, nullptr, cudaEventRecordDefault, t.ev, kTuneRounds);
         if (r) return r;
-        CK(cudaEventSynchronize(t.e1));
-        CK(cudaEventElapsedTime(&t.ms[s], t.e0, t.e1));
-        if (++t.next == kSweepShapes) {
-            t.chosen = 0;
-            for (int k = 1; k < kSweepShapes; ++k)
-                if (t.ms[k] < t.ms[t.chosen]) t.chosen = k;
+        CK(cudaEventSynchronize(t.ev[2 * kSweepShapes * kTuneRounds - 1]));
+        for (int s_ = 0; s_ < kSweepShapes; ++s_) {
+            t.ms[s_] = 0.0f;
+            for (int r_ = 0; r_ < kTuneRounds; ++r_) {
+                const int k = 2 * (r_ * kSweepShapes + s_);
+                float ms = 0.0f;
+                CK(cudaEventElapsedTime(&ms, t.ev[k], t.ev[k + 1]));
+                if (r_ == 0 || ms < t.ms[s_]) t.ms[s_] = ms;
+            }
         }
+        t.next = kSweepShapes;
+        t.chosen = 0;
+        for (int k = 1; k < kSweepShapes; ++k)
+            if (t.ms[k] < t.ms[t.chosen]) t.chosen = k;
         return FSIM_OK;
     }
     if (t.chosen < 0) t.chosen = 0; // no fluid: nothing to tune
@@ -721,6 +906,11 @@ fsim_status check_flags(fsim_sim *h)
     }
     if (flags & FLAG_OUT_OF_GRID) {
         fsim_set_error("a particle position fell outside the cell grid (clamped)");
+        return FSIM_ENUMERIC;
+    }
+    if (flags & FLAG_LIST_OVERFLOW) {
+        fsim_set_error("a fluid particle has more than %d neighbour-list candidates (results invalid); "
+                       "lower gb300_neighbor_skin or set it to 0", h->nl_cap);
         return FSIM_ENUMERIC;
     }
     if (flags & FLAG_CELL_OVERFULL) {
@@ -757,9 +947,13 @@ fsim_status sort_virtual(fsim_sim *h, const float *vpos_host, float4 *vpos_dev =
     float4 *tmp_pos = nullptr;
     int *key = nullptr, *slot = nullptr, *tmp = nullptr, *cnt = nullptr, *orig0 = nullptr;
     fsim_status st;
+    // neighbour-list instances keep their walls on the list grid (the list
+    // build walks them there) and note each wall's impact-grid cell
+    const DevParams &G = h->nl ? h->Pl : h->P;
+    const int gcells = h->nl ? h->ncell_l : h->ncell;
     if ((st = dalloc(h, &d_xyz, vpos_dev ? 1 : 3 * (size_t)n)) || (st = dalloc(h, &tmp_pos, n)) ||
         (st = dalloc(h, &key, n)) || (st = dalloc(h, &slot, n)) || (st = dalloc(h, &tmp, n)) ||
-        (st = dalloc(h, &cnt, h->ncell)) || (st = dalloc(h, &orig0, n)))
+        (st = dalloc(h, &cnt, gcells)) || (st = dalloc(h, &orig0, n)))
         return st;
     if (vpos_dev) {
         CK(cudaMemcpyAsync(tmp_pos, vpos_dev, sizeof(float4) * n, cudaMemcpyDeviceToDevice, h->stream));
@@ -771,29 +965,32 @@ fsim_status sort_virtual(fsim_sim *h, const float *vpos_host, float4 *vpos_dev =
     CK_LAUNCH();
     Plan pl;
     ArenaBuilder ab;
-    add_launch(pl, ab, L_ZERO, std::vector<Item<ZeroArgs>>{{h->P, ZeroArgs{cnt, h->ncell}}},
-               {blocks_for(h->ncell, kBlock)});
-    add_launch(pl, ab, L_HASH, std::vector<Item<HashArgs>>{{h->P, HashArgs{tmp_pos, n, key, slot, cnt, h->d_flags}}},
+    add_launch(pl, ab, L_ZERO, std::vector<Item<ZeroArgs>>{{G, ZeroArgs{cnt, gcells, nullptr}}},
+               {blocks_for(gcells, kBlock)});
+    add_launch(pl, ab, L_HASH,
+               std::vector<Item<HashArgs>>{{G, HashArgs{tmp_pos, n, key, slot, cnt, h->d_flags, nullptr}}},
                {blocks_for(n, kBlock)});
-    const std::vector<Item<ScanArgs>> sc{{h->P, ScanArgs{cnt, h->v_start, h->ncell, h->scan_partials}}};
-    add_launch(pl, ab, L_SCAN_REDUCE, sc, {blocks_for(h->ncell, kScanTile)});
+    const std::vector<Item<ScanArgs>> sc{{G, ScanArgs{cnt, h->v_start, gcells, h->scan_partials, nullptr}}};
+    add_launch(pl, ab, L_SCAN_REDUCE, sc, {blocks_for(gcells, kScanTile)});
     add_launch(pl, ab, L_SCAN_PARTIALS, sc, {1});
-    add_launch(pl, ab, L_SCAN_APPLY, sc, {blocks_for(h->ncell, kScanTile)});
-    add_launch(pl, ab, L_SCATTER, std::vector<Item<ScatterArgs>>{{h->P, ScatterArgs{key, slot, h->v_start, tmp, n}}},
+    add_launch(pl, ab, L_SCAN_APPLY, sc, {blocks_for(gcells, kScanTile)});
+    add_launch(pl, ab, L_SCATTER,
+               std::vector<Item<ScatterArgs>>{{G, ScatterArgs{key, slot, h->v_start, tmp, n, nullptr}}},
                {blocks_for(n, kBlock)});
     // the fluid gather with a dummy velocity stream
     add_launch(pl, ab, L_GATHER_F,
-               std::vector<Item<GatherFluidArgs>>{{h->P, GatherFluidArgs{tmp, key, h->v_start, n, tmp_pos, tmp_pos,
-                                                                         orig0, h->v_posr, h->v_velp, h->v_orig,
-                                                                         h->v_cell, h->d_flags}}},
+               std::vector<Item<GatherFluidArgs>>{{G, GatherFluidArgs{tmp, key, h->v_start, n, tmp_pos, tmp_pos,
+                                                                      orig0, h->v_posr, h->v_velp, h->v_orig,
+                                                                      h->v_cell, h->d_flags, nullptr, nullptr}}},
                {blocks_for(n, kBlock)});
     pl.host = ab.bytes;
     CK(cudaMalloc((void **)&pl.arena, ab.bytes.size()));
     cudaError_t e = cudaMemcpy(pl.arena, ab.bytes.data(), ab.bytes.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && (st = enqueue_plan(pl, h->stream, 0)) == FSIM_OK) {
         e = cudaMemsetAsync(h->v_velp, 0, sizeof(float4) * n, h->stream);
-        launch_k_virt_normal(blocks_for(n, kBlock), h->stream, h->P, h->v_posr, h->v_cell, h->v_start,
-                                                                        h->v_normal, n);
+        // the normal sums the walls within R: any grid of cells >= R finds them
+        launch_k_virt_normal(blocks_for(n, kBlock), h->stream, G, h->v_posr, h->v_cell, h->v_start, h->v_normal, n);
+        if (h->nl) launch_k_cells_of(blocks_for(n, kBlock), h->stream, h->P, h->v_posr, n, h->v_icell, h->v_icxyz);
         if (e == cudaSuccess) e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     }
@@ -935,6 +1132,28 @@ fsim_status alloc_state(fsim_sim *h)
     if ((st = dalloc(h, &h->v_posr, nv)) || (st = dalloc(h, &h->v_velp, nv)) || (st = dalloc(h, &h->v_normal, nv)) ||
         (st = dalloc(h, &h->v_orig, nv)) || (st = dalloc(h, &h->v_cell, nv)) || (st = dalloc(h, &h->v_start, nc + 1)))
         return st;
+    // fluid neighbour lists
+    if (h->nl) {
+        const int ncl = h->ncell_l;
+        if ((st = dalloc(h, &h->nl_list, (size_t)h->nl_cap * nf)) || (st = dalloc(h, &h->nl_cnt, nf)) ||
+            (st = dalloc(h, &h->nl_state, 1)) || (st = dalloc(h, &h->f_x0, nf)) || (st = dalloc(h, &h->s_x0, ns)) ||
+            (st = dalloc(h, &h->f_ids, nf)) || (st = dalloc(h, &h->f_lcell, nf)) ||
+            (st = dalloc(h, &h->f_lcnt, ncl)) || (st = dalloc(h, &h->f_lstart, ncl + 1)) ||
+            (st = dalloc(h, &h->s_ids, ns)) || (st = dalloc(h, &h->s_lcell, ns)) ||
+            (st = dalloc(h, &h->s_lcnt, ncl)) || (st = dalloc(h, &h->s_lstart, ncl + 1)) ||
+            (st = dalloc(h, &h->v_icell, nv)))
+            return st;
+        if (h->nl_check && ((st = dalloc(h, &h->f_cxyz, nf)) || (st = dalloc(h, &h->v_icxyz, nv)))) return st;
+        NlState init{};
+        init.force = 1; // the first step builds
+        CK(cudaMemcpyAsync(h->nl_state, &init, sizeof init, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemsetAsync(h->nl_cnt, 0, sizeof(int) * (nf ? nf : 1), h->stream));
+        CK(cudaMemsetAsync(h->f_x0, 0, sizeof(float4) * (nf ? nf : 1), h->stream));
+        CK(cudaMemsetAsync(h->s_x0, 0, sizeof(float4) * (ns ? ns : 1), h->stream));
+        CK(cudaMemsetAsync(h->f_lstart, 0, sizeof(int) * (ncl + 1), h->stream));
+        CK(cudaMemsetAsync(h->s_lstart, 0, sizeof(int) * (ncl + 1), h->stream));
+        CK(cudaStreamSynchronize(h->stream)); // `init` leaves scope
+    }
     // staging for field copies (input order)
     size_t words = 3 * (size_t)nf;
     if (9 * (size_t)ns > words) words = 9 * (size_t)ns;
@@ -1014,6 +1233,61 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
 
 // =================================================================== C ABI
 namespace {
+// Fluid neighbour lists (cfg.neighbor_skin > 0, plain form): list radius
+// Rs = R (1 + skin); a step rebuilds once any particle has moved more than
+// (Rs - R) / 2 less a rounding allowance since the last build, so that every
+// pair within R is in the lists.  The reference pairs particles within R in
+// neighbouring cells; where every cell side exceeds R by more than the FP32
+// rounding of the cell coordinate (the stream sweep's z re-check rule, here
+// on all three axes) that is the set {r < R}, else (nl_check) the list sweep
+// also compares the pair's packed cell coordinates.  The list grid has cells
+// of at least Rs (1 + 1e-3) on the reference grid's origin.
+void setup_lists(fsim_sim *h)
+{
+    h->nl = false;
+    h->nl_check = false;
+    const double skin = h->cfg.neighbor_skin;
+    if (h->mixed || !(skin > 0.0) || h->nf > kNlIndexMask || h->nv > kNlIndexMask || h->ns > kNlIndexMask) return;
+    const double R = std::sqrt((double)h->der.impact_distance_square);
+    for (int a = 0; a < 3; ++a) {
+        const double margin = (double)h->der.interval[a] / R - 1.0;
+        if (!(margin > 8e-7 * h->der.cell_number[a] + 1e-4)) h->nl_check = true;
+    }
+    // packed coordinates (x | y << 11 | z << 21) for the check
+    if (h->nl_check && (h->P.nx >= 2048 || h->P.ny >= 1024 || h->P.nz >= 2048)) return;
+    const double Rs = R * (1.0 + skin);
+    double maxabs = 0.0;
+    for (int a = 0; a < 3; ++a)
+        maxabs = std::max(maxabs, std::max(std::fabs((double)h->der.cell_min[a]), std::fabs((double)h->der.cell_max[a])));
+    // positions and their differences carry FP32 rounding of the coordinates
+    const double slack = 16.0 * std::ldexp(maxabs, -23) + 1e-3 * (Rs - R);
+    const double move = 0.5 * (Rs - R) - slack;
+    if (!(move > 0.0)) return;
+    DevParams Pl = h->P;
+    int n[3];
+    for (int a = 0; a < 3; ++a) {
+        const double L = (double)h->der.cell_max[a] - (double)h->der.cell_min[a];
+        n[a] = std::max(1, (int)std::floor(L / (Rs * (1.0 + 1e-3))));
+        Pl.cinv[a] = (float)(n[a] / L);
+        Pl.cdx[a] = (float)(L / n[a]);
+        // the cells must still hold Rs with the FP32 inverse the kernels use
+        if (!(1.0 / (double)Pl.cinv[a] >= Rs * (1.0 + 5e-4))) return;
+    }
+    Pl.nx = n[0];
+    Pl.ny = n[1];
+    Pl.nz = n[2];
+    Pl.ncell = n[0] * n[1] * n[2];
+    h->Pl = Pl;
+    h->ncell_l = Pl.ncell;
+    h->nl_R2s = (float)(Rs * Rs);
+    h->nl_move2 = (float)(move * move);
+    // list capacity: 1.5x a full sphere of radius Rs at the particle spacing
+    const double dx = h->cfg.particle_diameter;
+    const double full = 4.0 / 3.0 * 3.14159265358979 * std::pow(Rs / dx, 3.0);
+    h->nl_cap = ((int)std::ceil(1.5 * full) + 16 + 3) & ~3;
+    h->nl = true;
+}
+
 // A handle with its configuration, derived constants, device parameters and
 // counts set and checked; nothing allocated on the device yet.
 fsim_status new_handle(const fsim_config *cfg, int nf, int ns, int nv, int device, fsim_sim **out)
@@ -1071,6 +1345,7 @@ fsim_status new_handle(const fsim_config *cfg, int nf, int ns, int nv, int devic
         const double margin = (double)h->der.interval[2] / R - 1.0;
         h->check_z = !(margin > 8e-7 * h->der.cell_number[2] + 1e-4);
     }
+    setup_lists(h);
     *out = h;
     return FSIM_OK;
 }
@@ -1304,7 +1579,7 @@ fsim_status enqueue_unpermute(fsim_sim *h, int field, int n, float *stg)
     case FSIM_VIRT_P: launch_k_unpermute_f4(g, h->stream, h->v_velp, h->v_orig, n, 3, 1, stg); break;
     case FSIM_VIRT_NORMAL: launch_k_unpermute_f4(g, h->stream, h->v_normal, h->v_orig, n, 0, 3, stg); break;
     case FSIM_VIRT_CELL_ID:
-        launch_k_unpermute_words(g, h->stream, h->v_cell, h->v_orig, n, 1, (int *)stg);
+        launch_k_unpermute_words(g, h->stream, h->nl ? h->v_icell : h->v_cell, h->v_orig, n, 1, (int *)stg);
         break;
     default: return FSIM_EINVAL;
     }
@@ -1352,7 +1627,10 @@ fsim_status set_target(fsim_sim *h, int field, float4 **dst, const int **orig, i
 }
 
 // Enqueue on the handle's stream the kernel that scatters `field` (input
-// order, device memory `stg`) into the state (n > 0).
+// order, device memory `stg`) into the state (n > 0).  New fluid positions of
+// a neighbour-list instance count as displacement since the last list build
+// (the next step rebuilds if they moved too far); the solid's are measured at
+// the next step's decision anyway.
 fsim_status enqueue_permute_in(fsim_sim *h, int field, int n, const float *stg)
 {
     float4 *dst = nullptr;
@@ -1368,6 +1646,10 @@ fsim_status enqueue_permute_in(fsim_sim *h, int field, int n, const float *stg)
     else
         launch_k_permute_in_f4(blocks_for(n, kBlock), h->stream, dst, orig, n, comp, width, stg);
     CK_LAUNCH();
+    if (h->nl && field == FSIM_FLUID_POS) {
+        launch_k_nl_displacement(blocks_for(n, kBlock), h->stream, dst, h->f_x0, n, h->nl_state);
+        CK_LAUNCH();
+    }
     return FSIM_OK;
 }
 } // namespace
@@ -1512,6 +1794,8 @@ extern "C" fsim_status fsim_probe(fsim_handle h, const float *points, int n, flo
     A.s_vel = h->s_vel[h->s_cur];
     A.s_np = h->s_np;
     A.start_s = h->s_start;
+    A.ids_f = h->nl ? h->f_ids : nullptr;
+    A.ids_s = h->nl ? h->s_ids : nullptr;
     cudaError_t e = cudaMemcpyAsync(d, points, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) {
         launch_k_probe(blocks_for(32ll * n, kBlock), h->stream, h->P, A);
@@ -1548,11 +1832,86 @@ extern "C" fsim_status fsim_neighbor_counts(fsim_handle h, int *out, size_t byte
     DeviceGuard guard(h->device);
     int *d_counts = (int *)h->staging; // 3 * nf words fit the staging buffer
     const int g = blocks_for(h->nf, kBlock);
-    launch_k_neighbor_counts(g, h->stream, h->P, h->f_posr[h->f_cur], h->f_cell, h->f_start,
-                                                    h->s_pos[h->s_cur], h->s_start, h->v_posr, h->v_start, d_counts,
-                                                    h->nf);
+    launch_k_neighbor_counts(g, h->stream, h->P, h->nl ? h->Pl : h->P, h->f_posr[h->f_cur], h->f_cell, h->f_start,
+                             h->nl ? h->f_ids : nullptr, h->s_pos[h->s_cur], h->s_start, h->nl ? h->s_ids : nullptr,
+                             h->v_posr, h->v_start, d_counts, h->nf);
     CK_LAUNCH();
     // reorder to input order in place is not possible; copy sorted and unpermute on the host
+    std::vector<int> sorted(3 * (size_t)h->nf), orig(h->nf);
+    CK(cudaMemcpyAsync(sorted.data(), d_counts, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(orig.data(), h->f_orig[h->f_cur], sizeof(int) * h->nf, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int s = 0; s < h->nf; ++s)
+        for (int k = 0; k < 3; ++k) out[3 * orig[s] + k] = sorted[3 * s + k];
+    return FSIM_OK;
+}
+
+namespace {
+// fsim_get_cells of a neighbour-list instance: its particles lie in list-grid
+// order, so the impact-grid cells come from the per-step index (fluid, solid)
+// or from each wall's cell; the ids of a cell are listed in increasing input id.
+fsim_status get_cells_nl(fsim_sim *h, int species, int n, int *cell_start, int *ids)
+{
+    std::vector<int> cell(n), orig(n);
+    if (n) {
+        const int *c = species == 0 ? h->f_cell : species == 1 ? h->s_cell : h->v_icell;
+        const int *o = species == 0 ? h->f_orig[h->f_cur] : species == 1 ? h->s_orig[h->s_cur] : h->v_orig;
+        CK(cudaMemcpyAsync(cell.data(), c, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(orig.data(), o, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    std::vector<int> by_input(n);
+    for (int s = 0; s < n; ++s) by_input[orig[s]] = cell[s];
+    std::fill(cell_start, cell_start + h->ncell + 1, 0);
+    for (int i = 0; i < n; ++i) ++cell_start[by_input[i] + 1];
+    for (int c = 0; c < h->ncell; ++c) cell_start[c + 1] += cell_start[c];
+    std::vector<int> fill(cell_start, cell_start + h->ncell);
+    for (int i = 0; i < n; ++i) ids[fill[by_input[i]]++] = i;
+    return FSIM_OK;
+}
+} // namespace
+
+extern "C" fsim_status fsim_list_stats(fsim_handle h, int *enabled, int *builds, int *capacity, int *check)
+{
+    if (!h) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
+    int b = 0;
+    if (h->nl) {
+        DeviceGuard guard(h->device);
+        NlState st;
+        CK(cudaMemcpyAsync(&st, h->nl_state, sizeof st, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        b = st.builds;
+    }
+    if (enabled) *enabled = h->nl ? 1 : 0;
+    if (builds) *builds = b;
+    if (capacity) *capacity = h->nl ? h->nl_cap : 0;
+    if (check) *check = h->nl_check ? 1 : 0;
+    return FSIM_OK;
+}
+
+extern "C" fsim_status fsim_list_counts(fsim_handle h, int *out, size_t bytes)
+{
+    if (!h || (!out && bytes)) return FSIM_EINVAL;
+    if (h->batch) batch_wait(h);
+    if (!h->nl) {
+        fsim_set_error("the instance has no neighbour lists");
+        return FSIM_EINVAL;
+    }
+    if (bytes != (size_t)h->nf * 3 * 4) {
+        fsim_set_error("list counts need %zu bytes", (size_t)h->nf * 12);
+        return FSIM_EINVAL;
+    }
+    if (!h->f_sorted) {
+        fsim_set_error("run FSIM_PHASE_CELL first");
+        return FSIM_EINVAL;
+    }
+    if (!h->nf) return FSIM_OK;
+    DeviceGuard guard(h->device);
+    int *d_counts = (int *)h->staging; // 3 * nf words fit the staging buffer
+    launch_k_neighbor_counts_nl(blocks_for(h->nf, kBlock), h->stream, h->P, h->f_posr[h->f_cur], h->nl_list,
+                                h->nl_cnt, h->nl_cap, h->s_pos[h->s_cur], h->v_posr, d_counts, h->nf);
+    CK_LAUNCH();
     std::vector<int> sorted(3 * (size_t)h->nf), orig(h->nf);
     CK(cudaMemcpyAsync(sorted.data(), d_counts, bytes, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(orig.data(), h->f_orig[h->f_cur], sizeof(int) * h->nf, cudaMemcpyDeviceToHost, h->stream));
@@ -1577,6 +1936,7 @@ extern "C" fsim_status fsim_get_cells(fsim_handle h, int species, int *cell_star
         return FSIM_EINVAL;
     }
     DeviceGuard guard(h->device);
+    if (h->nl) return get_cells_nl(h, species, n, cell_start, ids);
     const int *start = species == 0 ? h->f_start : species == 1 ? h->s_start : h->v_start;
     const int *orig = species == 0 ? h->f_orig[h->f_cur] : species == 1 ? h->s_orig[h->s_cur] : h->v_orig;
     CK(cudaMemcpyAsync(cell_start, start, start_bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -1832,13 +2192,64 @@ struct SnapArray {
     void *dev;
     size_t bytes;
 };
+// A neighbour-list instance also saves what its lists were built from (the
+// positions and list-grid cells of the last build, the particles' order then)
+// and its list state; loading rebuilds the same lists from them.
 std::vector<SnapArray> snap_arrays(fsim_sim *h, int pf, int ps)
 {
     const size_t nf = h->nf, ns = h->ns, nv = h->nv, nc = h->ncell;
-    return {{h->f_posr[pf], 16 * nf}, {h->f_velp[pf], 16 * nf}, {h->f_orig[pf], 4 * nf},   {h->f_cell, 4 * nf},
-            {h->s_pos[ps], 16 * ns},  {h->s_vel[ps], 16 * ns},  {h->s_ref[ps], 16 * ns},   {h->s_type[ps], 4 * ns},
-            {h->s_orig[ps], 4 * ns},  {h->v_posr, 16 * nv},     {h->v_velp, 16 * nv},      {h->v_normal, 16 * nv},
-            {h->v_orig, 4 * nv},      {h->v_cell, 4 * nv},      {h->v_start, 4 * (nc + 1)}};
+    std::vector<SnapArray> a = {
+        {h->f_posr[pf], 16 * nf}, {h->f_velp[pf], 16 * nf}, {h->f_orig[pf], 4 * nf},   {h->f_cell, 4 * nf},
+        {h->s_pos[ps], 16 * ns},  {h->s_vel[ps], 16 * ns},  {h->s_ref[ps], 16 * ns},   {h->s_type[ps], 4 * ns},
+        {h->s_orig[ps], 4 * ns},  {h->v_posr, 16 * nv},     {h->v_velp, 16 * nv},      {h->v_normal, 16 * nv},
+        {h->v_orig, 4 * nv},      {h->v_cell, 4 * nv},      {h->v_start, 4 * (nc + 1)}};
+    if (h->nl) {
+        const size_t ncl = h->ncell_l;
+        const std::vector<SnapArray> b = {{h->f_x0, 16 * nf},           {h->f_lcell, 4 * nf},
+                                          {h->f_lstart, 4 * (ncl + 1)}, {h->s_x0, 16 * ns},
+                                          {h->s_lcell, 4 * ns},         {h->s_lstart, 4 * (ncl + 1)},
+                                          {h->s_inv, 4 * ns},           {h->nl_state, sizeof(NlState)}};
+        a.insert(a.end(), b.begin(), b.end());
+    }
+    return a;
+}
+
+// Build the lists from the saved build state (positions and cells of the last
+// build) without deciding or sorting, then restore the saved list state.
+fsim_status nl_restore(fsim_sim *h)
+{
+    NlState saved;
+    CK(cudaMemcpy(&saved, h->nl_state, sizeof saved, cudaMemcpyDeviceToHost));
+    NlState now = saved;
+    now.rebuild = 1;
+    CK(cudaMemcpy(h->nl_state, &now, sizeof now, cudaMemcpyHostToDevice));
+    if (h->nv) {
+        launch_k_cells_of(blocks_for(h->nv, kBlock), h->stream, h->P, h->v_posr, h->nv, h->v_icell, h->v_icxyz);
+        CK_LAUNCH();
+    }
+    Plan pl;
+    ArenaBuilder ab;
+    add_launch(pl, ab, L_NL_BUILD,
+               std::vector<Item<NlBuildArgs>>{{h->Pl, NlBuildArgs{h->f_x0, h->f_lcell, h->f_lstart, h->v_posr,
+                                                                  h->v_start, h->s_x0, h->s_lstart, h->nf, h->nl_cap,
+                                                                  h->nl_list, h->nl_cnt, h->nl_state, h->d_flags,
+                                                                  h->nl_R2s, h->nv, h->ns}}},
+               {blocks_for(h->nf, kNlBuildThreads)});
+    pl.host = ab.bytes;
+    CK(cudaMalloc((void **)&pl.arena, ab.bytes.size()));
+    cudaError_t e = cudaMemcpy(pl.arena, ab.bytes.data(), ab.bytes.size(), cudaMemcpyHostToDevice);
+    fsim_status st = FSIM_OK;
+    if (e == cudaSuccess) st = enqueue_plan(pl, h->stream, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(pl.arena);
+    pl.arena = nullptr;
+    if (e != cudaSuccess) {
+        fsim_set_error("rebuilding the neighbour lists failed: %s", cudaGetErrorString(e));
+        return FSIM_ECUDA;
+    }
+    if (st) return st;
+    CK(cudaMemcpy(h->nl_state, &saved, sizeof saved, cudaMemcpyHostToDevice));
+    return FSIM_OK;
 }
 size_t snap_payload(fsim_sim *h)
 {
@@ -1869,7 +2280,7 @@ extern "C" fsim_status fsim_snapshot_save(fsim_handle h, long long step, void *b
     SnapHeader hd;
     std::memset(&hd, 0, sizeof hd);
     std::memcpy(hd.magic, kSnapMagic, 8);
-    hd.version = 1;
+    hd.version = 2;
     hd.config_bytes = sizeof(fsim_config);
     hd.step = step;
     hd.n_fluid = h->nf;
@@ -1904,9 +2315,9 @@ extern "C" fsim_status fsim_snapshot_load(const void *buf, size_t bytes, int dev
         return FSIM_EIO;
     }
     std::memcpy(&hd, buf, sizeof hd);
-    if (std::memcmp(hd.magic, kSnapMagic, 8) || hd.version != 1 || hd.config_bytes != sizeof(fsim_config) ||
+    if (std::memcmp(hd.magic, kSnapMagic, 8) || hd.version != 2 || hd.config_bytes != sizeof(fsim_config) ||
         hd.n_fluid < 0 || hd.n_solid < 0 || hd.n_virt < 0) {
-        fsim_set_error("not a version-1 fluidsim snapshot");
+        fsim_set_error("not a version-2 fluidsim snapshot");
         return FSIM_EIO;
     }
     fsim_sim *h = nullptr;
@@ -1971,6 +2382,11 @@ extern "C" fsim_status fsim_snapshot_load(const void *buf, size_t bytes, int dev
             delete h;
             return st ? st : FSIM_ECUDA;
         }
+    }
+    if (h->nl && (st = nl_restore(h))) {
+        free_all(h);
+        delete h;
+        return st;
     }
     cudaStreamSynchronize(h->stream);
     h->f_cur = h->s_cur = 0;
@@ -2331,10 +2747,11 @@ extern "C" fsim_status fsim_batch_create(fsim_handle *members, int n, fsim_batch
             fsim_set_error("batch members must be distinct standalone handles on one device");
             return FSIM_EINVAL;
         }
-        if (members[k]->mixed != members[0]->mixed ||
+        if (members[k]->mixed != members[0]->mixed || members[k]->nl != members[0]->nl ||
             members[k]->cfg.solid_fused != members[0]->cfg.solid_fused ||
             members[k]->cfg.solid_full_walk != members[0]->cfg.solid_full_walk) {
-            fsim_set_error("batch members must share the precision form and the solid launch form");
+            fsim_set_error("batch members must share the precision form, the neighbour search (lists or cell "
+                           "walk) and the solid launch form");
             return FSIM_EINVAL;
         }
         for (int j = 0; j < k; ++j)
@@ -2407,10 +2824,11 @@ extern "C" fsim_status fsim_batch_add(fsim_batch_t b, fsim_handle h)
         fsim_set_error("a batch member must be a standalone handle on the batch's device");
         return FSIM_EINVAL;
     }
-    if (!b->members.empty() && (h->mixed != b->members[0]->mixed ||
+    if (!b->members.empty() && (h->mixed != b->members[0]->mixed || h->nl != b->members[0]->nl ||
                                 h->cfg.solid_fused != b->members[0]->cfg.solid_fused ||
                                 h->cfg.solid_full_walk != b->members[0]->cfg.solid_full_walk)) {
-        fsim_set_error("batch members must share the precision form and the solid launch form");
+        fsim_set_error("batch members must share the precision form, the neighbour search (lists or cell walk) "
+                       "and the solid launch form");
         return FSIM_EINVAL;
     }
     DeviceGuard guard(b->device);
@@ -2539,6 +2957,16 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
     b += nv * (3 * sizeof(float4) + 2 * sizeof(int));
     b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 3; // counts, starts
     if (cfg->precision == FSIM_PRECISION_MIXED) b += nc * sizeof(float2); // per-cell references
+    if (cfg->precision != FSIM_PRECISION_MIXED && cfg->neighbor_skin > 0.0f) {
+        // fluid neighbour lists (as setup_lists sizes them) and the list-grid
+        // sort, build state and per-step index (at most as many cells as nc)
+        const double rs = std::sqrt((double)d.impact_distance_square) * (1.0 + cfg->neighbor_skin) /
+                          (double)cfg->particle_diameter;
+        const size_t cap = (((size_t)std::ceil(1.5 * 4.18879 * rs * rs * rs) + 16 + 3) & ~size_t(3));
+        b += nf * (cap + 4) * sizeof(int) + nf * sizeof(float4);
+        b += ns * (sizeof(float4) + 2 * sizeof(int)) + nv * 2 * sizeof(int);
+        b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 2 + sizeof(NlState);
+    }
     b += 2 * kMaxScanTiles * sizeof(int) + sizeof(unsigned);
     size_t words = 3 * nf;
     if (9 * ns > words) words = 9 * ns;

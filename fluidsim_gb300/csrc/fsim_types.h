@@ -37,8 +37,20 @@ struct DevParams {
     float fl_build2, fl_move2;
 };
 
+// Per-instance state of the fluid neighbour lists, in device memory.  The
+// sweep and the list-decision kernel own it; the host only forces a rebuild
+// (after it changed positions) and reads the counters.
+struct NlState {
+    unsigned maxd2;   // largest squared displacement since the last build (float bits; >= 0)
+    int rebuild;      // this step rebuilds (set by the decision kernel at the start of the step)
+    int force;        // the next step rebuilds whatever the displacement
+    int builds;       // list builds so far
+    int overflow;     // particles whose list exceeded the capacity at the last build
+    int pad[3];
+};
+
 // per-instance error flags (device word, read by check_flags)
-enum : unsigned { FLAG_OUT_OF_GRID = 1u, FLAG_BARRIER_TIMEOUT = 2u, FLAG_CELL_OVERFULL = 4u };
+enum : unsigned { FLAG_OUT_OF_GRID = 1u, FLAG_BARRIER_TIMEOUT = 2u, FLAG_CELL_OVERFULL = 4u, FLAG_LIST_OVERFLOW = 8u };
 // A cell's particles are ordered by their previous sorted position with a scan
 // over the cell; cells above this count keep the scatter's order instead (the
 // scan's cost grows with the square of the count) and raise FLAG_CELL_OVERFULL.
@@ -63,16 +75,20 @@ struct Item {
 
 // ---- argument blocks of the batched kernels (one Item per instance)
 // cell phase: hash (plain / mixed), count reset, scans, scatter, gathers
+// `gate` (neighbour-list instances): when set, the kernel runs only in steps
+// whose *gate is non-zero (a list rebuild); the other steps skip it.
 struct HashArgs {
     const float4 *pos;
     int n;
     int *key, *slot, *cnt;
     unsigned *flags;
+    const int *gate;
 };
 
 struct ZeroArgs {
     int *p;
     int n;
+    const int *gate;
 };
 
 struct ScanArgs {
@@ -80,14 +96,18 @@ struct ScanArgs {
     int *out;
     int n;
     int *partial;
+    const int *gate;
 };
 
 struct ScatterArgs {
     const int *key, *slot, *start;
     int *tmp;
     int n;
+    const int *gate;
 };
 
+// With a gate, a step that does not rebuild copies the state unpermuted; a
+// step that does also records the new positions in x0_out.
 struct GatherFluidArgs {
     const int *tmp, *key, *start;
     int n;
@@ -96,6 +116,8 @@ struct GatherFluidArgs {
     float4 *posr_out, *velp_out;
     int *orig_out, *cell_out;
     unsigned *flags;
+    const int *gate;
+    float4 *x0_out;
 };
 
 struct GatherSolidArgs {
@@ -106,9 +128,52 @@ struct GatherSolidArgs {
     float4 *pos_out, *vel_out, *ref_out;
     int *type_out, *orig_out, *cell_out;
     int *inv_out;       // sorted position of every input id
-    unsigned *cxyz_out; // cell coordinates packed x | y << 11 | z << 21
+    unsigned *cxyz_out; // cell coordinates packed x | y << 11 | z << 21 (nullptr: not written)
+    unsigned *flags;
+    const int *gate;
+    float4 *x0_out;
+};
+
+// Neighbour-list instances: the per-step cell index over the (unmoved)
+// particles of the impact-distance grid.  ids[start[c] .. start[c+1]) are the
+// slots of cell c in increasing slot order; cell_out[slot] is the slot's cell
+// and (solid) cxyz_out[slot] its packed coordinates.
+struct RankArgs {
+    const int *tmp, *key, *start;
+    int n;
+    int *ids, *cell_out;
+    unsigned *cxyz_out;
     unsigned *flags;
 };
+
+// list decision: one block per instance
+struct NlDecideArgs {
+    NlState *nl;
+    const float4 *s_pos, *s_x0; // the solid's step-start positions and their values at the last build
+    int ns;
+    float move2; // squared displacement allowed since the build: ((Rs - R) / 2 - rounding slack)^2
+};
+
+// list build: every fluid particle's candidates within the list radius among
+// fluid, wall and solid particles of its 27 cells of the list grid (whose
+// cells are at least the list radius), in cell-row order; entry = index |
+// species << kNlSpeciesShift, entry-major (entry e of particle i at e * n + i)
+struct NlBuildArgs {
+    const float4 *posr;       // fluid positions at the build (sorted on the list grid)
+    const int *cell_f, *start_f;
+    const float4 *v_posr;
+    const int *start_v;
+    const float4 *s_pos;
+    const int *start_s;
+    int n, cap;
+    int *list, *cnt;
+    NlState *nl;
+    unsigned *flags;
+    float R2s; // list radius^2
+    int nv, ns;
+};
+constexpr int kNlSpeciesShift = 30; // list entry: index | species << 30 (0 fluid, 1 wall, 2 solid)
+constexpr int kNlIndexMask = (1 << kNlSpeciesShift) - 1;
 
 // fused fluid sweep + update (plain and mixed)
 struct FluidSweepArgs {
@@ -125,7 +190,22 @@ struct FluidSweepArgs {
     int n;
     int keep; // write drho/dt and du/dt
     const float2 *cm; // mixed form: per-cell (density deviation, pressure) references
+    // neighbour-list sweep: the lists, the positions of the last build and the
+    // instance's list state (largest displacement since the build)
+    const int *nl_list, *nl_cnt;
+    int nl_cap, nl_nv, nl_ns; // list capacity; wall and solid counts
+    const float4 *x0;
+    NlState *nl;
+    // where the impact grid's cells are too close to the impact distance for
+    // r < R to imply neighbouring cells under FP32 rounding: the packed
+    // impact-grid cell of every fluid, wall and solid slot (else nullptr), and
+    // a pair also needs neighbouring cells, as in the reference's cell walk
+    const unsigned *nl_cxyz_f, *nl_cxyz_v, *nl_cxyz_s;
 };
+
+// The cell walks below take `ids_*`: nullptr when the particles are sorted by
+// the walked grid (slot = position in the cell order), else the slots of the
+// per-step cell index (RankArgs) of a neighbour-list instance.
 
 // wall particles' data from their nearest fluid particle
 struct VirtArgs {
@@ -134,7 +214,8 @@ struct VirtArgs {
     const float4 *fposr, *fvelp;
     const int *forig, *start_f;
     float4 *v_posr, *v_velp;
-    int n;
+    int n, nf;
+    const int *ids_f;
 };
 
 // solid normal and Shepard pressure
@@ -144,7 +225,8 @@ struct CoupleArgs {
     const float4 *fposr, *fvelp;
     const int *start_f;
     float4 *s_np;
-    int n;
+    int n, nf;
+    const int *ids_f, *ids_s;
 };
 
 // mixed form: re-binning hash, per-cell references of the FP16 gather
@@ -168,14 +250,15 @@ struct CellRefArgs {
 struct SolidArgs {
     float4 *pos, *vel;
     const float4 *ref;
-    const int *type, *cell, *start_s;
+    const int *type, *cell;
+    const int *ids_f;      // per-step fluid cell index of a neighbour-list instance (else nullptr)
     const float4 *np;
     float *F, *Pk, *L, *AV; // 9 floats per particle, row-major
     float *PL;              // kPLStride floats per particle (9 used): three 16-byte loads per neighbour
     float4 *dudt, *couple;
     const float4 *fposr, *fvelp;
     const int *start_f;
-    int n;
+    int n, nf;             // solid and fluid particles
     // static reference-configuration neighbours (CSR over input ids)
     const int *orig, *inv, *nbr_off, *nbr_orig;
     const int *nbr_owner;  // input id of each entry's particle
@@ -203,7 +286,7 @@ struct ParamBlock {
 
 // the batched sweep's instances passed by value as one kernel parameter block
 // (at most 32,764 bytes of kernel parameters)
-constexpr int kSweepParamItems = 72;
+constexpr int kSweepParamItems = 64;
 struct SweepBatchParams {
     int n;
     int bstart[kSweepParamItems + 1];
@@ -306,6 +389,7 @@ struct ProbeArgs {
     const int *start_f;
     const float4 *s_pos, *s_vel, *s_np;
     const int *start_s;
+    const int *ids_f, *ids_s;
 };
 
 // grid barrier of the fused solid kernel
@@ -329,6 +413,12 @@ constexpr int kSweepShapes = 3;
 
 constexpr int kShapeWarps[kSweepShapes] = {4, 4, 8}; // warps per block of sweep shapes 0..2
 
+// L_SWEEP variants: 0-5 stream sweep (CHECK_Z * 3 + VISCID mode), 6-8 mixed
+// form (6 + VISCID mode), 9-11 list sweep (kSweepNlVariant + VISCID mode)
+constexpr int kSweepNlVariant = 9;
+// threads per block of the list build
+constexpr int kNlBuildThreads = 128;
+
 // ---------------------------------------------------------------- plans
 // A plan is the ordered list of batched launches that advance a set of
 // instances by one step (or one phase), with every launch's {params, args}
@@ -337,7 +427,8 @@ enum LaunchKind {
     L_ZERO, L_HASH, L_SCAN_REDUCE, L_SCAN_PARTIALS, L_SCAN_APPLY, L_SCATTER, L_GATHER_F, L_GATHER_S,
     L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE,
     L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M, L_SOLID_FUSED, L_SOLID_SLOTS,
-    L_FORCE_RECORD, L_FORCE_LISTED, L_DEFORM_R, L_DEFORM_M_R
+    L_FORCE_RECORD, L_FORCE_LISTED, L_DEFORM_R, L_DEFORM_M_R,
+    L_NL_DECIDE, L_NL_BUILD, L_RANK_F, L_RANK_S
 };
 
 struct Launch {
@@ -407,9 +498,13 @@ const Item<Args> &host_item(const Plan &pl, const Launch &L)
 // `shape`; optional events around the sweep (recorded with sweep_flags:
 // cudaEventRecordExternal makes them event nodes of a captured graph).
 // per_launch: 2 events per launch, recorded before and after it.
+// tune_ev (the autotuner): instead of one sweep, tune_rounds rounds of one
+// sweep per launch shape, round r shape s between tune_ev[2 (r S + s)] and
+// tune_ev[2 (r S + s) + 1] (S = kSweepShapes).
 fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape, cudaEvent_t sweep0 = nullptr,
                          cudaEvent_t sweep1 = nullptr, const cudaEvent_t *per_launch = nullptr,
-                         unsigned sweep_flags = cudaEventRecordDefault);
+                         unsigned sweep_flags = cudaEventRecordDefault, const cudaEvent_t *tune_ev = nullptr,
+                         int tune_rounds = 0);
 // the FSIM_PHASE_* a launch kind belongs to
 int launch_phase(int kind);
 // CTAs of the fused solid kernel that fit on the current device at once (<= want)
@@ -426,7 +521,10 @@ void launch_k_unpermute_words(int grid, cudaStream_t st, const int *src, const i
 void launch_k_permute_in_mixed(int grid, cudaStream_t st, const DevParams P, float4 *pos, float4 *velp, const int *cell, const int *orig, int n, int what, const float *in);
 void launch_k_permute_in_f4(int grid, cudaStream_t st, float4 *dst, const int *orig, int n, int comp, int width, const float *in);
 void launch_k_probe(int grid, cudaStream_t st, const DevParams P, const ProbeArgs A);
-void launch_k_neighbor_counts(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *cell_f, const int *start_f, const float4 *s_pos, const int *start_s, const float4 *v_posr, const int *start_v, int *out, int n);
+void launch_k_neighbor_counts(int grid, cudaStream_t st, const DevParams P, const DevParams Pv, const float4 *fposr, const int *cell_f, const int *start_f, const int *ids_f, const float4 *s_pos, const int *start_s, const int *ids_s, const float4 *v_posr, const int *start_v, int *out, int n);
+void launch_k_neighbor_counts_nl(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *list, const int *cnt, int cap, const float4 *s_pos, const float4 *v_posr, int *out, int n);
+void launch_k_nl_displacement(int grid, cudaStream_t st, const float4 *posr, const float4 *x0, int n, NlState *nl);
+void launch_k_cells_of(int grid, cudaStream_t st, const DevParams P, const float4 *pos, int n, int *out, unsigned *packed);
 void launch_k_conservation_fluid(int grid, cudaStream_t st, const DevParams P, const float4 *posr, const float4 *velp, const int *cell, int n, double vol, double *partials);
 void launch_k_conservation_solid(int grid, cudaStream_t st, const DevParams P, const float4 *pos, const float4 *vel, const float *F, int n, double rho_s, double vol, double *partials);
 void launch_k_case_generate(int grid, cudaStream_t st, const CaseGenArgs A);

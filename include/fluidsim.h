@@ -101,6 +101,13 @@ typedef struct fsim_config {
                                        2^22 (a quarter of a second and more).
                                        Small values exist to exercise the
                                        timeout path.                         */
+    float neighbor_skin;            /* > 0: the plain form advances the fluid
+                                       with per-particle neighbour lists of
+                                       radius R (1 + skin), R the impact
+                                       distance, rebuilt when a particle has
+                                       moved half the skin (default 0.1);
+                                       0: a cell walk every step.  Same pair
+                                       set either way.                       */
 } fsim_config;
 
 /* Derived constants, as Parameter::initiateParameter computes them in FP32
@@ -254,6 +261,18 @@ fsim_status fsim_set_fields(fsim_handle h, int n, const int *fields, const void 
  * and virtual particles within the impact distance among its 27 cells
  * (3*n_fluid ints), using the same FP32 distance test as the sweep. */
 fsim_status fsim_neighbor_counts(fsim_handle h, int *host_counts, size_t bytes);
+/* Fluid neighbour lists (no counterpart in the reference, which walks its
+ * cells every step; cfg.neighbor_skin): *enabled = 1 when the instance
+ * advances its fluid with lists, *builds = list builds so far, *capacity =
+ * entries a particle's list holds, *check = 1 when pairs also need
+ * neighbouring cells (cell sides within FP32 rounding of the impact
+ * distance).  Any pointer may be NULL. */
+fsim_status fsim_list_stats(fsim_handle h, int *enabled, int *builds, int *capacity, int *check);
+/* For every fluid particle (input order, 3 ints): the fluid, solid and
+ * virtual entries of its neighbour list within the impact distance of the
+ * current positions; equal to fsim_neighbor_counts while no list rebuild is
+ * due (after FSIM_PHASE_CELL).  FSIM_EINVAL without lists. */
+fsim_status fsim_list_counts(fsim_handle h, int *host_counts, size_t bytes);
 /* Cell structure of one species (0 fluid, 1 solid, 2 virtual): cell_start
  * (cell_number_total+1 ints) and the input ids in cell order (n ints). */
 fsim_status fsim_get_cells(fsim_handle h, int species, int *cell_start, size_t start_bytes,

@@ -41,6 +41,7 @@ typedef struct orc_config {
     int   solid_fused; /* device launch choice; no effect on the oracle */
     int   solid_full_walk; /* device launch choice; no effect on the oracle */
     int   barrier_wait_polls; /* device launch choice; no effect on the oracle */
+    float neighbor_skin; /* device search choice; no effect on the oracle */
 } orc_config;
 
 typedef struct orc_derived {

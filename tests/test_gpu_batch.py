@@ -45,7 +45,10 @@ def test_batch_members_equal_standalone(steps):
     with api.Batch(sims) as b:
         b.step(steps)
         b.sync()
-        assert b.launches_per_step() <= 14 + 3 * 6
+        # 20 launches outside the solid sub-steps: the neighbour-list decision,
+        # the list-grid sort (work only on a rebuild), the per-step cell index,
+        # the list build, coupling, walls and the sweep; 3 per solid sub-step
+        assert b.launches_per_step() <= 20 + 3 * 6
         batched = [_fields(s) for s in sims]
     for k, (a, c) in enumerate(zip(alone, batched)):
         for f in a:
@@ -146,7 +149,7 @@ def test_fused_solid_launch_matches_standalone_and_oracle_policy():
     with api.Batch(sims) as b:
         b.step(7)
         b.sync()
-        assert b.launches_per_step() <= 15  # the solid sub-steps are one launch
+        assert b.launches_per_step() <= 22  # the solid sub-steps are one launch (plus its slot pass)
         batched = [_fields(s) for s in sims]
     for k, (a, c) in enumerate(zip(alone, batched)):
         for f in a:

@@ -222,7 +222,7 @@ def test_time_sweep_graph_replays_equal_plain_steps():
     a = api.Simulation(cfg, pa, device=0)
     b = api.Simulation(cfg, pa, device=0)
     for s in (a, b):
-        s.step(4)  # the tuner's three steps and one graph replay
+        s.step(4)  # the tuner's step and three graph replays
     tot, sweep = a.time_sweep(5)
     tot2, sweep2 = a.time_sweep(3)  # the captured timed graphs are reused
     b.step(8)

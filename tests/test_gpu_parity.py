@@ -115,9 +115,10 @@ def test_one_step_graph_matches_phases(dam):
 
 
 def test_sweep_shapes_bit_identical(dam):
-    """The autotuner's first three steps run the three sweep launch shapes;
-    a handle stepped by phases keeps shape 0.  The states agree bit for bit,
-    and the tuner has picked one shape from three timed ones."""
+    """The autotuner's first step sweeps with each of the three launch shapes
+    (twice) in place of one sweep; a handle stepped by phases keeps shape 0.
+    The states agree bit for bit, and the tuner has picked one shape from
+    three timed ones."""
     cfg, pa = dam
     a = api.Simulation(cfg, pa, device=0)
     b = api.Simulation(cfg, pa, device=0)
