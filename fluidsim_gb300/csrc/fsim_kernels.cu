@@ -792,15 +792,38 @@ FSIM_BATCHED_KERNEL(kb_nl_decide, NlDecideArgs, nl_decide_body, kBlock)
 // the stream sweep sums them.
 constexpr int kNlBuildWarps = kNlBuildThreads / 32, kNlBuildCap = 32, kNlBuildChunk = 8;
 
-__device__ __forceinline__ void nl_flush(const NlBuildArgs &A, int (*lst)[32], int lane, int i, int &cnt, int &tot)
+// Append a lane's pending hits lst[0..cnt) to its list in whole groups of
+// kNlGroup entries (two 16-byte stores: a full sector); the remainder stays
+// pending at the front.  `tot` counts the entries stored so far; the final
+// flush stores the last partial group padded with -1 and makes `tot` exact.
+__device__ __forceinline__ void nl_flush(const NlBuildArgs &A, int (*lst)[32], int lane, int i, int &cnt, int &tot,
+                                         bool last)
 {
-    const int m = __reduce_max_sync(kFull, cnt);
-    for (int k = 0; k < m; ++k) {
-        const int e = tot + k;
-        if (k < cnt && e < A.cap) A.list[(size_t)e * A.n + i] = lst[k][lane];
+    const int full = last ? (cnt + kNlGroup - 1) / kNlGroup : cnt / kNlGroup;
+    const int mfull = __reduce_max_sync(kFull, full);
+    for (int g = 0; g < mfull; ++g) {
+        const int grp = tot / kNlGroup + g;
+        if (g < full && grp * kNlGroup < A.cap) {
+            int v[kNlGroup];
+#pragma unroll
+            for (int q = 0; q < kNlGroup; ++q) {
+                const int k = g * kNlGroup + q;
+                v[q] = k < cnt ? lst[k][lane] : -1;
+            }
+            int4 *dst = reinterpret_cast<int4 *>(A.list + ((size_t)grp * A.n + i) * kNlGroup);
+            dst[0] = make_int4(v[0], v[1], v[2], v[3]);
+            dst[1] = make_int4(v[4], v[5], v[6], v[7]);
+        }
     }
-    tot += cnt;
-    cnt = 0;
+    if (last) {
+        tot += cnt;
+        cnt = 0;
+        return;
+    }
+    const int rem = cnt - full * kNlGroup; // < kNlGroup; moves down from index >= kNlGroup (or stays put)
+    for (int q = 0; q < rem; ++q) lst[q][lane] = lst[full * kNlGroup + q][lane];
+    tot += full * kNlGroup;
+    cnt = rem;
 }
 
 template <int SP>
@@ -820,7 +843,8 @@ __device__ __forceinline__ void nl_gather(const DevParams &P, const NlBuildArgs 
             int j = start[base + z0];
             const int je = start[base + z1];
             while (j < je) {
-                if (__reduce_max_sync(kFull, cnt) > kNlBuildCap - kNlBuildChunk) nl_flush(A, lst, lane, i, cnt, tot);
+                if (__reduce_max_sync(kFull, cnt) > kNlBuildCap - kNlBuildChunk)
+                    nl_flush(A, lst, lane, i, cnt, tot, false);
                 const int jend = min(j + kNlBuildChunk, je);
 #pragma unroll 4
                 for (; j < jend; ++j) {
@@ -861,7 +885,7 @@ __device__ __forceinline__ void nl_build_body(const DevParams &P, const NlBuildA
         nl_gather<1>(P, A, lst, lane, i, cnt, tot, in, cx, cy, z0, z1, pr);
         nl_gather<2>(P, A, lst, lane, i, cnt, tot, in, cx, cy, z0, z1, pr);
     }
-    nl_flush(A, lst, lane, i, cnt, tot);
+    nl_flush(A, lst, lane, i, cnt, tot, true);
     if (valid) {
         A.cnt[i] = tot;
         if (tot > A.cap) {
@@ -882,31 +906,38 @@ __device__ __forceinline__ void fluid_sweep_nl_pairs(const DevParams &P, const F
                                                      float4 vp, PairAcc &acc)
 {
     const int m = min(A.nl_cnt[i], A.nl_cap);
-    const int *__restrict__ l = A.nl_list + i;
-    const size_t stride = (size_t)A.n;
+    const int4 *__restrict__ l = reinterpret_cast<const int4 *>(A.nl_list) + (size_t)i * (kNlGroup / 4);
+    const size_t stride = (size_t)A.n * (kNlGroup / 4); // int4 per group row
     const unsigned ci = CHECK ? A.nl_cxyz_f[i] : 0u;
-    for (int k = 0; k < m; ++k) {
-        const unsigned e = (unsigned)__ldg(l + (size_t)k * stride);
-        const int sp = (int)(e >> kNlSpeciesShift), j = (int)(e & kNlIndexMask);
-        FSIM_DCHECK(sp == 0 ? j < A.n : sp == 1 ? j < A.nl_nv : sp == 2 && j < A.nl_ns, 1u, continue);
-        if (sp == 2) {
-            const float4 q = A.s_pos[j];
-            const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
-            const float r2 = dist2(dx, dy, dz);
-            if (r2 < P.R2 && (!CHECK || cells_adjacent(ci, A.nl_cxyz_s[j]))) {
-                const float4 np = A.s_np[j], sv = A.s_vel[j];
-                const float k2 = 2.0f * ((vp.x - sv.x) * np.x + (vp.y - sv.y) * np.y + (vp.z - sv.z) * np.z);
-                riemann_pair<false, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, vp.x - k2 * np.x,
-                                            vp.y - k2 * np.y, vp.z - k2 * np.z, pr.w, np.w, false, acc);
-            }
-        } else {
-            const float4 q = sp ? A.v_posr[j] : A.posr[j];
-            const float dx = q.x - pr.x, dy = q.y - pr.y, dz = q.z - pr.z;
-            const float r2 = dist2(dx, dy, dz);
-            if (r2 < P.R2 && (!CHECK || cells_adjacent(ci, sp ? A.nl_cxyz_v[j] : A.nl_cxyz_f[j]))) {
-                const float4 u = sp ? A.v_velp[j] : A.velp[j];
-                riemann_pair<true, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q.w,
-                                           u.w, sp == 1, acc);
+    for (int k0 = 0; k0 < m; k0 += kNlGroup) {
+        // one group: a whole 32-byte sector of the lane's list
+        const int4 a = __ldg(l + (size_t)(k0 / kNlGroup) * stride), b = __ldg(l + (size_t)(k0 / kNlGroup) * stride + 1);
+        const int grp[kNlGroup] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int q = 0; q < kNlGroup; ++q) {
+            if (k0 + q >= m) break;
+            const unsigned e = (unsigned)grp[q];
+            const int sp = (int)(e >> kNlSpeciesShift), j = (int)(e & kNlIndexMask);
+            FSIM_DCHECK(sp == 0 ? j < A.n : sp == 1 ? j < A.nl_nv : sp == 2 && j < A.nl_ns, 1u, continue);
+            if (sp == 2) {
+                const float4 q4 = A.s_pos[j];
+                const float dx = q4.x - pr.x, dy = q4.y - pr.y, dz = q4.z - pr.z;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 < P.R2 && (!CHECK || cells_adjacent(ci, A.nl_cxyz_s[j]))) {
+                    const float4 np = A.s_np[j], sv = A.s_vel[j];
+                    const float k2 = 2.0f * ((vp.x - sv.x) * np.x + (vp.y - sv.y) * np.y + (vp.z - sv.z) * np.z);
+                    riemann_pair<false, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, vp.x - k2 * np.x,
+                                                vp.y - k2 * np.y, vp.z - k2 * np.z, pr.w, np.w, false, acc);
+                }
+            } else {
+                const float4 q4 = sp ? A.v_posr[j] : A.posr[j];
+                const float dx = q4.x - pr.x, dy = q4.y - pr.y, dz = q4.z - pr.z;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 < P.R2 && (!CHECK || cells_adjacent(ci, sp ? A.nl_cxyz_v[j] : A.nl_cxyz_f[j]))) {
+                    const float4 u = sp ? A.v_velp[j] : A.velp[j];
+                    riemann_pair<true, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q4.w,
+                                               u.w, sp == 1, acc);
+                }
             }
         }
     }
@@ -2244,7 +2275,7 @@ __global__ void k_neighbor_counts_nl(const DevParams P, const float4 *__restrict
     int c[3] = {0, 0, 0};
     const int m = min(cnt[i], cap);
     for (int k = 0; k < m; ++k) {
-        const unsigned e = (unsigned)list[(size_t)k * n + i];
+        const unsigned e = (unsigned)list[((size_t)(k / kNlGroup) * n + i) * kNlGroup + k % kNlGroup];
         const int sp = (int)(e >> kNlSpeciesShift), j = (int)(e & kNlIndexMask);
         const float4 q = sp == 0 ? fposr[j] : sp == 1 ? v_posr[j] : s_pos[j];
         if (dist2(q.x - p.x, q.y - p.y, q.z - p.z) < P.R2) ++c[sp == 0 ? 0 : sp == 2 ? 1 : 2];

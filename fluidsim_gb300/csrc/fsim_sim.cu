@@ -1284,7 +1284,7 @@ void setup_lists(fsim_sim *h)
     // list capacity: 1.5x a full sphere of radius Rs at the particle spacing
     const double dx = h->cfg.particle_diameter;
     const double full = 4.0 / 3.0 * 3.14159265358979 * std::pow(Rs / dx, 3.0);
-    h->nl_cap = ((int)std::ceil(1.5 * full) + 16 + 3) & ~3;
+    h->nl_cap = ((int)std::ceil(1.5 * full) + 16 + kNlGroup - 1) & ~(kNlGroup - 1); // whole groups
     h->nl = true;
 }
 
@@ -2962,7 +2962,7 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
         // sort, build state and per-step index (at most as many cells as nc)
         const double rs = std::sqrt((double)d.impact_distance_square) * (1.0 + cfg->neighbor_skin) /
                           (double)cfg->particle_diameter;
-        const size_t cap = (((size_t)std::ceil(1.5 * 4.18879 * rs * rs * rs) + 16 + 3) & ~size_t(3));
+        const size_t cap = (((size_t)std::ceil(1.5 * 4.18879 * rs * rs * rs) + 16 + kNlGroup - 1) & ~size_t(kNlGroup - 1));
         b += nf * (cap + 4) * sizeof(int) + nf * sizeof(float4);
         b += ns * (sizeof(float4) + 2 * sizeof(int)) + nv * 2 * sizeof(int);
         b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 2 + sizeof(NlState);

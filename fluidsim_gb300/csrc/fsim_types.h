@@ -157,7 +157,9 @@ struct NlDecideArgs {
 // list build: every fluid particle's candidates within the list radius among
 // fluid, wall and solid particles of its 27 cells of the list grid (whose
 // cells are at least the list radius), in cell-row order; entry = index |
-// species << kNlSpeciesShift, entry-major (entry e of particle i at e * n + i)
+// species << kNlSpeciesShift, in groups of kNlGroup: entry e of particle i at
+// ((e / kNlGroup) * n + i) * kNlGroup + e % kNlGroup, so that a lane writes and
+// reads a whole 32-byte sector per group and a warp's group is 1 KB contiguous
 struct NlBuildArgs {
     const float4 *posr;       // fluid positions at the build (sorted on the list grid)
     const int *cell_f, *start_f;
@@ -173,6 +175,7 @@ struct NlBuildArgs {
     int nv, ns;
 };
 constexpr int kNlSpeciesShift = 30; // list entry: index | species << 30 (0 fluid, 1 wall, 2 solid)
+constexpr int kNlGroup = 8;         // list entries per 32-byte group (the capacity is a multiple)
 constexpr int kNlIndexMask = (1 << kNlSpeciesShift) - 1;
 
 // fused fluid sweep + update (plain and mixed)
