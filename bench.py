@@ -631,8 +631,9 @@ def run_cpu_full(args):
 
 
 def run_profile(args):
-    """Fewest launches for an ncu capture: creation, then N graph-free steps
-    (the same kernels as the timed region).  --profile-form picks the plain
+    """Fewest launches for an ncu capture: creation, the autotuner's step
+    (the sweep once per launch shape and round), then N steps of the timed
+    region's graph.  --profile-form picks the plain
     4M case, the mixed form of the jittered 4M case, or the batched ensemble."""
     from fluidsim_gb300 import api, cases
 
@@ -651,6 +652,7 @@ def run_profile(args):
     else:
         cfg, pa = workload(args)
     sim = api.Simulation(cfg, pa, device=0)
+    sim.step(1)  # the autotuner's step: every sweep shape, then the fastest is kept
     tot, sweep = sim.time_sweep(args.profile_steps)
     sim.close()
     print(json.dumps({"profile_steps": args.profile_steps, "form": args.profile_form,

@@ -328,20 +328,29 @@ __device__ __forceinline__ void gather_fluid_body(const DevParams &, const Gathe
     if (A.gate && !*A.gate) {
         // neighbour-list step without a rebuild: the order stays, the state
         // moves to the other buffer unpermuted
-        A.posr_out[d] = A.posr_in[d];
-        A.velp_out[d] = A.velp_in[d];
+        const float4 p = A.posr_in[d], v = A.velp_in[d];
+        A.posr_out[d] = p;
+        A.velp_out[d] = v;
         A.orig_out[d] = A.orig_in[d];
+        if (A.rec_out) {
+            A.rec_out[2 * (size_t)d] = p;
+            A.rec_out[2 * (size_t)d + 1] = v;
+        }
         return;
     }
     int src, cell;
     const int dst = stable_dst(A.tmp, A.key, A.start, d, src, cell, A.flags, A.n);
     FSIM_DCHECK(dst >= 0 && dst < A.n && src >= 0 && src < A.n, 8u, return);
-    const float4 p = A.posr_in[src];
+    const float4 p = A.posr_in[src], v = A.velp_in[src];
     A.posr_out[dst] = p;
-    A.velp_out[dst] = A.velp_in[src];
+    A.velp_out[dst] = v;
     A.orig_out[dst] = A.orig_in[src];
     A.cell_out[dst] = cell;
     if (A.x0_out) A.x0_out[dst] = p;
+    if (A.rec_out) {
+        A.rec_out[2 * (size_t)dst] = p;
+        A.rec_out[2 * (size_t)dst + 1] = v;
+    }
 }
 FSIM_BATCHED_KERNEL(kb_gather_fluid, GatherFluidArgs, gather_fluid_body, kBlock)
 
@@ -901,6 +910,15 @@ FSIM_BATCHED_KERNEL(kb_nl_build, NlBuildArgs, nl_build_body, kNlBuildWarps * 32)
 // candidates, as the stream sweep sums them), then fluidUpdate
 // (src/fluid.cu:234-269) as in the stream sweep; the particle's squared
 // displacement since the build goes into the instance's running maximum.
+// One 32-byte (position, velocity) record with a single 256-bit load through
+// the read-only path (32-byte aligned: records start on 256-byte allocations).
+__device__ __forceinline__ void load_record(const float4 *p, float4 &a, float4 &b)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 template <int VISCID, bool CHECK>
 __device__ __forceinline__ void fluid_sweep_nl_pairs(const DevParams &P, const FluidSweepArgs &A, int i, float4 pr,
                                                      float4 vp, PairAcc &acc)
@@ -929,14 +947,23 @@ __device__ __forceinline__ void fluid_sweep_nl_pairs(const DevParams &P, const F
                     riemann_pair<false, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, vp.x - k2 * np.x,
                                                 vp.y - k2 * np.y, vp.z - k2 * np.z, pr.w, np.w, false, acc);
                 }
-            } else {
-                const float4 q4 = sp ? A.v_posr[j] : A.posr[j];
+            } else if (sp == 1) {
+                const float4 q4 = A.v_posr[j];
                 const float dx = q4.x - pr.x, dy = q4.y - pr.y, dz = q4.z - pr.z;
                 const float r2 = dist2(dx, dy, dz);
-                if (r2 < P.R2 && (!CHECK || cells_adjacent(ci, sp ? A.nl_cxyz_v[j] : A.nl_cxyz_f[j]))) {
-                    const float4 u = sp ? A.v_velp[j] : A.velp[j];
+                if (r2 < P.R2 && (!CHECK || cells_adjacent(ci, A.nl_cxyz_v[j]))) {
+                    const float4 u = A.v_velp[j];
                     riemann_pair<true, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q4.w,
-                                               u.w, sp == 1, acc);
+                                               u.w, true, acc);
+                }
+            } else {
+                float4 q4, u;
+                load_record(A.rec + 2 * (size_t)j, q4, u); // position and velocity: one sector
+                const float dx = q4.x - pr.x, dy = q4.y - pr.y, dz = q4.z - pr.z;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 < P.R2 && (!CHECK || cells_adjacent(ci, A.nl_cxyz_f[j]))) {
+                    riemann_pair<true, VISCID>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, pr.w, vp.w, u.x, u.y, u.z, q4.w,
+                                               u.w, false, acc);
                 }
             }
         }
@@ -967,9 +994,9 @@ template <int BS, int MINB>
 struct NlShape {
     static constexpr int threads = BS, min_blocks = MINB;
 };
-using NlShape0 = NlShape<128, 1>;
+using NlShape0 = NlShape<128, 16>; // at most 32 registers: 16 blocks (64 warps) per SM
 using NlShape1 = NlShape<128, 12>; // at most 40 registers: 12 blocks (48 warps) per SM
-using NlShape2 = NlShape<256, 1>;
+using NlShape2 = NlShape<256, 5>;  // at most 51 registers: 5 blocks (40 warps) per SM
 static_assert(kShapeWarps[0] * 32 == NlShape0::threads && kShapeWarps[1] * 32 == NlShape1::threads &&
                   kShapeWarps[2] * 32 == NlShape2::threads,
               "list-sweep shapes follow the block sizes of fsim_types.h");
@@ -2285,6 +2312,16 @@ __global__ void k_neighbor_counts_nl(const DevParams P, const float4 *__restrict
     out[3 * i + 2] = c[2];
 }
 
+// (posr, velp) records of every fluid slot (after fields were set from the host)
+__global__ void k_pack_records(const float4 *__restrict__ posr, const float4 *__restrict__ velp, int n,
+                               float4 *__restrict__ rec)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    rec[2 * (size_t)i] = posr[i];
+    rec[2 * (size_t)i + 1] = velp[i];
+}
+
 // Positions set from the host: fold their squared displacement since the last
 // list build into the instance's running maximum (the next step's decision).
 __global__ void k_nl_displacement(const float4 *__restrict__ posr, const float4 *__restrict__ x0, int n,
@@ -2807,6 +2844,11 @@ void launch_k_neighbor_counts(int grid, cudaStream_t st, const DevParams P, cons
 void launch_k_neighbor_counts_nl(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *list, const int *cnt, int cap, const float4 *s_pos, const float4 *v_posr, int *out, int n)
 {
     k_neighbor_counts_nl<<<grid, kBlock, 0, st>>>(P, fposr, list, cnt, cap, s_pos, v_posr, out, n);
+}
+
+void launch_k_pack_records(int grid, cudaStream_t st, const float4 *posr, const float4 *velp, int n, float4 *rec)
+{
+    k_pack_records<<<grid, kBlock, 0, st>>>(posr, velp, n, rec);
 }
 
 void launch_k_nl_displacement(int grid, cudaStream_t st, const float4 *posr, const float4 *x0, int n, NlState *nl)

@@ -109,6 +109,8 @@ struct fsim_sim {
     int *f_ids = nullptr, *f_lcell = nullptr, *f_lcnt = nullptr, *f_lstart = nullptr;
     int *s_ids = nullptr, *s_lcell = nullptr, *s_lcnt = nullptr, *s_lstart = nullptr;
     int *v_icell = nullptr;
+    float4 *f_rec = nullptr;      // (posr, velp) per slot, 32 bytes: the list sweep's neighbour records
+    bool rec_live = false;        // a cell phase wrote f_rec and the fluid phase has not run yet
     // misc
     int *scan_partials = nullptr; // 2 * kMaxScanTiles
     unsigned *d_flags = nullptr;
@@ -383,7 +385,7 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
         const int *gate = &h->nl_state->rebuild;
         const GatherFluidArgs fa{h->f_tmp, h->f_key, h->f_lstart, h->nf, h->f_posr[pf], h->f_velp[pf], h->f_orig[pf],
                                  h->f_posr[1 - pf], h->f_velp[1 - pf], h->f_orig[1 - pf], h->f_lcell, h->d_flags,
-                                 gate, h->f_x0};
+                                 gate, h->f_x0, h->f_rec};
         const Item<GatherFluidArgs> fi{h->Pl, fa};
         gf.push_back(fi);
         gfb.push_back(blocks_for(h->nf, kBlock));
@@ -604,6 +606,7 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         A.nl_cxyz_f = h->nl_check ? h->f_cxyz : nullptr;
         A.nl_cxyz_v = h->nl_check ? h->v_icxyz : nullptr;
         A.nl_cxyz_s = h->nl_check ? h->s_cxyz : nullptr;
+        A.rec = h->f_rec;
         it.push_back({h->P, A});
         for (int sh = 0; sh < kSweepShapes; ++sh) nb[sh].push_back(blocks_for(h->nf, kShapeWarps[sh] * 32));
         if (h->nf) {
@@ -829,6 +832,8 @@ void after_plan(fsim_sim *h, unsigned phases, const Plan &pl)
     }
     if ((phases & (1u << FSIM_PHASE_COUPLE)) && h->nf && h->ns) h->s_np_ok = true;
     if (phases & (1u << FSIM_PHASE_FLUID)) h->f_deriv_ok = h->keep && h->nf > 0;
+    if (phases & (1u << FSIM_PHASE_CELL)) h->rec_live = true;
+    if (phases & (1u << FSIM_PHASE_FLUID)) h->rec_live = false;
     if ((phases & (1u << FSIM_PHASE_SOLID)) && h->ns) h->s_mech_ok = true;
 }
 
@@ -1141,7 +1146,7 @@ fsim_status alloc_state(fsim_sim *h)
             (st = dalloc(h, &h->f_lcnt, ncl)) || (st = dalloc(h, &h->f_lstart, ncl + 1)) ||
             (st = dalloc(h, &h->s_ids, ns)) || (st = dalloc(h, &h->s_lcell, ns)) ||
             (st = dalloc(h, &h->s_lcnt, ncl)) || (st = dalloc(h, &h->s_lstart, ncl + 1)) ||
-            (st = dalloc(h, &h->v_icell, nv)))
+            (st = dalloc(h, &h->v_icell, nv)) || (st = dalloc(h, &h->f_rec, 2 * (size_t)nf)))
             return st;
         if (h->nl_check && ((st = dalloc(h, &h->f_cxyz, nf)) || (st = dalloc(h, &h->v_icxyz, nv)))) return st;
         NlState init{};
@@ -1648,6 +1653,10 @@ fsim_status enqueue_permute_in(fsim_sim *h, int field, int n, const float *stg)
     CK_LAUNCH();
     if (h->nl && field == FSIM_FLUID_POS) {
         launch_k_nl_displacement(blocks_for(n, kBlock), h->stream, dst, h->f_x0, n, h->nl_state);
+        CK_LAUNCH();
+    }
+    if (h->nl && field < 10 && h->rec_live) { // between the cell and fluid phases: records follow the state
+        launch_k_pack_records(blocks_for(n, kBlock), h->stream, h->f_posr[h->f_cur], h->f_velp[h->f_cur], n, h->f_rec);
         CK_LAUNCH();
     }
     return FSIM_OK;

@@ -118,6 +118,7 @@ struct GatherFluidArgs {
     unsigned *flags;
     const int *gate;
     float4 *x0_out;
+    float4 *rec_out; // neighbour-list instances: (posr, velp) of every slot side by side (32 bytes)
 };
 
 struct GatherSolidArgs {
@@ -204,6 +205,9 @@ struct FluidSweepArgs {
     // impact-grid cell of every fluid, wall and solid slot (else nullptr), and
     // a pair also needs neighbouring cells, as in the reference's cell walk
     const unsigned *nl_cxyz_f, *nl_cxyz_v, *nl_cxyz_s;
+    // the step-start (posr, velp) of every fluid slot side by side: one
+    // 32-byte sector per fluid neighbour, fetched with one 256-bit load
+    const float4 *rec;
 };
 
 // The cell walks below take `ids_*`: nullptr when the particles are sorted by
@@ -526,6 +530,7 @@ void launch_k_permute_in_f4(int grid, cudaStream_t st, float4 *dst, const int *o
 void launch_k_probe(int grid, cudaStream_t st, const DevParams P, const ProbeArgs A);
 void launch_k_neighbor_counts(int grid, cudaStream_t st, const DevParams P, const DevParams Pv, const float4 *fposr, const int *cell_f, const int *start_f, const int *ids_f, const float4 *s_pos, const int *start_s, const int *ids_s, const float4 *v_posr, const int *start_v, int *out, int n);
 void launch_k_neighbor_counts_nl(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *list, const int *cnt, int cap, const float4 *s_pos, const float4 *v_posr, int *out, int n);
+void launch_k_pack_records(int grid, cudaStream_t st, const float4 *posr, const float4 *velp, int n, float4 *rec);
 void launch_k_nl_displacement(int grid, cudaStream_t st, const float4 *posr, const float4 *x0, int n, NlState *nl);
 void launch_k_cells_of(int grid, cudaStream_t st, const DevParams P, const float4 *pos, int n, int *out, unsigned *packed);
 void launch_k_conservation_fluid(int grid, cudaStream_t st, const DevParams P, const float4 *posr, const float4 *velp, const int *cell, int n, double vol, double *partials);
