@@ -304,6 +304,7 @@ def run_gb300(args, dist):
     clocks = ClockSampler(dev)
     dist.barrier()
     sim.sync()
+    lists0 = sim.list_stats()
     clocks.start()
     t_wall = time.perf_counter()
     # the timed region: K replays of the step graph, whose event nodes around
@@ -311,6 +312,10 @@ def run_gb300(args, dist):
     ms, sweep_ms = sim.time_sweep(args.steps)
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
+    lists1 = sim.list_stats()
+    neighbor_lists = {"enabled": bool(lists1["enabled"]), "skin": cfg.neighbor_skin,
+                      "capacity": lists1["capacity"], "builds_in_timed_steps": lists1["builds"] - lists0["builds"],
+                      "cell_check": bool(lists1["check"])}
     dist.barrier()
     ms = dist.max(ms)
     sweep_ms = dist.max(sweep_ms)
@@ -426,6 +431,7 @@ def run_gb300(args, dist):
             "reference_build": ref_build,
             "clocks": clk,
             "forms": forms,
+            "neighbor_lists": neighbor_lists,
             "gpu_launches": launches * args.steps,
             "wall_s_timed": t_wall,
         }
@@ -579,17 +585,18 @@ def run_ensemble(dev, steps):
     }
 
 
-def run_served(dev):
+def run_served(dev, n=24):
     """The served workload, shortened in request count only: a seeded Poisson
     stream (20 requests/s) of ensemble-style dam-break scenarios (fluid 10k-1M
     log-uniform, solid 1k-27k, 200-2000 steps), served with continuous
     batching under a 150 GB budget, and the same stream
     served one request at a time.  Request data is generated before the clock
-    starts.  24 requests keep the run to tens of seconds; at 20 requests/s the
-    stream saturates the GPU, as the 2000-request stream does."""
+    starts.  The default 24 requests keep the run to tens of seconds; at 20
+    requests/s the stream saturates the GPU, as the 2000-request stream does.
+    `--served-requests N` runs the first N requests of the same stream alone."""
     from fluidsim_gb300 import serve
 
-    spec = dict(n=24, rate=20.0, seed=7, fluid_range=(10_000, 1_000_000), solid_range=(1_000, 27_000),
+    spec = dict(n=n, rate=20.0, seed=7, fluid_range=(10_000, 1_000_000), solid_range=(1_000, 27_000),
                 steps_range=(200, 2000))
     reqs = serve.pregenerate(serve.poisson_stream(**spec))
     batched = serve.Server(budget_bytes=150 * 10 ** 9, backend=serve.GpuBackend(dev), quantum=20,
@@ -672,11 +679,16 @@ def main():
     ap.add_argument("--profile-form", choices=("plain", "mixed", "ensemble"), default="plain")
     ap.add_argument("--cpu-full", action="store_true",
                     help="time the FP64 oracle on the small dam break (2000 steps) and the 4M case (200 steps)")
+    ap.add_argument("--served-requests", type=int, default=0,
+                    help="run only the served stream, with this many requests, and print its JSON")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling run for ncu: create the workload, run this many steps, print nothing else")
     args = ap.parse_args()
     if args.profile_steps:
         return run_profile(args)
+    if args.served_requests:
+        print(json.dumps({"served": run_served(0, args.served_requests)}), flush=True)
+        return 0
     if args.cpu_full:
         return run_cpu_full(args)
     if args.warmup < 3 and args.impl == "gb300":

@@ -245,7 +245,7 @@ extern "C" fsim_status fsim_config_defaults(fsim_config *c)
     c->impact_length_hsml_ratio = 3.0f;
     c->thread_num = 32;
     c->precision = FSIM_PRECISION_FP32;
-    c->neighbor_skin = 0.1f;
+    c->neighbor_skin = 0.15f;
     return FSIM_OK;
 }
 

@@ -105,7 +105,7 @@ typedef struct fsim_config {
                                        with per-particle neighbour lists of
                                        radius R (1 + skin), R the impact
                                        distance, rebuilt when a particle has
-                                       moved half the skin (default 0.1);
+                                       moved half the skin (default 0.15);
                                        0: a cell walk every step.  Same pair
                                        set either way.                       */
 } fsim_config;
