@@ -170,27 +170,39 @@ __device__ __forceinline__ int cell_slot(int *cnt, int c, bool active)
     return base + __popc(peers & ((1u << lane) - 1u));
 }
 
+// the element blocks an item's block `blk` covers: blk, blk + grid, ... (all of
+// them when the item is launched with one block per element block)
+#define FSIM_ELEMENT_BLOCKS(A, blk, b)                                                                     \
+    for (int b = (blk), nb_ = blocks_for((A).n, (int)blockDim.x), st_ = (A).grid ? (A).grid : nb_; b < nb_; \
+         b += st_)
+
 __device__ __forceinline__ void hash_body(const DevParams &P, const HashArgs &A, int blk)
 {
     if (A.gate && !*A.gate) return; // uniform per block
-    const int s = blk * blockDim.x + threadIdx.x;
-    const bool active = s < A.n;
-    int c = 0;
-    if (active) {
-        const float4 p = A.pos[s];
-        c = cell_index(P, p.x, p.y, p.z, A.flags);
-        A.key[s] = c;
+    FSIM_ELEMENT_BLOCKS(A, blk, b)
+    {
+        const int s = b * blockDim.x + threadIdx.x;
+        const bool active = s < A.n;
+        int c = 0;
+        if (active) {
+            const float4 p = A.pos[s];
+            c = cell_index(P, p.x, p.y, p.z, A.flags);
+            A.key[s] = c;
+        }
+        const int slot = cell_slot(A.cnt, c, active);
+        if (active) A.slot[s] = slot;
     }
-    const int slot = cell_slot(A.cnt, c, active);
-    if (active) A.slot[s] = slot;
 }
 FSIM_BATCHED_KERNEL(kb_hash, HashArgs, hash_body, kBlock)
 
 __device__ __forceinline__ void zero_body(const DevParams &, const ZeroArgs &A, int blk)
 {
     if (A.gate && !*A.gate) return;
-    const int s = blk * blockDim.x + threadIdx.x;
-    if (s < A.n) A.p[s] = 0;
+    FSIM_ELEMENT_BLOCKS(A, blk, b)
+    {
+        const int s = b * blockDim.x + threadIdx.x;
+        if (s < A.n) A.p[s] = 0;
+    }
 }
 FSIM_BATCHED_KERNEL(kb_zero, ZeroArgs, zero_body, kBlock)
 
@@ -285,10 +297,13 @@ FSIM_BATCHED_KERNEL(kb_scan_apply, ScanArgs, scan_apply_body, kScanThreads)
 __device__ __forceinline__ void scatter_body(const DevParams &, const ScatterArgs &A, int blk)
 {
     if (A.gate && !*A.gate) return;
-    const int s = blk * blockDim.x + threadIdx.x;
-    if (s >= A.n) return;
-    FSIM_DCHECK(A.start[A.key[s]] + A.slot[s] >= 0 && A.start[A.key[s]] + A.slot[s] < A.n, 8192u, return);
-    A.tmp[A.start[A.key[s]] + A.slot[s]] = s;
+    FSIM_ELEMENT_BLOCKS(A, blk, b)
+    {
+        const int s = b * blockDim.x + threadIdx.x;
+        if (s >= A.n) continue;
+        FSIM_DCHECK(A.start[A.key[s]] + A.slot[s] >= 0 && A.start[A.key[s]] + A.slot[s] < A.n, 8192u, continue);
+        A.tmp[A.start[A.key[s]] + A.slot[s]] = s;
+    }
 }
 FSIM_BATCHED_KERNEL(kb_scatter, ScatterArgs, scatter_body, kBlock)
 
@@ -767,11 +782,11 @@ __global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep_p(const __grid_
 // One block per instance at the start of every step: rebuild when forced or
 // when the largest displacement since the last build (fluid: accumulated by
 // the last sweep; solid: measured here) exceeds the allowance.
-__device__ __forceinline__ void nl_decide_body(const DevParams &, const NlDecideArgs &A, int)
+__device__ __forceinline__ void nl_decide_body(const DevParams &, const NlDecideArgs &A, int blk)
 {
     __shared__ unsigned wmax[kBlock / 32];
     unsigned m = 0;
-    for (int i = threadIdx.x; i < A.ns; i += blockDim.x) {
+    for (int i = blk * blockDim.x + threadIdx.x; i < A.ns; i += A.nblocks * blockDim.x) {
         const float4 p = A.s_pos[i], o = A.s_x0[i];
         m = max(m, __float_as_uint(dist2(p.x - o.x, p.y - o.y, p.z - o.z)));
     }
@@ -781,11 +796,17 @@ __device__ __forceinline__ void nl_decide_body(const DevParams &, const NlDecide
     if (threadIdx.x) return;
     for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, wmax[w]);
     NlState &S = *A.nl;
-    const float d2 = __uint_as_float(max(m, S.maxd2)); // NaN bits compare above every distance
+    if (m) atomicMax(&S.maxd2, m); // NaN bits compare above every distance
+    __threadfence();
+    if (atomicAdd(&S.ticket, 1u) != (unsigned)A.nblocks - 1u) return;
+    // the last block: every block's maximum (and the last sweep's) is in maxd2
+    __threadfence();
+    const float d2 = __uint_as_float(atomicMax(&S.maxd2, 0u));
     const int rb = S.force || !(d2 <= A.move2);
     S.rebuild = rb;
     S.force = 0;
     S.maxd2 = 0u; // this step's sweep accumulates afresh (against the new x0 if rebuilt)
+    S.ticket = 0u;
     if (rb) {
         S.builds += 1;
         S.overflow = 0;
@@ -867,9 +888,16 @@ __device__ __forceinline__ void nl_gather(const DevParams &P, const NlBuildArgs 
     }
 }
 
+__device__ __forceinline__ void nl_build_block(const DevParams &P, const NlBuildArgs &A, int blk);
+
 __device__ __forceinline__ void nl_build_body(const DevParams &P, const NlBuildArgs &A, int blk)
 {
     if (!A.nl->rebuild) return; // uniform per block
+    FSIM_ELEMENT_BLOCKS(A, blk, b) nl_build_block(P, A, b);
+}
+
+__device__ __forceinline__ void nl_build_block(const DevParams &P, const NlBuildArgs &A, int blk)
+{
     __shared__ int lists[kNlBuildWarps][kNlBuildCap][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = (blk * kNlBuildWarps + warp) * 32 + lane;

@@ -330,15 +330,21 @@ void add_sweep_launch(Plan &pl, ArenaBuilder &ab, const std::vector<Item<FluidSw
 // the list decision; on a rebuild, the counting sort of fluid and solid on the
 // list grid, else an unpermuted copy; the per-step impact-grid index; on a
 // rebuild, the list build.
+// Blocks a gated launch gets per instance at most (8 per SM of a GB300; the
+// list build, whose blocks carry uneven work, 32 per SM): each loops over its
+// element blocks when the step rebuilds and returns at once when it does not.
+constexpr int kGatedGrid = 8 * 152, kGatedBuildGrid = 32 * 152;
+
 void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
 {
     std::vector<Item<NlDecideArgs>> di;
     std::vector<int> db;
     for (fsim_sim *h : m) {
-        NlDecideArgs a{h->nl_state, h->s_pos[ps], h->s_x0, h->ns, h->nl_move2};
+        const int nb = std::min(64, std::max(1, blocks_for(h->ns, kBlock)));
+        NlDecideArgs a{h->nl_state, h->s_pos[ps], h->s_x0, h->ns, h->nl_move2, nb};
         Item<NlDecideArgs> it{h->P, a};
         di.push_back(it);
-        db.push_back(1);
+        db.push_back(nb);
     }
     add_launch(pl, ab, L_NL_DECIDE, di, db);
     // list-grid sort, run only when the decision says rebuild
@@ -352,24 +358,26 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
         for (int s_ = 0; s_ < 2; ++s_) {
             const int n = s_ ? h->ns : h->nf;
             int *lcnt = s_ ? h->s_lcnt : h->f_lcnt, *lstart = s_ ? h->s_lstart : h->f_lstart;
-            const Item<ZeroArgs> z{h->Pl, ZeroArgs{lcnt, n ? h->ncell_l : 0, gate}};
+            const int zn = n ? h->ncell_l : 0, zg = std::min(blocks_for(zn, kBlock), kGatedGrid);
+            const Item<ZeroArgs> z{h->Pl, ZeroArgs{lcnt, zn, gate, zg}};
             zi.push_back(z);
-            zb.push_back(blocks_for(z.A.n, kBlock));
-            const HashArgs ha = s_ ? HashArgs{h->s_pos[ps], h->ns, h->s_key, h->s_slot, lcnt, h->d_flags, gate}
-                                   : HashArgs{h->f_posr[pf], h->nf, h->f_key, h->f_slot, lcnt, h->d_flags, gate};
+            zb.push_back(zg);
+            const int hg = std::min(blocks_for(n, kBlock), kGatedGrid);
+            const HashArgs ha = s_ ? HashArgs{h->s_pos[ps], h->ns, h->s_key, h->s_slot, lcnt, h->d_flags, gate, hg}
+                                   : HashArgs{h->f_posr[pf], h->nf, h->f_key, h->f_slot, lcnt, h->d_flags, gate, hg};
             const Item<HashArgs> hh{h->Pl, ha};
             hi.push_back(hh);
-            hb.push_back(blocks_for(n, kBlock));
+            hb.push_back(hg);
             const Item<ScanArgs> sc{h->Pl,
                                     ScanArgs{lcnt, lstart, h->ncell_l, h->scan_partials + (s_ ? kMaxScanTiles : 0), gate}};
             si.push_back(sc);
             sb.push_back(n ? blocks_for(h->ncell_l, kScanTile) : 0);
             sp.push_back(n ? 1 : 0);
-            const ScatterArgs ca = s_ ? ScatterArgs{h->s_key, h->s_slot, lstart, h->s_tmp, h->ns, gate}
-                                      : ScatterArgs{h->f_key, h->f_slot, lstart, h->f_tmp, h->nf, gate};
+            const ScatterArgs ca = s_ ? ScatterArgs{h->s_key, h->s_slot, lstart, h->s_tmp, h->ns, gate, hg}
+                                      : ScatterArgs{h->f_key, h->f_slot, lstart, h->f_tmp, h->nf, gate, hg};
             const Item<ScatterArgs> cc{h->Pl, ca};
             ci.push_back(cc);
-            cb.push_back(blocks_for(n, kBlock));
+            cb.push_back(hg);
         }
     }
     add_launch(pl, ab, L_ZERO, zi, zb);
@@ -453,13 +461,14 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
     std::vector<Item<NlBuildArgs>> bi;
     std::vector<int> bb;
     for (fsim_sim *h : m) {
+        const int bg = std::min(blocks_for(h->nf, kNlBuildThreads), kGatedBuildGrid);
         const NlBuildArgs ba{h->f_x0,   h->f_lcell,  h->f_lstart, h->v_posr,  h->v_start,
                              h->s_x0,   h->s_lstart, h->nf,       h->nl_cap,  h->nl_list,
                              h->nl_cnt, h->nl_state, h->d_flags,  h->nl_R2s,  h->nv,
-                             h->ns};
+                             h->ns,     bg};
         const Item<NlBuildArgs> bt{h->Pl, ba};
         bi.push_back(bt);
-        bb.push_back(blocks_for(h->nf, kNlBuildThreads));
+        bb.push_back(bg);
     }
     add_launch(pl, ab, L_NL_BUILD, bi, bb);
 }

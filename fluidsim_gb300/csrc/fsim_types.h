@@ -46,7 +46,8 @@ struct NlState {
     int force;        // the next step rebuilds whatever the displacement
     int builds;       // list builds so far
     int overflow;     // particles whose list exceeded the capacity at the last build
-    int pad[3];
+    unsigned ticket;  // blocks of the decision kernel done this step
+    int pad[2];
 };
 
 // per-instance error flags (device word, read by check_flags)
@@ -76,19 +77,24 @@ struct Item {
 // ---- argument blocks of the batched kernels (one Item per instance)
 // cell phase: hash (plain / mixed), count reset, scans, scatter, gathers
 // `gate` (neighbour-list instances): when set, the kernel runs only in steps
-// whose *gate is non-zero (a list rebuild); the other steps skip it.
+// whose *gate is non-zero (a list rebuild); the other steps skip it.  `grid`
+// (0: one block per blockDim.x elements): the blocks launched for the item,
+// each looping over the element blocks -- a small grid, so that a gated launch
+// that has nothing to do costs little.
 struct HashArgs {
     const float4 *pos;
     int n;
     int *key, *slot, *cnt;
     unsigned *flags;
     const int *gate;
+    int grid;
 };
 
 struct ZeroArgs {
     int *p;
     int n;
     const int *gate;
+    int grid;
 };
 
 struct ScanArgs {
@@ -104,6 +110,7 @@ struct ScatterArgs {
     int *tmp;
     int n;
     const int *gate;
+    int grid;
 };
 
 // With a gate, a step that does not rebuild copies the state unpermuted; a
@@ -147,12 +154,14 @@ struct RankArgs {
     unsigned *flags;
 };
 
-// list decision: one block per instance
+// list decision: `nblocks` blocks per instance share the solid's displacement;
+// the last one to finish decides
 struct NlDecideArgs {
     NlState *nl;
     const float4 *s_pos, *s_x0; // the solid's step-start positions and their values at the last build
     int ns;
     float move2; // squared displacement allowed since the build: ((Rs - R) / 2 - rounding slack)^2
+    int nblocks;
 };
 
 // list build: every fluid particle's candidates within the list radius among
@@ -174,6 +183,7 @@ struct NlBuildArgs {
     unsigned *flags;
     float R2s; // list radius^2
     int nv, ns;
+    int grid;  // blocks launched (each loops over warps of particles; 0: one block per 4 warps)
 };
 constexpr int kNlSpeciesShift = 30; // list entry: index | species << 30 (0 fluid, 1 wall, 2 solid)
 constexpr int kNlGroup = 8;         // list entries per 32-byte group (the capacity is a multiple)
