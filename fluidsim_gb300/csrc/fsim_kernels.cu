@@ -841,8 +841,8 @@ __device__ __forceinline__ void nl_flush(const NlBuildArgs &A, int (*lst)[32], i
                 v[q] = k < cnt ? lst[k][lane] : -1;
             }
             int4 *dst = reinterpret_cast<int4 *>(A.list + ((size_t)grp * A.n + i) * kNlGroup);
-            dst[0] = make_int4(v[0], v[1], v[2], v[3]);
-            dst[1] = make_int4(v[4], v[5], v[6], v[7]);
+            __stcs(dst, make_int4(v[0], v[1], v[2], v[3])); // streaming: keep the positions in L2
+            __stcs(dst + 1, make_int4(v[4], v[5], v[6], v[7]));
         }
     }
     if (last) {
@@ -956,8 +956,10 @@ __device__ __forceinline__ void fluid_sweep_nl_pairs(const DevParams &P, const F
     const size_t stride = (size_t)A.n * (kNlGroup / 4); // int4 per group row
     const unsigned ci = CHECK ? A.nl_cxyz_f[i] : 0u;
     for (int k0 = 0; k0 < m; k0 += kNlGroup) {
-        // one group: a whole 32-byte sector of the lane's list
-        const int4 a = __ldg(l + (size_t)(k0 / kNlGroup) * stride), b = __ldg(l + (size_t)(k0 / kNlGroup) * stride + 1);
+        // one group: a whole 32-byte sector of the lane's list, read once per
+        // sweep, so loaded evict-first: the lists (1.6 GB at the 4M case) would
+        // otherwise push the neighbour records out of L1 and L2
+        const int4 a = __ldcs(l + (size_t)(k0 / kNlGroup) * stride), b = __ldcs(l + (size_t)(k0 / kNlGroup) * stride + 1);
         const int grp[kNlGroup] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 #pragma unroll
         for (int q = 0; q < kNlGroup; ++q) {
