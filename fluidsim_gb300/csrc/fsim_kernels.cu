@@ -347,6 +347,7 @@ __device__ __forceinline__ void gather_fluid_body(const DevParams &, const Gathe
         A.posr_out[d] = p;
         A.velp_out[d] = v;
         A.orig_out[d] = A.orig_in[d];
+        if (A.icell_out) A.icell_out[d] = A.icell_in[d];
         if (A.rec_out) {
             A.rec_out[2 * (size_t)d] = p;
             A.rec_out[2 * (size_t)d + 1] = v;
@@ -361,7 +362,8 @@ __device__ __forceinline__ void gather_fluid_body(const DevParams &, const Gathe
     A.velp_out[dst] = v;
     A.orig_out[dst] = A.orig_in[src];
     A.cell_out[dst] = cell;
-    if (A.x0_out) A.x0_out[dst] = p;
+    if (A.x0_out) A.x0_out[dst] = A.x0_in ? A.x0_in[src] : p;
+    if (A.icell_out) A.icell_out[dst] = A.icell_in[src];
     if (A.rec_out) {
         A.rec_out[2 * (size_t)dst] = p;
         A.rec_out[2 * (size_t)dst + 1] = v;
@@ -1308,31 +1310,56 @@ FSIM_BATCHED_KERNEL(kb_hash_mixed, HashMixedArgs, hash_mixed_body, kBlock)
 // water at dx = 5 mm, where an absolute FP16 pressure would be ~3 Pa.
 __device__ __forceinline__ void cell_ref_body(const DevParams &P, const CellRefArgs &A, int blk)
 {
-    // one warp per cell, one particle per lane (a cell holds ~18 at the
-    // benchmark spacing; larger cells loop in chunks of 32)
-    const int c = (blk * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (c >= A.ncell) return; // whole warp
-    const int b = A.start[c], e = A.start[c + 1];
-    if (b == e) return; // never read: no particle refers to an empty cell
+    // kCellRefLanes lanes per cell (a cell holds ~18 particles at the
+    // benchmark spacing, and most cells of the grid are empty), each summing
+    // every kCellRefLanes-th particle; then a butterfly over the lanes
+    const int t = blk * blockDim.x + threadIdx.x;
+    const int c = t / kCellRefLanes, sub = t % kCellRefLanes;
+    int b = 0, e = 0;
+    if (c < A.ncell) {
+        b = A.start[c];
+        e = A.start[c + 1];
+    }
     float sd = 0.0f, sp = 0.0f;
-    for (int j = b + lane; j < e; j += 32) {
-        const float d = A.velp[j].w;
+    for (int k = b + sub; k < e; k += kCellRefLanes) {
+        const float d = A.velp[A.ids ? A.ids[k] : k].w;
         sd += d;
         sp += eos_delta(P, d);
     }
-    sd = warp_sum(sd);
-    sp = warp_sum(sp);
+#pragma unroll
+    for (int o = kCellRefLanes / 2; o > 0; o >>= 1) {
+        sd += __shfl_xor_sync(kFull, sd, o);
+        sp += __shfl_xor_sync(kFull, sp, o);
+    }
+    if (b == e) return; // never read: no particle refers to an empty cell
     const float inv_n = 1.0f / (float)(e - b);
     const float dm = sd * inv_n, pm = sp * inv_n;
-    if (lane == 0) A.cm[c] = make_float2(dm, pm);
+    if (sub == 0) A.cm[c] = make_float2(dm, pm);
+    if (A.ids) return; // neighbour-list instances: kb_mixed_records, in slot order
     float *w = reinterpret_cast<float *>(A.posr);
-    for (int j = b + lane; j < e; j += 32) {
+    for (int j = b + sub; j < e; j += kCellRefLanes) {
         const float d = A.velp[j].w;
         w[4 * (size_t)j + 3] = __uint_as_float(half2_bits((d - dm) * kDeltaScale, (eos_delta(P, d) - pm) * P.p_unit_inv));
     }
 }
 FSIM_BATCHED_KERNEL(kb_cell_ref, CellRefArgs, cell_ref_body, kBlock)
+
+// Neighbour-list instances: every slot's FP16 gather pair against its cell's
+// references (the same expression as kb_cell_ref's), and its 32-byte record
+// for the list sweep (offset, FP16 pair | velocity, packed cell).
+__device__ __forceinline__ void mixed_records_body(const DevParams &P, const CellRefArgs &A, int blk)
+{
+    const int i = blk * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    const float4 v = A.velp[i];
+    float4 p = A.posr[i];
+    const float2 ref = A.cm[A.cell[i]];
+    p.w = __uint_as_float(half2_bits((v.w - ref.x) * kDeltaScale, (eos_delta(P, v.w) - ref.y) * P.p_unit_inv));
+    A.posr[i] = p;
+    A.rec[2 * (size_t)i] = p;
+    A.rec[2 * (size_t)i + 1] = make_float4(v.x, v.y, v.z, __uint_as_float(A.cxyz[i]));
+}
+FSIM_BATCHED_KERNEL(kb_mixed_records, CellRefArgs, mixed_records_body, kBlock)
 
 // Own particle of the mixed sweep.
 struct OwnMixed {
@@ -1340,6 +1367,25 @@ struct OwnMixed {
     int cbase;        // linear cell of code (0, 0, 0)
     float rho, p;
 };
+// The own offset (plus one cell, `ob`) shifted by `o` in {-1, 0, 1} cells:
+// what a pair subtracts from the offset of a neighbour in the cell `o` away.
+// Every mixed-form pair test and pair term rounds it this one way.
+__device__ __forceinline__ float shifted(float ob, int o, float cdx) { return fmaf(-(float)(o + 1), cdx, ob); }
+// Cell codes (o + 1 per axis, each in {0, 1, 2} for neighbouring cells) of a
+// pair from packed coordinates (x | y << 11 | z << 21): with cb = kCellBias -
+// c_i, the fields of c_j + cb are the codes when the cells are neighbours;
+// otherwise some field exceeds 2 (a field below -1 wraps to at least 3 in its
+// own bits, given fewer than 2^11, 2^10, 2^11 cells per axis, and any borrow
+// it passes up only shows where a field has already failed).
+constexpr unsigned kCellBias = 1u | (1u << 11) | (1u << 21);
+__device__ __forceinline__ bool cell_codes(unsigned cj, unsigned cb, int &bx, int &by, int &bz)
+{
+    const unsigned d = cj + cb;
+    bx = (int)(d & 0x7ffu);
+    by = (int)((d >> 11) & 0x3ffu);
+    bz = (int)(d >> 21);
+    return bx <= 2 && by <= 2 && bz <= 2;
+}
 
 template <int SP, int VISCID>
 __device__ __forceinline__ void flush_list_m(const DevParams &P, const FluidSweepArgs &A, int (*lst)[32], int lane,
@@ -1389,11 +1435,11 @@ __device__ __forceinline__ void gather_species_m(const DevParams &P, const Fluid
     for (int ox = -1; ox <= 1; ++ox) {
         const int x = cx + ox;
         if (x < 0 || x >= P.nx) continue;
-        const float psx = fmaf(-(float)ox, P.cdx[0], off.x);
+        const float psx = shifted(o.bx, ox, P.cdx[0]);
         for (int oy = -1; oy <= 1; ++oy) {
             const int y = cy + oy;
             if (y < 0 || y >= P.ny) continue;
-            const float psy = fmaf(-(float)oy, P.cdx[1], off.y);
+            const float psy = shifted(o.by, oy, P.cdx[1]);
             const int rb = (x * P.ny + y) * P.nz;
             const unsigned code_xy = (unsigned)(ox + 1) | ((unsigned)(oy + 1) << 2);
             int j = start[rb + z0];
@@ -1401,7 +1447,7 @@ __device__ __forceinline__ void gather_species_m(const DevParams &P, const Fluid
                 const int je = start[rb + z + 1];
                 const int dzc = z - cz;
                 const bool inz = in && dzc >= -1 && dzc <= 1;
-                const float psz = fmaf(-(float)dzc, P.cdx[2], off.z);
+                const float psz = shifted(o.bz, dzc, P.cdx[2]);
                 const unsigned code = (code_xy | ((unsigned)(dzc + 1) << 4)) << kCodeShift;
                 while (j < je) {
                     if (__reduce_max_sync(kFull, cnt) > SH::cap - SH::chunk)
@@ -1421,8 +1467,9 @@ __device__ __forceinline__ void gather_species_m(const DevParams &P, const Fluid
 }
 
 // fluidUpdate (src/fluid.cu:234-269) in the mixed form: delta and offsets.
-__device__ __forceinline__ void fluid_update_store_m(const DevParams &P, const FluidSweepArgs &A, int i, float4 off,
-                                                     float4 vp, float rho, const PairAcc &acc, int cx, int cy, int cz)
+__device__ __forceinline__ float4 fluid_update_store_m(const DevParams &P, const FluidSweepArgs &A, int i, float4 off,
+                                                       float4 vp, float rho, const PairAcc &acc, int cx, int cy,
+                                                       int cz)
 {
     // explicit roundings throughout (see riemann_pair's KAHAN branch)
     const float rho_inv = __fdividef(1.0f, rho);
@@ -1452,6 +1499,7 @@ __device__ __forceinline__ void fluid_update_store_m(const DevParams &P, const F
         A.drho_out[i] = drho;
         A.dudt_out[i] = make_float4(ax, ay, az, 0.0f);
     }
+    return make_float4(x, y, z, 0.0f);
 }
 
 template <int VISCID, class SH>
@@ -1514,6 +1562,176 @@ __global__ void __launch_bounds__(SH::warps * 32) kb_fluid_sweep_m1(const DevPar
     fluid_sweep_mixed_body<VISCID, SH>(P, A, (int)blockIdx.x);
 }
 
+// Absolute FP32 position of a mixed-form particle at offset `off` from the
+// corner of cell (cx, cy, cz) (the sweep's position of the fluid particle for
+// its solid pairs; the list build's positions).
+__device__ __forceinline__ float4 mixed_abs(const DevParams &P, float4 off, int cx, int cy, int cz, float w)
+{
+    return make_float4(__fadd_rn(fmaf((float)cx, P.cdx[0], P.cmin[0]), off.x),
+                       __fadd_rn(fmaf((float)cy, P.cdx[1], P.cmin[1]), off.y),
+                       __fadd_rn(fmaf((float)cz, P.cdx[2], P.cmin[2]), off.z), w);
+}
+__device__ __forceinline__ void unpack_cell(unsigned c, int &cx, int &cy, int &cz)
+{
+    cx = (int)(c & 0x7ffu);
+    cy = (int)((c >> 11) & 0x3ffu);
+    cz = (int)(c >> 21);
+}
+
+// Neighbour lists in the mixed form.  The particles keep the order of the last
+// list build between builds; each step re-bins every offset to the cell it now
+// lies in (in place), and the per-step cell index (kb_rank) gives every
+// particle's cell and packed cell coordinates.  A fluid neighbour's record
+// (32 bytes, written with the per-cell references) is
+//   (offset x y z, FP16 (delta, p) deviations | u v w, packed cell)
+// and a pair is taken exactly as the mixed cell walk takes it: the two cells
+// are neighbours, and r^2 < R^2 with the offset of i shifted by the cell
+// difference (`shifted`), so both sum bit-identical pair terms (in list order).
+template <int VISCID>
+__device__ __forceinline__ void fluid_sweep_nlm_pairs(const DevParams &P, const FluidSweepArgs &A, int i,
+                                                      const OwnMixed &o, float4 pa, float4 vp, unsigned ci,
+                                                      PairAcc &acc)
+{
+    const unsigned cb = kCellBias - ci;
+    const int m = min(A.nl_cnt[i], A.nl_cap);
+    const int4 *__restrict__ l = reinterpret_cast<const int4 *>(A.nl_list) + (size_t)i * (kNlGroup / 4);
+    const size_t stride = (size_t)A.n * (kNlGroup / 4);
+    const int nynz = P.ny * P.nz;
+    for (int k0 = 0; k0 < m; k0 += kNlGroup) {
+        const int4 a = __ldcs(l + (size_t)(k0 / kNlGroup) * stride), b = __ldcs(l + (size_t)(k0 / kNlGroup) * stride + 1);
+        const int grp[kNlGroup] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int q = 0; q < kNlGroup; ++q) {
+            if (k0 + q >= m) break;
+            const unsigned e = (unsigned)grp[q];
+            const int sp = (int)(e >> kNlSpeciesShift), j = (int)(e & kNlIndexMask);
+            FSIM_DCHECK(sp == 0 ? j < A.n : sp == 1 ? j < A.nl_nv : sp == 2 && j < A.nl_ns, 1u, continue);
+            if (sp == 2) {
+                const float4 q4 = A.s_pos[j];
+                const float dx = q4.x - pa.x, dy = q4.y - pa.y, dz = q4.z - pa.z;
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 < P.R2 && cells_adjacent(ci, A.nl_cxyz_s[j])) {
+                    const float4 np = A.s_np[j], sv = A.s_vel[j];
+                    const float k2 = __fmul_rn(2.0f, fmaf(__fsub_rn(vp.z, sv.z), np.z,
+                                                          fmaf(__fsub_rn(vp.y, sv.y), np.y,
+                                                               __fmul_rn(__fsub_rn(vp.x, sv.x), np.x))));
+                    riemann_pair<false, VISCID, true>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, o.rho, o.p,
+                                                      fmaf(-k2, np.x, vp.x), fmaf(-k2, np.y, vp.y),
+                                                      fmaf(-k2, np.z, vp.z), o.rho, np.w, false, acc);
+                }
+                continue;
+            }
+            float4 q4, u;
+            unsigned cj;
+            if (sp == 1) {
+                q4 = A.v_posr[j];
+                u = A.v_velp[j];
+                cj = A.nl_cxyz_v[j];
+            } else {
+                load_record(A.rec + 2 * (size_t)j, q4, u);
+                cj = __float_as_uint(u.w);
+            }
+            int bx, by, bz;
+            if (!cell_codes(cj, cb, bx, by, bz)) continue;
+            // = shifted(o.b*, b* - 1, cdx)
+            const float dx = q4.x - fmaf(-(float)bx, P.cdx[0], o.bx);
+            const float dy = q4.y - fmaf(-(float)by, P.cdx[1], o.by);
+            const float dz = q4.z - fmaf(-(float)bz, P.cdx[2], o.bz);
+            const float r2 = dist2(dx, dy, dz);
+            if (!(r2 < P.R2)) continue;
+            float rhoj, pj;
+            if (sp == 0) {
+                const float2 ref = A.cm[o.cbase + bx * nynz + by * P.nz + bz];
+                const float2 dev = half2_floats(q4.w);
+                rhoj = fmaf(P.rho0, fmaf(dev.x, kDeltaUnit, ref.x), P.rho0);
+                pj = fmaf(dev.y, P.p_unit, ref.y);
+            } else {
+                rhoj = q4.w;
+                pj = u.w;
+            }
+            riemann_pair<true, VISCID, true>(P, dx, dy, dz, r2, vp.x, vp.y, vp.z, o.rho, o.p, u.x, u.y, u.z, rhoj, pj,
+                                             sp == 1, acc);
+        }
+    }
+}
+
+template <int VISCID>
+__device__ __forceinline__ void fluid_sweep_nlm_body(const DevParams &P, const FluidSweepArgs &A, int blk)
+{
+    const int i = blk * blockDim.x + threadIdx.x;
+    const bool valid = i < A.n;
+    unsigned d2bits = 0u;
+    if (valid) {
+        const float4 off = A.posr[i], vp = A.velp[i];
+        const unsigned ci = A.nl_cxyz_f[i];
+        int cx, cy, cz;
+        unpack_cell(ci, cx, cy, cz);
+        OwnMixed o;
+        o.bx = __fadd_rn(off.x, P.cdx[0]);
+        o.by = __fadd_rn(off.y, P.cdx[1]);
+        o.bz = __fadd_rn(off.z, P.cdx[2]);
+        o.cbase = A.cell_f[i] - P.ny * P.nz - P.nz - 1;
+        o.rho = fmaf(P.rho0, vp.w, P.rho0);
+        o.p = eos_delta(P, vp.w);
+        const float4 pa = mixed_abs(P, off, cx, cy, cz, o.rho);
+        PairAcc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        fluid_sweep_nlm_pairs<VISCID>(P, A, i, o, pa, vp, ci, acc);
+        const float4 x = mixed_abs(P, fluid_update_store_m(P, A, i, off, vp, o.rho, acc, cx, cy, cz), cx, cy, cz,
+                                   0.0f);
+        const float4 x0 = A.x0[i];
+        d2bits = __float_as_uint(dist2(x.x - x0.x, x.y - x0.y, x.z - x0.z));
+    }
+    const unsigned wmax = __reduce_max_sync(kFull, d2bits);
+    if ((threadIdx.x & 31) == 0 && wmax) atomicMax(&A.nl->maxd2, wmax);
+}
+
+// launch shapes of the mixed list sweep (more registers than the plain one)
+using NlmShape0 = NlShape<128, 8>;  // at most 64 registers
+using NlmShape1 = NlShape<128, 10>; // at most 48 registers (a few spills)
+using NlmShape2 = NlShape<256, 3>;  // at most 85 registers
+static_assert(NlmShape0::threads == NlShape0::threads && NlmShape1::threads == NlShape1::threads &&
+                  NlmShape2::threads == NlShape2::threads,
+              "mixed list-sweep shapes use the block sizes of the plain ones");
+
+template <int VISCID, class SH>
+__global__ void __launch_bounds__(SH::threads, SH::min_blocks) kb_fluid_sweep_nlm_1(const DevParams P,
+                                                                                    const FluidSweepArgs A)
+{
+    fluid_sweep_nlm_body<VISCID>(P, A, (int)blockIdx.x);
+}
+template <int VISCID, class SH>
+__global__ void __launch_bounds__(SH::threads, SH::min_blocks)
+    kb_fluid_sweep_nlm(const Item<FluidSweepArgs> *__restrict__ items, const int *__restrict__ bstart, int ninst)
+{
+    const int inst = locate_instance(bstart, ninst, blockIdx.x);
+    fluid_sweep_nlm_body<VISCID>(items[inst].P, items[inst].A, (int)blockIdx.x - bstart[inst]);
+}
+template <int VISCID, class SH>
+__global__ void __launch_bounds__(SH::threads, SH::min_blocks)
+    kb_fluid_sweep_nlm_p(const __grid_constant__ SweepBatchParams B)
+{
+    const int inst = locate_instance(B.bstart, B.n, blockIdx.x);
+    const Item<FluidSweepArgs> &it = B.it[inst];
+    fluid_sweep_nlm_body<VISCID>(it.P, it.A, (int)blockIdx.x - B.bstart[inst]);
+}
+
+// Neighbour-list instances in the mixed form, on a rebuild: every particle's
+// absolute position from its cell and offset (the list grid's sort key and, in
+// the new order, the positions of the build).
+__device__ __forceinline__ void mixed_abs_body(const DevParams &P, const MixedAbsArgs &A, int blk)
+{
+    if (A.gate && !*A.gate) return; // uniform per block
+    FSIM_ELEMENT_BLOCKS(A, blk, b)
+    {
+        const int s = b * blockDim.x + threadIdx.x;
+        if (s >= A.n) continue;
+        int cx, cy, cz;
+        cell_xyz(P, A.cell[s], cx, cy, cz);
+        A.out[s] = mixed_abs(P, A.posr[s], cx, cy, cz, 0.0f);
+    }
+}
+FSIM_BATCHED_KERNEL(kb_mixed_abs, MixedAbsArgs, mixed_abs_body, kBlock)
+
 // getVirtData (src/virt.cu:9-75) in the mixed form.
 __device__ __forceinline__ void virt_mixed_body(const DevParams &P, const VirtArgs &A, int blk)
 {
@@ -1537,7 +1755,9 @@ __device__ __forceinline__ void virt_mixed_body(const DevParams &P, const VirtAr
             const int rb = (x * P.ny + y) * P.nz;
             for (int z = z0; z < z1; ++z) {
                 const float psz = fmaf(-(float)(z - cz), P.cdx[2], xi.z);
-                for (int j = A.start_f[rb + z], je = A.start_f[rb + z + 1]; j < je; ++j) {
+                for (int t = A.start_f[rb + z], te = A.start_f[rb + z + 1]; t < te; ++t) {
+                    const int j = A.ids_f ? A.ids_f[t] : t;
+                    FSIM_DCHECK(j >= 0 && j < A.nf, 32u, continue);
                     const float4 q = A.fposr[j];
                     const float d2 = dist2(q.x - psx, q.y - psy, q.z - psz);
                     bool take = d2 < best;
@@ -1577,10 +1797,10 @@ struct RowMixed {
     int b1, b2, z0;  // start of the row's 2nd and 3rd cell, first cell
     float sx, sy;    // solid offset minus the row's x/y cell shift
 };
-__device__ __forceinline__ void fluid_rel(const DevParams &P, const RowMixed &R, int j, float sz0, float4 q, float &dx,
+__device__ __forceinline__ void fluid_rel(const DevParams &P, const RowMixed &R, int t, float sz0, float4 q, float &dx,
                                           float &dy, float &dz)
 {
-    const int k = (j >= R.b1) + (j >= R.b2);
+    const int k = (t >= R.b1) + (t >= R.b2);
     dx = q.x - R.sx;
     dy = q.y - R.sy;
     dz = q.z - fmaf(-(float)k, P.cdx[2], sz0);
@@ -1588,10 +1808,13 @@ __device__ __forceinline__ void fluid_rel(const DevParams &P, const RowMixed &R,
 
 // The mixed-form row walk of a solid particle: calls f(j, q, dx, dy, dz) for
 // every fluid candidate of the 27 cells of solid cell `cell`, lanes of a group
-// of `G` taking every G-th candidate of a row.
+// of `G` taking every G-th candidate of a row.  `ids`: the per-step cell index
+// of a neighbour-list instance (slot t of the walk is particle ids[t]), else
+// nullptr (slot = particle).
 template <int G, class F>
 __device__ __forceinline__ void solid_fluid_walk_m(const DevParams &P, const int *__restrict__ start_f,
-                                                   const float4 *__restrict__ fposr, int cell, float4 xi, int g, F &&f)
+                                                   const int *__restrict__ ids, const float4 *__restrict__ fposr,
+                                                   int cell, float4 xi, int g, F &&f)
 {
     int cx, cy, cz;
     cell_xyz(P, cell, cx, cy, cz);
@@ -1613,10 +1836,11 @@ __device__ __forceinline__ void solid_fluid_walk_m(const DevParams &P, const int
             R.b2 = start_f[rb + min(z0 + 2, z1)];
             R.sx = fmaf(-(float)ox, P.cdx[0], sox);
             R.sy = fmaf(-(float)oy, P.cdx[1], soy);
-            for (int j = start_f[rb + z0] + g, je = start_f[rb + z1]; j < je; j += G) {
+            for (int t = start_f[rb + z0] + g, te = start_f[rb + z1]; t < te; t += G) {
+                const int j = ids ? ids[t] : t;
                 const float4 q = fposr[j];
                 float dx, dy, dz;
-                fluid_rel(P, R, j, sz0, q, dx, dy, dz);
+                fluid_rel(P, R, t, sz0, q, dx, dy, dz);
                 f(j, dx, dy, dz);
             }
         }
@@ -1632,7 +1856,7 @@ __device__ __forceinline__ void couple_mixed_body(const DevParams &P, const Coup
     float nx = 0.0f, ny = 0.0f, nz = 0.0f, psum = 0.0f, wsum = 0.0f;
     if (valid) {
         const float4 xi = A.s_pos[i];
-        solid_fluid_walk_m<kSolidGroup>(P, A.start_f, A.fposr, A.s_cell[i], xi, g,
+        solid_fluid_walk_m<kSolidGroup>(P, A.start_f, A.ids_f, A.fposr, A.s_cell[i], xi, g,
                                         [&](int j, float dx, float dy, float dz) {
                                             const float r2 = dist2(dx, dy, dz);
                                             if (r2 < P.R2) {
@@ -1645,8 +1869,8 @@ __device__ __forceinline__ void couple_mixed_body(const DevParams &P, const Coup
         neighbor_rows(P, A.s_cell[i], rows);
         for (int r = 0; r < rows.count; ++r) {
             const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-            for (int j = A.start_s[c0] + g, je = A.start_s[c1]; j < je; j += kSolidGroup) {
-                const float4 q = A.s_pos[j];
+            for (int ts = A.start_s[c0] + g, te = A.start_s[c1]; ts < te; ts += kSolidGroup) {
+                const float4 q = A.s_pos[A.ids_s ? A.ids_s[ts] : ts];
                 const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
                 const float r2 = dist2(dx, dy, dz);
                 if (r2 < P.R2) {
@@ -1900,7 +2124,7 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
             cz = fmaf(f, dz, cz);
         };
         if (MIXED) {
-            solid_fluid_walk_m<kSolidGroup>(P, S.start_f, S.fposr, S.cell[i], xi, g,
+            solid_fluid_walk_m<kSolidGroup>(P, S.start_f, S.ids_f, S.fposr, S.cell[i], xi, g,
                                             [&](int j, float dx, float dy, float dz) {
                                                 const float r2 = dist2(dx, dy, dz);
                                                 if (r2 < P.R2) {
@@ -2144,7 +2368,7 @@ __global__ void k_probe(const DevParams P, const ProbeArgs A)
             }
         };
         if (P.mixed) {
-            solid_fluid_walk_m<32>(P, A.start_f, A.fposr, cell, xi, lane, fluid);
+            solid_fluid_walk_m<32>(P, A.start_f, A.ids_f, A.fposr, cell, xi, lane, fluid);
         }
         Rows rows;
         neighbor_rows(P, cell, rows);
@@ -2342,25 +2566,141 @@ __global__ void k_neighbor_counts_nl(const DevParams P, const float4 *__restrict
     out[3 * i + 2] = c[2];
 }
 
-// (posr, velp) records of every fluid slot (after fields were set from the host)
-__global__ void k_pack_records(const float4 *__restrict__ posr, const float4 *__restrict__ velp, int n,
-                               float4 *__restrict__ rec)
+// The counts in the mixed form: pairs as the mixed sweep's cell walk takes
+// them (fluid and wall candidates of the 27 cells, r^2 < R^2 with the
+// particle's offset shifted by the cell difference; solid candidates of the 27
+// cells within R of the absolute position).  Walls lie on the walked grid
+// (v_cxyz == nullptr, offsets from the walked cell) or, in a neighbour-list
+// instance, on the list grid Pv with their impact-grid cells in v_cxyz.
+__global__ void k_neighbor_counts_mixed(const DevParams P, const DevParams Pv, const float4 *__restrict__ fposr,
+                                        const int *__restrict__ cell_f, const int *__restrict__ start_f,
+                                        const int *__restrict__ ids_f, const float4 *__restrict__ s_pos,
+                                        const int *__restrict__ start_s, const int *__restrict__ ids_s,
+                                        const float4 *__restrict__ v_posr, const int *__restrict__ start_v,
+                                        const unsigned *__restrict__ v_cxyz, int *__restrict__ out, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const float4 off = fposr[i];
+    int cx, cy, cz;
+    cell_xyz(P, cell_f[i], cx, cy, cz);
+    const float4 pa = mixed_abs(P, off, cx, cy, cz, 0.0f);
+    const float obx = __fadd_rn(off.x, P.cdx[0]), oby = __fadd_rn(off.y, P.cdx[1]), obz = __fadd_rn(off.z, P.cdx[2]);
+    int cf = 0, cs = 0, cv = 0;
+    for (int ox = -1; ox <= 1; ++ox)
+        for (int oy = -1; oy <= 1; ++oy)
+            for (int oz = -1; oz <= 1; ++oz) {
+                const int x = cx + ox, y = cy + oy, z = cz + oz;
+                if (x < 0 || x >= P.nx || y < 0 || y >= P.ny || z < 0 || z >= P.nz) continue;
+                const int c = (x * P.ny + y) * P.nz + z;
+                const float psx = shifted(obx, ox, P.cdx[0]), psy = shifted(oby, oy, P.cdx[1]),
+                            psz = shifted(obz, oz, P.cdx[2]);
+                for (int t = start_f[c]; t < start_f[c + 1]; ++t) {
+                    const float4 q = fposr[ids_f ? ids_f[t] : t];
+                    cf += dist2(q.x - psx, q.y - psy, q.z - psz) < P.R2;
+                }
+                for (int t = start_s[c]; t < start_s[c + 1]; ++t) {
+                    const float4 q = s_pos[ids_s ? ids_s[t] : t];
+                    cs += dist2(q.x - pa.x, q.y - pa.y, q.z - pa.z) < P.R2;
+                }
+                if (!v_cxyz)
+                    for (int j = start_v[c]; j < start_v[c + 1]; ++j) {
+                        const float4 q = v_posr[j];
+                        cv += dist2(q.x - psx, q.y - psy, q.z - psz) < P.R2;
+                    }
+            }
+    if (v_cxyz) {
+        Rows vrows;
+        neighbor_rows(Pv, cell_index(Pv, pa.x, pa.y, pa.z, nullptr), vrows);
+        for (int r = 0; r < vrows.count; ++r) {
+            const int c0 = vrows.base[r] + vrows.z0, c1 = vrows.base[r] + vrows.z1;
+            for (int j = start_v[c0]; j < start_v[c1]; ++j) {
+                int jx, jy, jz;
+                unpack_cell(v_cxyz[j], jx, jy, jz);
+                const int ox = jx - cx, oy = jy - cy, oz = jz - cz;
+                if (abs(ox) > 1 || abs(oy) > 1 || abs(oz) > 1) continue;
+                const float4 q = v_posr[j];
+                cv += dist2(q.x - shifted(obx, ox, P.cdx[0]), q.y - shifted(oby, oy, P.cdx[1]),
+                            q.z - shifted(obz, oz, P.cdx[2])) < P.R2;
+            }
+        }
+    }
+    out[3 * i] = cf;
+    out[3 * i + 1] = cs;
+    out[3 * i + 2] = cv;
+}
+
+// The same counts of a mixed-form neighbour-list instance from its lists,
+// with the list sweep's pair rule.
+__global__ void k_neighbor_counts_nlm(const DevParams P, const float4 *__restrict__ fposr,
+                                      const int *__restrict__ cell_f, const unsigned *__restrict__ cxyz_f,
+                                      const int *__restrict__ list, const int *__restrict__ cnt, int cap,
+                                      const float4 *__restrict__ s_pos, const unsigned *__restrict__ cxyz_s,
+                                      const float4 *__restrict__ v_posr, const unsigned *__restrict__ cxyz_v,
+                                      int *__restrict__ out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 off = fposr[i];
+    int cx, cy, cz;
+    cell_xyz(P, cell_f[i], cx, cy, cz);
+    const float4 pa = mixed_abs(P, off, cx, cy, cz, 0.0f);
+    const float obx = __fadd_rn(off.x, P.cdx[0]), oby = __fadd_rn(off.y, P.cdx[1]), obz = __fadd_rn(off.z, P.cdx[2]);
+    const unsigned ci = cxyz_f[i];
+    int c[3] = {0, 0, 0};
+    const int m = min(cnt[i], cap);
+    for (int k = 0; k < m; ++k) {
+        const unsigned e = (unsigned)list[((size_t)(k / kNlGroup) * n + i) * kNlGroup + k % kNlGroup];
+        const int sp = (int)(e >> kNlSpeciesShift), j = (int)(e & kNlIndexMask);
+        if (sp == 2) {
+            const float4 q = s_pos[j];
+            if (dist2(q.x - pa.x, q.y - pa.y, q.z - pa.z) < P.R2 && cells_adjacent(ci, cxyz_s[j])) ++c[1];
+            continue;
+        }
+        const float4 q = sp == 0 ? fposr[j] : v_posr[j];
+        int jx, jy, jz;
+        unpack_cell(sp == 0 ? cxyz_f[j] : cxyz_v[j], jx, jy, jz);
+        const int ox = jx - cx, oy = jy - cy, oz = jz - cz;
+        if (abs(ox) > 1 || abs(oy) > 1 || abs(oz) > 1) continue;
+        if (dist2(q.x - shifted(obx, ox, P.cdx[0]), q.y - shifted(oby, oy, P.cdx[1]),
+                  q.z - shifted(obz, oz, P.cdx[2])) < P.R2)
+            ++c[sp == 0 ? 0 : 2];
+    }
+    out[3 * i] = c[0];
+    out[3 * i + 1] = c[1];
+    out[3 * i + 2] = c[2];
+}
+
+// (posr, velp) records of every fluid slot (after fields were set from the
+// host); the mixed form (cxyz != nullptr) carries the packed cell in place of
+// the density deviation
+__global__ void k_pack_records(const float4 *__restrict__ posr, const float4 *__restrict__ velp,
+                               const unsigned *__restrict__ cxyz, int n, float4 *__restrict__ rec)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = velp[i];
+    if (cxyz) v.w = __uint_as_float(cxyz[i]);
     rec[2 * (size_t)i] = posr[i];
-    rec[2 * (size_t)i + 1] = velp[i];
+    rec[2 * (size_t)i + 1] = v;
 }
 
 // Positions set from the host: fold their squared displacement since the last
 // list build into the instance's running maximum (the next step's decision).
-__global__ void k_nl_displacement(const float4 *__restrict__ posr, const float4 *__restrict__ x0, int n,
-                                  NlState *__restrict__ nl)
+// Mixed form (cell != nullptr): posr holds offsets from the cells.
+__global__ void k_nl_displacement(const DevParams P, const float4 *__restrict__ posr, const int *__restrict__ cell,
+                                  const float4 *__restrict__ x0, int n, NlState *__restrict__ nl)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned d2 = 0u;
     if (i < n) {
-        const float4 p = posr[i], o = x0[i];
+        float4 p = posr[i];
+        if (cell) {
+            int cx, cy, cz;
+            cell_xyz(P, cell[i], cx, cy, cz);
+            p = mixed_abs(P, p, cx, cy, cz, 0.0f);
+        }
+        const float4 o = x0[i];
         d2 = __float_as_uint(dist2(p.x - o.x, p.y - o.y, p.z - o.z));
     }
     d2 = __reduce_max_sync(kFull, d2);
@@ -2678,6 +3018,19 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape_arg, cudaEve
         {kb_fluid_sweep_nl<0, NlShape0>, kb_fluid_sweep_nl<0, NlShape1>, kb_fluid_sweep_nl<0, NlShape2>},
         {kb_fluid_sweep_nl<1, NlShape0>, kb_fluid_sweep_nl<1, NlShape1>, kb_fluid_sweep_nl<1, NlShape2>},
         {kb_fluid_sweep_nl<2, NlShape0>, kb_fluid_sweep_nl<2, NlShape1>, kb_fluid_sweep_nl<2, NlShape2>}};
+    // mixed-form list sweep, the variants kSweepNlMixedVariant + VISCID
+    static const Sweep1Fn nlm1[3][kSweepShapes] = {
+        {kb_fluid_sweep_nlm_1<0, NlmShape0>, kb_fluid_sweep_nlm_1<0, NlmShape1>, kb_fluid_sweep_nlm_1<0, NlmShape2>},
+        {kb_fluid_sweep_nlm_1<1, NlmShape0>, kb_fluid_sweep_nlm_1<1, NlmShape1>, kb_fluid_sweep_nlm_1<1, NlmShape2>},
+        {kb_fluid_sweep_nlm_1<2, NlmShape0>, kb_fluid_sweep_nlm_1<2, NlmShape1>, kb_fluid_sweep_nlm_1<2, NlmShape2>}};
+    static const SweepPFn nlmp[3][kSweepShapes] = {
+        {kb_fluid_sweep_nlm_p<0, NlmShape0>, kb_fluid_sweep_nlm_p<0, NlmShape1>, kb_fluid_sweep_nlm_p<0, NlmShape2>},
+        {kb_fluid_sweep_nlm_p<1, NlmShape0>, kb_fluid_sweep_nlm_p<1, NlmShape1>, kb_fluid_sweep_nlm_p<1, NlmShape2>},
+        {kb_fluid_sweep_nlm_p<2, NlmShape0>, kb_fluid_sweep_nlm_p<2, NlmShape1>, kb_fluid_sweep_nlm_p<2, NlmShape2>}};
+    static const SweepFn nlmb[3][kSweepShapes] = {
+        {kb_fluid_sweep_nlm<0, NlmShape0>, kb_fluid_sweep_nlm<0, NlmShape1>, kb_fluid_sweep_nlm<0, NlmShape2>},
+        {kb_fluid_sweep_nlm<1, NlmShape0>, kb_fluid_sweep_nlm<1, NlmShape1>, kb_fluid_sweep_nlm<1, NlmShape2>},
+        {kb_fluid_sweep_nlm<2, NlmShape0>, kb_fluid_sweep_nlm<2, NlmShape1>, kb_fluid_sweep_nlm<2, NlmShape2>}};
     for (size_t k = 0; k < pl.launches.size(); ++k) {
         const Launch &L = pl.launches[k];
         const int *tb = reinterpret_cast<const int *>(pl.arena + L.table_off);
@@ -2696,6 +3049,8 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape_arg, cudaEve
         case L_RANK_S: FSIM_LAUNCH(kb_rank, RankArgs, kBlock); break;
         case L_NL_DECIDE: FSIM_LAUNCH(kb_nl_decide, NlDecideArgs, kBlock); break;
         case L_NL_BUILD: FSIM_LAUNCH(kb_nl_build, NlBuildArgs, kNlBuildWarps * 32); break;
+        case L_MIXED_ABS: FSIM_LAUNCH(kb_mixed_abs, MixedAbsArgs, kBlock); break;
+        case L_MIXED_REC: FSIM_LAUNCH(kb_mixed_records, CellRefArgs, kBlock); break;
         case L_COUPLE: FSIM_LAUNCH(kb_couple, CoupleArgs, kBlock); break;
         case L_VIRT: FSIM_LAUNCH(kb_virt, VirtArgs, kBlock); break;
         case L_SWEEP:
@@ -2706,18 +3061,19 @@ fsim_status enqueue_plan(const Plan &pl, cudaStream_t st, int shape_arg, cudaEve
                 const int *tbs = reinterpret_cast<const int *>(pl.arena + L.shape_table_off[shape]);
                 const int gs = L.shape_blocks[shape], thr = kShapeWarps[shape] * 32;
                 if (L.variant >= kSweepNlVariant) {
-                    const int v = L.variant - kSweepNlVariant;
+                    const bool mx = L.variant >= kSweepNlMixedVariant;
+                    const int v = L.variant - (mx ? kSweepNlMixedVariant : kSweepNlVariant);
                     if (n == 1) {
                         const Item<FluidSweepArgs> &it = host_item<FluidSweepArgs>(pl, L);
-                        nl1[v][shape]<<<gs, thr, 0, st>>>(it.P, it.A);
+                        (mx ? nlm1 : nl1)[v][shape]<<<gs, thr, 0, st>>>(it.P, it.A);
                     } else if (n <= kSweepParamItems) {
                         static thread_local SweepBatchParams B;
                         B.n = n;
                         std::memcpy(B.bstart, pl.host.data() + L.shape_table_off[shape], sizeof(int) * (n + 1));
                         std::memcpy(B.it, pl.host.data() + L.items_off, sizeof(Item<FluidSweepArgs>) * n);
-                        nlp[v][shape]<<<gs, thr, 0, st>>>(B);
+                        (mx ? nlmp : nlp)[v][shape]<<<gs, thr, 0, st>>>(B);
                     } else {
-                        nlb[v][shape]<<<gs, thr, 0, st>>>(items_of<FluidSweepArgs>(pl, L), tbs, n);
+                        (mx ? nlmb : nlb)[v][shape]<<<gs, thr, 0, st>>>(items_of<FluidSweepArgs>(pl, L), tbs, n);
                     }
                 } else if (n == 1) {
                     const Item<FluidSweepArgs> &it = host_item<FluidSweepArgs>(pl, L);
@@ -2876,14 +3232,24 @@ void launch_k_neighbor_counts_nl(int grid, cudaStream_t st, const DevParams P, c
     k_neighbor_counts_nl<<<grid, kBlock, 0, st>>>(P, fposr, list, cnt, cap, s_pos, v_posr, out, n);
 }
 
-void launch_k_pack_records(int grid, cudaStream_t st, const float4 *posr, const float4 *velp, int n, float4 *rec)
+void launch_k_neighbor_counts_mixed(int grid, cudaStream_t st, const DevParams P, const DevParams Pv, const float4 *fposr, const int *cell_f, const int *start_f, const int *ids_f, const float4 *s_pos, const int *start_s, const int *ids_s, const float4 *v_posr, const int *start_v, const unsigned *v_cxyz, int *out, int n)
 {
-    k_pack_records<<<grid, kBlock, 0, st>>>(posr, velp, n, rec);
+    k_neighbor_counts_mixed<<<grid, kBlock, 0, st>>>(P, Pv, fposr, cell_f, start_f, ids_f, s_pos, start_s, ids_s, v_posr, start_v, v_cxyz, out, n);
 }
 
-void launch_k_nl_displacement(int grid, cudaStream_t st, const float4 *posr, const float4 *x0, int n, NlState *nl)
+void launch_k_neighbor_counts_nlm(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *cell_f, const unsigned *cxyz_f, const int *list, const int *cnt, int cap, const float4 *s_pos, const unsigned *cxyz_s, const float4 *v_posr, const unsigned *cxyz_v, int *out, int n)
 {
-    k_nl_displacement<<<grid, kBlock, 0, st>>>(posr, x0, n, nl);
+    k_neighbor_counts_nlm<<<grid, kBlock, 0, st>>>(P, fposr, cell_f, cxyz_f, list, cnt, cap, s_pos, cxyz_s, v_posr, cxyz_v, out, n);
+}
+
+void launch_k_pack_records(int grid, cudaStream_t st, const float4 *posr, const float4 *velp, const unsigned *cxyz, int n, float4 *rec)
+{
+    k_pack_records<<<grid, kBlock, 0, st>>>(posr, velp, cxyz, n, rec);
+}
+
+void launch_k_nl_displacement(int grid, cudaStream_t st, const DevParams P, const float4 *posr, const int *cell, const float4 *x0, int n, NlState *nl)
+{
+    k_nl_displacement<<<grid, kBlock, 0, st>>>(P, posr, cell, x0, n, nl);
 }
 
 void launch_k_cells_of(int grid, cudaStream_t st, const DevParams P, const float4 *pos, int n, int *out, unsigned *packed)

@@ -110,6 +110,11 @@ struct fsim_sim {
     int *s_ids = nullptr, *s_lcell = nullptr, *s_lcnt = nullptr, *s_lstart = nullptr;
     int *v_icell = nullptr;
     float4 *f_rec = nullptr;      // (posr, velp) per slot, 32 bytes: the list sweep's neighbour records
+    // mixed form with lists: f_cell is every slot's impact-grid cell (its
+    // offset's cell), carried through a rebuild's gather in f_cell2; the walls'
+    // absolute positions for the build (their v_posr are offsets from v_icell)
+    int *f_cell2 = nullptr;
+    float4 *v_abs = nullptr;
     bool rec_live = false;        // a cell phase wrote f_rec and the fluid phase has not run yet
     // misc
     int *scan_partials = nullptr; // 2 * kMaxScanTiles
@@ -347,6 +352,21 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
         db.push_back(nb);
     }
     add_launch(pl, ab, L_NL_DECIDE, di, db);
+    // mixed form: the absolute positions the list grid sorts by (into f_rec,
+    // which the cell references overwrite later in the phase)
+    const bool mixed = !m.empty() && m[0]->mixed;
+    if (mixed) {
+        std::vector<Item<MixedAbsArgs>> ai;
+        std::vector<int> abk;
+        for (fsim_sim *h : m) {
+            const int ag = std::min(blocks_for(h->nf, kBlock), kGatedGrid);
+            const Item<MixedAbsArgs> it{h->P, MixedAbsArgs{h->f_posr[pf], h->f_cell, h->f_rec, h->nf,
+                                                           &h->nl_state->rebuild, ag}};
+            ai.push_back(it);
+            abk.push_back(ag);
+        }
+        add_launch(pl, ab, L_MIXED_ABS, ai, abk);
+    }
     // list-grid sort, run only when the decision says rebuild
     std::vector<Item<ZeroArgs>> zi;
     std::vector<Item<HashArgs>> hi;
@@ -363,8 +383,9 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
             zi.push_back(z);
             zb.push_back(zg);
             const int hg = std::min(blocks_for(n, kBlock), kGatedGrid);
+            const float4 *fpos = mixed ? h->f_rec : h->f_posr[pf];
             const HashArgs ha = s_ ? HashArgs{h->s_pos[ps], h->ns, h->s_key, h->s_slot, lcnt, h->d_flags, gate, hg}
-                                   : HashArgs{h->f_posr[pf], h->nf, h->f_key, h->f_slot, lcnt, h->d_flags, gate, hg};
+                                   : HashArgs{fpos, h->nf, h->f_key, h->f_slot, lcnt, h->d_flags, gate, hg};
             const Item<HashArgs> hh{h->Pl, ha};
             hi.push_back(hh);
             hb.push_back(hg);
@@ -391,9 +412,12 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
     std::vector<int> gfb, gsb;
     for (fsim_sim *h : m) {
         const int *gate = &h->nl_state->rebuild;
-        const GatherFluidArgs fa{h->f_tmp, h->f_key, h->f_lstart, h->nf, h->f_posr[pf], h->f_velp[pf], h->f_orig[pf],
-                                 h->f_posr[1 - pf], h->f_velp[1 - pf], h->f_orig[1 - pf], h->f_lcell, h->d_flags,
-                                 gate, h->f_x0, h->f_rec};
+        const GatherFluidArgs fa{h->f_tmp,          h->f_key,           h->f_lstart,        h->nf,
+                                 h->f_posr[pf],     h->f_velp[pf],      h->f_orig[pf],      h->f_posr[1 - pf],
+                                 h->f_velp[1 - pf], h->f_orig[1 - pf],  h->f_lcell,         h->d_flags,
+                                 gate,              h->f_x0,            mixed ? nullptr : h->f_rec,
+                                 mixed ? h->f_rec : nullptr,            mixed ? h->f_cell : nullptr,
+                                 mixed ? h->f_cell2 : nullptr};
         const Item<GatherFluidArgs> fi{h->Pl, fa};
         gf.push_back(fi);
         gfb.push_back(blocks_for(h->nf, kBlock));
@@ -418,7 +442,8 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
     sp.clear();
     cb.clear();
     std::vector<Item<RankArgs>> ri;
-    std::vector<int> rb;
+    std::vector<Item<HashMixedArgs>> hmi;
+    std::vector<int> rb, hmb;
     for (fsim_sim *h : m) {
         for (int s_ = 0; s_ < 2; ++s_) {
             const int n = s_ ? h->ns : h->nf;
@@ -426,11 +451,21 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
             const Item<ZeroArgs> z{h->P, ZeroArgs{cnt, n ? h->ncell : 0, nullptr}};
             zi.push_back(z);
             zb.push_back(blocks_for(z.A.n, kBlock));
-            const HashArgs ha = s_ ? HashArgs{h->s_pos[1 - ps], h->ns, h->s_key, h->s_slot, cnt, h->d_flags, nullptr}
-                                   : HashArgs{h->f_posr[1 - pf], h->nf, h->f_key, h->f_slot, cnt, h->d_flags, nullptr};
-            const Item<HashArgs> hh{h->P, ha};
-            hi.push_back(hh);
-            hb.push_back(blocks_for(n, kBlock));
+            if (!s_ && mixed) {
+                // the mixed form re-bins every offset to its cell (in place)
+                const Item<HashMixedArgs> hm{h->P, HashMixedArgs{h->f_posr[1 - pf], h->f_cell2, h->nf, h->f_key,
+                                                                 h->f_slot, cnt, h->d_flags}};
+                hmi.push_back(hm);
+                hmb.push_back(blocks_for(n, kBlock));
+            } else {
+                const HashArgs ha = s_ ? HashArgs{h->s_pos[1 - ps], h->ns, h->s_key, h->s_slot, cnt, h->d_flags,
+                                                  nullptr}
+                                       : HashArgs{h->f_posr[1 - pf], h->nf, h->f_key, h->f_slot, cnt, h->d_flags,
+                                                  nullptr};
+                const Item<HashArgs> hh{h->P, ha};
+                hi.push_back(hh);
+                hb.push_back(blocks_for(n, kBlock));
+            }
             const Item<ScanArgs> sc{h->P,
                                     ScanArgs{cnt, start, h->ncell, h->scan_partials + (s_ ? kMaxScanTiles : 0), nullptr}};
             si.push_back(sc);
@@ -452,17 +487,34 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
     }
     add_launch(pl, ab, L_ZERO, zi, zb);
     add_launch(pl, ab, L_HASH, hi, hb);
+    add_launch(pl, ab, L_HASH_M, hmi, hmb);
     add_launch(pl, ab, L_SCAN_REDUCE, si, sb);
     add_launch(pl, ab, L_SCAN_PARTIALS, si, sp);
     add_launch(pl, ab, L_SCAN_APPLY, si, sb);
     add_launch(pl, ab, L_SCATTER, ci, cb);
     add_launch(pl, ab, L_RANK_F, ri, rb);
+    if (mixed) {
+        // per-cell references, then per slot the FP16 gather pair and the
+        // sweep's record
+        std::vector<Item<CellRefArgs>> cr;
+        std::vector<int> crb, rcb;
+        for (fsim_sim *h : m) {
+            const CellRefArgs ca{h->f_posr[1 - pf], h->f_velp[1 - pf], h->f_start, h->f_cm, h->ncell,
+                                 h->f_ids,          h->nf,             h->f_cell,  h->f_cxyz, h->f_rec};
+            const Item<CellRefArgs> c{h->P, ca};
+            cr.push_back(c);
+            crb.push_back(h->nf ? blocks_for((long long)kCellRefLanes * h->ncell, kBlock) : 0);
+            rcb.push_back(blocks_for(h->nf, kBlock));
+        }
+        add_launch(pl, ab, L_CELLREF, cr, crb);
+        add_launch(pl, ab, L_MIXED_REC, cr, rcb);
+    }
     // the list build (runs only on a rebuild)
     std::vector<Item<NlBuildArgs>> bi;
     std::vector<int> bb;
     for (fsim_sim *h : m) {
         const int bg = std::min(blocks_for(h->nf, kNlBuildThreads), kGatedBuildGrid);
-        const NlBuildArgs ba{h->f_x0,   h->f_lcell,  h->f_lstart, h->v_posr,  h->v_start,
+        const NlBuildArgs ba{h->f_x0,   h->f_lcell,  h->f_lstart, mixed ? h->v_abs : h->v_posr, h->v_start,
                              h->s_x0,   h->s_lstart, h->nf,       h->nl_cap,  h->nl_list,
                              h->nl_cnt, h->nl_state, h->d_flags,  h->nl_R2s,  h->nv,
                              h->ns,     bg};
@@ -542,7 +594,7 @@ void plan_cell(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
     for (fsim_sim *h : m) {
         if (!h->mixed) continue;
         cr.push_back({h->P, CellRefArgs{h->f_posr[1 - pf], h->f_velp[1 - pf], h->f_start, h->f_cm, h->ncell}});
-        crb.push_back(h->nf ? blocks_for(32ll * h->ncell, kBlock) : 0);
+        crb.push_back(h->nf ? blocks_for((long long)kCellRefLanes * h->ncell, kBlock) : 0);
     }
     add_launch(pl, ab, L_CELLREF, cr, crb);
 }
@@ -612,7 +664,7 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
         A.nl_ns = h->ns;
         A.x0 = h->f_x0;
         A.nl = h->nl_state;
-        A.nl_cxyz_f = h->nl_check ? h->f_cxyz : nullptr;
+        A.nl_cxyz_f = h->nl_check ? h->f_cxyz : nullptr; // (always in the mixed form)
         A.nl_cxyz_v = h->nl_check ? h->v_icxyz : nullptr;
         A.nl_cxyz_s = h->nl_check ? h->s_cxyz : nullptr;
         A.rec = h->f_rec;
@@ -628,7 +680,8 @@ void plan_fluid(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, in
     const size_t before = pl.launches.size();
     const bool mixed = !m.empty() && m[0]->mixed, nl = !m.empty() && m[0]->nl;
     add_sweep_launch(pl, ab, it, nb,
-                     nl ? kSweepNlVariant + visc_mode : mixed ? 6 + visc_mode : (any_check ? 3 : 0) + visc_mode);
+                     nl ? (mixed ? kSweepNlMixedVariant : kSweepNlVariant) + visc_mode
+                        : mixed ? 6 + visc_mode : (any_check ? 3 : 0) + visc_mode);
     if (pl.launches.size() > before) pl.sweep_index = (int)before;
 }
 
@@ -1103,6 +1156,18 @@ fsim_status build_solid_neighbors(fsim_sim *h, const float *ref)
     return FSIM_OK;
 }
 
+// The mixed form keeps the walls' positions as offsets from their impact-grid
+// cells; a neighbour-list instance also keeps their absolute positions, which
+// its list build walks on the list grid.
+fsim_status walls_to_mixed(fsim_sim *h)
+{
+    if (h->nl) CK(cudaMemcpyAsync(h->v_abs, h->v_posr, sizeof(float4) * h->nv, cudaMemcpyDeviceToDevice, h->stream));
+    launch_k_offsets_in_cells(blocks_for(h->nv, kBlock), h->stream, h->P, h->v_posr, h->nl ? h->v_icell : h->v_cell,
+                              h->nv);
+    CK_LAUNCH();
+    return FSIM_OK;
+}
+
 // Stream, events and every device array of a handle whose counts are set.
 fsim_status alloc_state(fsim_sim *h)
 {
@@ -1158,6 +1223,7 @@ fsim_status alloc_state(fsim_sim *h)
             (st = dalloc(h, &h->v_icell, nv)) || (st = dalloc(h, &h->f_rec, 2 * (size_t)nf)))
             return st;
         if (h->nl_check && ((st = dalloc(h, &h->f_cxyz, nf)) || (st = dalloc(h, &h->v_icxyz, nv)))) return st;
+        if (h->mixed && ((st = dalloc(h, &h->f_cell2, nf)) || (st = dalloc(h, &h->v_abs, nv)))) return st;
         NlState init{};
         init.force = 1; // the first step builds
         CK(cudaMemcpyAsync(h->nl_state, &init, sizeof init, cudaMemcpyHostToDevice, h->stream));
@@ -1235,10 +1301,7 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
         if ((st = build_solid_neighbors(h, p->solid_ref_pos))) return st;
     }
     if (nv && (st = sort_virtual(h, p->virt_pos))) return st;
-    if (nv && h->mixed) {
-        launch_k_offsets_in_cells(blocks_for(nv, kBlock), h->stream, h->P, h->v_posr, h->v_cell, nv);
-        CK_LAUNCH();
-    }
+    if (nv && h->mixed && (st = walls_to_mixed(h))) return st;
     CK(cudaStreamSynchronize(h->stream));
     return check_flags(h);
 }
@@ -1261,12 +1324,15 @@ void setup_lists(fsim_sim *h)
     h->nl = false;
     h->nl_check = false;
     const double skin = h->cfg.neighbor_skin;
-    if (h->mixed || !(skin > 0.0) || h->nf > kNlIndexMask || h->nv > kNlIndexMask || h->ns > kNlIndexMask) return;
+    if (!(skin > 0.0) || h->nf > kNlIndexMask || h->nv > kNlIndexMask || h->ns > kNlIndexMask) return;
     const double R = std::sqrt((double)h->der.impact_distance_square);
     for (int a = 0; a < 3; ++a) {
         const double margin = (double)h->der.interval[a] / R - 1.0;
         if (!(margin > 8e-7 * h->der.cell_number[a] + 1e-4)) h->nl_check = true;
     }
+    // the mixed form's pair positions come from cell differences: it always
+    // compares cell coordinates
+    if (h->mixed) h->nl_check = true;
     // packed coordinates (x | y << 11 | z << 21) for the check
     if (h->nl_check && (h->P.nx >= 2048 || h->P.ny >= 1024 || h->P.nz >= 2048)) return;
     const double Rs = R * (1.0 + skin);
@@ -1511,8 +1577,8 @@ fsim_status enqueue_unpermute(fsim_sim *h, int field, int n, float *stg)
     if (h->mixed && (field == FSIM_FLUID_POS || field == FSIM_FLUID_RHO || field == FSIM_FLUID_P ||
                      field == FSIM_VIRT_POS)) {
         if (field == FSIM_VIRT_POS)
-            launch_k_unpermute_mixed(g, h->stream, h->P, h->v_posr, h->v_velp, h->v_cell, h->v_orig, n, MF_POS,
-                                                            stg);
+            launch_k_unpermute_mixed(g, h->stream, h->P, h->v_posr, h->v_velp, h->nl ? h->v_icell : h->v_cell,
+                                     h->v_orig, n, MF_POS, stg);
         else
             launch_k_unpermute_mixed(g, h->stream, h->P, h->f_posr[h->f_cur], h->f_velp[h->f_cur], h->f_cell,
                                                             forig, n,
@@ -1661,11 +1727,13 @@ fsim_status enqueue_permute_in(fsim_sim *h, int field, int n, const float *stg)
         launch_k_permute_in_f4(blocks_for(n, kBlock), h->stream, dst, orig, n, comp, width, stg);
     CK_LAUNCH();
     if (h->nl && field == FSIM_FLUID_POS) {
-        launch_k_nl_displacement(blocks_for(n, kBlock), h->stream, dst, h->f_x0, n, h->nl_state);
+        launch_k_nl_displacement(blocks_for(n, kBlock), h->stream, h->P, dst, h->mixed ? h->f_cell : nullptr, h->f_x0,
+                                 n, h->nl_state);
         CK_LAUNCH();
     }
     if (h->nl && field < 10 && h->rec_live) { // between the cell and fluid phases: records follow the state
-        launch_k_pack_records(blocks_for(n, kBlock), h->stream, h->f_posr[h->f_cur], h->f_velp[h->f_cur], n, h->f_rec);
+        launch_k_pack_records(blocks_for(n, kBlock), h->stream, h->f_posr[h->f_cur], h->f_velp[h->f_cur],
+                              h->mixed ? h->f_cxyz : nullptr, n, h->f_rec);
         CK_LAUNCH();
     }
     return FSIM_OK;
@@ -1842,17 +1910,19 @@ extern "C" fsim_status fsim_neighbor_counts(fsim_handle h, int *out, size_t byte
         fsim_set_error("run FSIM_PHASE_CELL first");
         return FSIM_EINVAL;
     }
-    if (h->mixed) {
-        fsim_set_error("neighbour counts are a check of the plain form's FP32 pair set");
-        return FSIM_EINVAL;
-    }
     if (!h->nf) return FSIM_OK;
     DeviceGuard guard(h->device);
     int *d_counts = (int *)h->staging; // 3 * nf words fit the staging buffer
     const int g = blocks_for(h->nf, kBlock);
-    launch_k_neighbor_counts(g, h->stream, h->P, h->nl ? h->Pl : h->P, h->f_posr[h->f_cur], h->f_cell, h->f_start,
-                             h->nl ? h->f_ids : nullptr, h->s_pos[h->s_cur], h->s_start, h->nl ? h->s_ids : nullptr,
-                             h->v_posr, h->v_start, d_counts, h->nf);
+    if (h->mixed)
+        launch_k_neighbor_counts_mixed(g, h->stream, h->P, h->nl ? h->Pl : h->P, h->f_posr[h->f_cur], h->f_cell,
+                                       h->f_start, h->nl ? h->f_ids : nullptr, h->s_pos[h->s_cur], h->s_start,
+                                       h->nl ? h->s_ids : nullptr, h->v_posr, h->v_start,
+                                       h->nl ? h->v_icxyz : nullptr, d_counts, h->nf);
+    else
+        launch_k_neighbor_counts(g, h->stream, h->P, h->nl ? h->Pl : h->P, h->f_posr[h->f_cur], h->f_cell,
+                                 h->f_start, h->nl ? h->f_ids : nullptr, h->s_pos[h->s_cur], h->s_start,
+                                 h->nl ? h->s_ids : nullptr, h->v_posr, h->v_start, d_counts, h->nf);
     CK_LAUNCH();
     // reorder to input order in place is not possible; copy sorted and unpermute on the host
     std::vector<int> sorted(3 * (size_t)h->nf), orig(h->nf);
@@ -1927,8 +1997,13 @@ extern "C" fsim_status fsim_list_counts(fsim_handle h, int *out, size_t bytes)
     if (!h->nf) return FSIM_OK;
     DeviceGuard guard(h->device);
     int *d_counts = (int *)h->staging; // 3 * nf words fit the staging buffer
-    launch_k_neighbor_counts_nl(blocks_for(h->nf, kBlock), h->stream, h->P, h->f_posr[h->f_cur], h->nl_list,
-                                h->nl_cnt, h->nl_cap, h->s_pos[h->s_cur], h->v_posr, d_counts, h->nf);
+    if (h->mixed)
+        launch_k_neighbor_counts_nlm(blocks_for(h->nf, kBlock), h->stream, h->P, h->f_posr[h->f_cur], h->f_cell,
+                                     h->f_cxyz, h->nl_list, h->nl_cnt, h->nl_cap, h->s_pos[h->s_cur], h->s_cxyz,
+                                     h->v_posr, h->v_icxyz, d_counts, h->nf);
+    else
+        launch_k_neighbor_counts_nl(blocks_for(h->nf, kBlock), h->stream, h->P, h->f_posr[h->f_cur], h->nl_list,
+                                    h->nl_cnt, h->nl_cap, h->s_pos[h->s_cur], h->v_posr, d_counts, h->nf);
     CK_LAUNCH();
     std::vector<int> sorted(3 * (size_t)h->nf), orig(h->nf);
     CK(cudaMemcpyAsync(sorted.data(), d_counts, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -2228,6 +2303,7 @@ std::vector<SnapArray> snap_arrays(fsim_sim *h, int pf, int ps)
                                           {h->s_lcell, 4 * ns},         {h->s_lstart, 4 * (ncl + 1)},
                                           {h->s_inv, 4 * ns},           {h->nl_state, sizeof(NlState)}};
         a.insert(a.end(), b.begin(), b.end());
+        if (h->mixed) a.push_back({h->v_abs, 16 * nv});
     }
     return a;
 }
@@ -2241,14 +2317,15 @@ fsim_status nl_restore(fsim_sim *h)
     NlState now = saved;
     now.rebuild = 1;
     CK(cudaMemcpy(h->nl_state, &now, sizeof now, cudaMemcpyHostToDevice));
+    const float4 *vpos = h->mixed ? h->v_abs : h->v_posr; // absolute wall positions
     if (h->nv) {
-        launch_k_cells_of(blocks_for(h->nv, kBlock), h->stream, h->P, h->v_posr, h->nv, h->v_icell, h->v_icxyz);
+        launch_k_cells_of(blocks_for(h->nv, kBlock), h->stream, h->P, vpos, h->nv, h->v_icell, h->v_icxyz);
         CK_LAUNCH();
     }
     Plan pl;
     ArenaBuilder ab;
     add_launch(pl, ab, L_NL_BUILD,
-               std::vector<Item<NlBuildArgs>>{{h->Pl, NlBuildArgs{h->f_x0, h->f_lcell, h->f_lstart, h->v_posr,
+               std::vector<Item<NlBuildArgs>>{{h->Pl, NlBuildArgs{h->f_x0, h->f_lcell, h->f_lstart, vpos,
                                                                   h->v_start, h->s_x0, h->s_lstart, h->nf, h->nl_cap,
                                                                   h->nl_list, h->nl_cnt, h->nl_state, h->d_flags,
                                                                   h->nl_R2s, h->nv, h->ns}}},
@@ -2617,11 +2694,7 @@ extern "C" fsim_status fsim_create_case(const fsim_config *cfg, const fsim_case 
     }
     if (h->nv) {
         if ((st = sort_virtual(h, nullptr, d_vpos))) return fail(st);
-        if (h->mixed) {
-            launch_k_offsets_in_cells(blocks_for(h->nv, kBlock), h->stream, h->P, h->v_posr, h->v_cell,
-                                                                                     h->nv);
-            CK(cudaGetLastError());
-        }
+        if (h->mixed && (st = walls_to_mixed(h))) return fail(st);
     }
     // generation temporaries are released now
     CK(cudaStreamSynchronize(h->stream));
@@ -2975,14 +3048,17 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
     b += nv * (3 * sizeof(float4) + 2 * sizeof(int));
     b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 3; // counts, starts
     if (cfg->precision == FSIM_PRECISION_MIXED) b += nc * sizeof(float2); // per-cell references
-    if (cfg->precision != FSIM_PRECISION_MIXED && cfg->neighbor_skin > 0.0f) {
+    if (cfg->neighbor_skin > 0.0f) {
         // fluid neighbour lists (as setup_lists sizes them) and the list-grid
-        // sort, build state and per-step index (at most as many cells as nc)
+        // sort, build state and per-step index (at most as many cells as nc):
+        // lists, list counts, ids, list cells, packed cells; x0 and the 32-byte
+        // records; the mixed form's carried cells and absolute wall positions
         const double rs = std::sqrt((double)d.impact_distance_square) * (1.0 + cfg->neighbor_skin) /
                           (double)cfg->particle_diameter;
         const size_t cap = (((size_t)std::ceil(1.5 * 4.18879 * rs * rs * rs) + 16 + kNlGroup - 1) & ~size_t(kNlGroup - 1));
-        b += nf * (cap + 4) * sizeof(int) + nf * sizeof(float4);
+        b += nf * (cap + 4) * sizeof(int) + nf * 3 * sizeof(float4);
         b += ns * (sizeof(float4) + 2 * sizeof(int)) + nv * 2 * sizeof(int);
+        if (cfg->precision == FSIM_PRECISION_MIXED) b += nf * sizeof(int) + nv * sizeof(float4);
         b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 2 + sizeof(NlState);
     }
     b += 2 * kMaxScanTiles * sizeof(int) + sizeof(unsigned);

@@ -64,6 +64,7 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kMaxScanTiles = 16384; // cell grids up to 67M cells
 constexpr int kFluidListCap = 48;   // fluid list entries per solid lane
 constexpr int kPLStride = 12;       // floats per particle of the solid's P L^-1 array (16-byte rows)
+constexpr int kCellRefLanes = 8;    // lanes per cell of the mixed form's per-cell references (a power of two)
 
 __host__ __device__ inline int blocks_for(long long n, int b) { return (int)((n + b - 1) / b); }
 
@@ -126,6 +127,23 @@ struct GatherFluidArgs {
     const int *gate;
     float4 *x0_out;
     float4 *rec_out; // neighbour-list instances: (posr, velp) of every slot side by side (32 bytes)
+    // mixed-form neighbour-list instances: x0_out takes x0_in (absolute
+    // positions in the old order) instead of posr, and every particle's
+    // impact-grid cell moves along from icell_in to icell_out
+    const float4 *x0_in;
+    const int *icell_in;
+    int *icell_out;
+};
+
+// mixed-form neighbour-list instances, on a rebuild: absolute positions
+// (cell corner + offset) of every fluid particle
+struct MixedAbsArgs {
+    const float4 *posr;
+    const int *cell;
+    float4 *out;
+    int n;
+    const int *gate;
+    int grid;
 };
 
 struct GatherSolidArgs {
@@ -261,6 +279,15 @@ struct CellRefArgs {
     const int *start;
     float2 *cm;
     int ncell;
+    // neighbour-list instances: the per-step cell index (slots ids[start[c] ..
+    // start[c+1]) of cell c; kb_cell_ref then only forms cm), and for
+    // kb_mixed_records the fluid slots, their cells and packed cell
+    // coordinates, and the records the list sweep reads
+    const int *ids;
+    int n;
+    const int *cell;
+    const unsigned *cxyz;
+    float4 *rec;
 };
 
 // solid sub-step kernels (deformation, force, update, fused)
@@ -431,8 +458,10 @@ constexpr int kSweepShapes = 3;
 constexpr int kShapeWarps[kSweepShapes] = {4, 4, 8}; // warps per block of sweep shapes 0..2
 
 // L_SWEEP variants: 0-5 stream sweep (CHECK_Z * 3 + VISCID mode), 6-8 mixed
-// form (6 + VISCID mode), 9-11 list sweep (kSweepNlVariant + VISCID mode)
+// form (6 + VISCID mode), 9-11 list sweep (kSweepNlVariant + VISCID mode),
+// 12-14 mixed-form list sweep (kSweepNlMixedVariant + VISCID mode)
 constexpr int kSweepNlVariant = 9;
+constexpr int kSweepNlMixedVariant = 12;
 // threads per block of the list build
 constexpr int kNlBuildThreads = 128;
 
@@ -445,7 +474,7 @@ enum LaunchKind {
     L_COUPLE, L_VIRT, L_SWEEP, L_DEFORM, L_FORCE, L_UPDATE,
     L_HASH_M, L_CELLREF, L_COUPLE_M, L_VIRT_M, L_DEFORM_M, L_FORCE_M, L_SOLID_FUSED, L_SOLID_SLOTS,
     L_FORCE_RECORD, L_FORCE_LISTED, L_DEFORM_R, L_DEFORM_M_R,
-    L_NL_DECIDE, L_NL_BUILD, L_RANK_F, L_RANK_S
+    L_NL_DECIDE, L_NL_BUILD, L_RANK_F, L_RANK_S, L_MIXED_ABS, L_MIXED_REC
 };
 
 struct Launch {
@@ -540,8 +569,10 @@ void launch_k_permute_in_f4(int grid, cudaStream_t st, float4 *dst, const int *o
 void launch_k_probe(int grid, cudaStream_t st, const DevParams P, const ProbeArgs A);
 void launch_k_neighbor_counts(int grid, cudaStream_t st, const DevParams P, const DevParams Pv, const float4 *fposr, const int *cell_f, const int *start_f, const int *ids_f, const float4 *s_pos, const int *start_s, const int *ids_s, const float4 *v_posr, const int *start_v, int *out, int n);
 void launch_k_neighbor_counts_nl(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *list, const int *cnt, int cap, const float4 *s_pos, const float4 *v_posr, int *out, int n);
-void launch_k_pack_records(int grid, cudaStream_t st, const float4 *posr, const float4 *velp, int n, float4 *rec);
-void launch_k_nl_displacement(int grid, cudaStream_t st, const float4 *posr, const float4 *x0, int n, NlState *nl);
+void launch_k_neighbor_counts_mixed(int grid, cudaStream_t st, const DevParams P, const DevParams Pv, const float4 *fposr, const int *cell_f, const int *start_f, const int *ids_f, const float4 *s_pos, const int *start_s, const int *ids_s, const float4 *v_posr, const int *start_v, const unsigned *v_cxyz, int *out, int n);
+void launch_k_neighbor_counts_nlm(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *cell_f, const unsigned *cxyz_f, const int *list, const int *cnt, int cap, const float4 *s_pos, const unsigned *cxyz_s, const float4 *v_posr, const unsigned *cxyz_v, int *out, int n);
+void launch_k_pack_records(int grid, cudaStream_t st, const float4 *posr, const float4 *velp, const unsigned *cxyz, int n, float4 *rec);
+void launch_k_nl_displacement(int grid, cudaStream_t st, const DevParams P, const float4 *posr, const int *cell, const float4 *x0, int n, NlState *nl);
 void launch_k_cells_of(int grid, cudaStream_t st, const DevParams P, const float4 *pos, int n, int *out, unsigned *packed);
 void launch_k_conservation_fluid(int grid, cudaStream_t st, const DevParams P, const float4 *posr, const float4 *velp, const int *cell, int n, double vol, double *partials);
 void launch_k_conservation_solid(int grid, cudaStream_t st, const DevParams P, const float4 *pos, const float4 *vel, const float *F, int n, double rho_s, double vol, double *partials);

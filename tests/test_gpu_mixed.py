@@ -36,8 +36,15 @@ def test_mixed_field_round_trip():
     with pytest.raises(api.FsimError):
         sim.set("fluid_p", pa.fluid_p)  # pressure follows from density
     sim.phase(api.PHASE_CELL)
-    with pytest.raises(api.FsimError):
-        sim.neighbor_counts()  # a check of the FP32 form's pair set only
+    # the mixed form's pair set (offsets shifted by whole cells) is the FP32
+    # form's up to pairs within rounding of the impact distance
+    cfg_plain = api.Config.from_buffer_copy(cfg)
+    cfg_plain.precision = api.PRECISION_FP32
+    with api.Simulation(cfg_plain, pa, device=0) as plain:
+        plain.set("fluid_pos", x)
+        plain.phase(api.PHASE_CELL)
+        got, want = sim.neighbor_counts(), plain.neighbor_counts()
+    assert (got[:, 0] > 0).all() and (got != want).any(axis=1).mean() < 1e-3
     sim.close()
 
 
