@@ -101,7 +101,7 @@ typedef struct fsim_config {
                                        2^22 (a quarter of a second and more).
                                        Small values exist to exercise the
                                        timeout path.                         */
-    float neighbor_skin;            /* > 0: the plain form advances the fluid
+    float neighbor_skin;            /* > 0: both forms advance the fluid
                                        with per-particle neighbour lists of
                                        radius R (1 + skin), R the impact
                                        distance, rebuilt when a particle has
@@ -259,14 +259,16 @@ fsim_status fsim_set_fields(fsim_handle h, int n, const int *fields, const void 
 /* Neighbour search products.
  * counts: for every fluid particle (input order) the number of fluid, solid
  * and virtual particles within the impact distance among its 27 cells
- * (3*n_fluid ints), using the same FP32 distance test as the sweep. */
+ * (3*n_fluid ints), using the same FP32 distance test as the sweep (in the
+ * mixed form, offsets shifted by whole cells, as its sweep tests them). */
 fsim_status fsim_neighbor_counts(fsim_handle h, int *host_counts, size_t bytes);
 /* Fluid neighbour lists (no counterpart in the reference, which walks its
  * cells every step; cfg.neighbor_skin): *enabled = 1 when the instance
  * advances its fluid with lists, *builds = list builds so far, *capacity =
  * entries a particle's list holds, *check = 1 when pairs also need
  * neighbouring cells (cell sides within FP32 rounding of the impact
- * distance).  Any pointer may be NULL. */
+ * distance, and always in the mixed form, whose pair vectors come from cell
+ * differences).  Any pointer may be NULL. */
 fsim_status fsim_list_stats(fsim_handle h, int *enabled, int *builds, int *capacity, int *check);
 /* For every fluid particle (input order, 3 ints): the fluid, solid and
  * virtual entries of its neighbour list within the impact distance of the
