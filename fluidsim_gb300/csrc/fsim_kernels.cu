@@ -301,8 +301,10 @@ __device__ __forceinline__ void scatter_body(const DevParams &, const ScatterArg
     {
         const int s = b * blockDim.x + threadIdx.x;
         if (s >= A.n) continue;
-        FSIM_DCHECK(A.start[A.key[s]] + A.slot[s] >= 0 && A.start[A.key[s]] + A.slot[s] < A.n, 8192u, continue);
-        A.tmp[A.start[A.key[s]] + A.slot[s]] = s;
+        const int c = A.key[s];
+        FSIM_DCHECK(A.start[c] + A.slot[s] >= 0 && A.start[c] + A.slot[s] < A.n, 8192u, continue);
+        A.tmp[A.start[c] + A.slot[s]] = s;
+        if (A.reset) A.reset[c] = 0; // the counts are spent: zero for the next sort
     }
 }
 FSIM_BATCHED_KERNEL(kb_scatter, ScatterArgs, scatter_body, kBlock)

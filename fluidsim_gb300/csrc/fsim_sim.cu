@@ -335,13 +335,17 @@ void add_sweep_launch(Plan &pl, ArenaBuilder &ab, const std::vector<Item<FluidSw
 // the list decision; on a rebuild, the counting sort of fluid and solid on the
 // list grid, else an unpermuted copy; the per-step impact-grid index; on a
 // rebuild, the list build.
-// Blocks a gated launch gets per instance at most (8 per SM of a GB300; the
-// list build, whose blocks carry uneven work, 32 per SM): each loops over its
-// element blocks when the step rebuilds and returns at once when it does not.
+// Blocks a gated launch gets at most (8 per SM of a GB300; the list build,
+// whose blocks carry uneven work, 32 per SM), shared among a batch's
+// instances: each block loops over its element blocks when the step rebuilds
+// and returns at once when it does not, so the empty launches of a batch cost
+// what one instance's do.
 constexpr int kGatedGrid = 8 * 152, kGatedBuildGrid = 32 * 152;
 
 void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
 {
+    const int ninst = std::max(1, (int)m.size());
+    const int gated = std::max(1, kGatedGrid / ninst), gated_build = std::max(8, kGatedBuildGrid / ninst);
     std::vector<Item<NlDecideArgs>> di;
     std::vector<int> db;
     for (fsim_sim *h : m) {
@@ -359,7 +363,7 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
         std::vector<Item<MixedAbsArgs>> ai;
         std::vector<int> abk;
         for (fsim_sim *h : m) {
-            const int ag = std::min(blocks_for(h->nf, kBlock), kGatedGrid);
+            const int ag = std::min(blocks_for(h->nf, kBlock), gated);
             const Item<MixedAbsArgs> it{h->P, MixedAbsArgs{h->f_posr[pf], h->f_cell, h->f_rec, h->nf,
                                                            &h->nl_state->rebuild, ag}};
             ai.push_back(it);
@@ -378,11 +382,11 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
         for (int s_ = 0; s_ < 2; ++s_) {
             const int n = s_ ? h->ns : h->nf;
             int *lcnt = s_ ? h->s_lcnt : h->f_lcnt, *lstart = s_ ? h->s_lstart : h->f_lstart;
-            const int zn = n ? h->ncell_l : 0, zg = std::min(blocks_for(zn, kBlock), kGatedGrid);
+            const int zn = n ? h->ncell_l : 0, zg = std::min(blocks_for(zn, kBlock), gated);
             const Item<ZeroArgs> z{h->Pl, ZeroArgs{lcnt, zn, gate, zg}};
             zi.push_back(z);
             zb.push_back(zg);
-            const int hg = std::min(blocks_for(n, kBlock), kGatedGrid);
+            const int hg = std::min(blocks_for(n, kBlock), gated);
             const float4 *fpos = mixed ? h->f_rec : h->f_posr[pf];
             const HashArgs ha = s_ ? HashArgs{h->s_pos[ps], h->ns, h->s_key, h->s_slot, lcnt, h->d_flags, gate, hg}
                                    : HashArgs{fpos, h->nf, h->f_key, h->f_slot, lcnt, h->d_flags, gate, hg};
@@ -448,9 +452,6 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
         for (int s_ = 0; s_ < 2; ++s_) {
             const int n = s_ ? h->ns : h->nf;
             int *cnt = s_ ? h->s_cnt : h->f_cnt, *start = s_ ? h->s_start : h->f_start;
-            const Item<ZeroArgs> z{h->P, ZeroArgs{cnt, n ? h->ncell : 0, nullptr}};
-            zi.push_back(z);
-            zb.push_back(blocks_for(z.A.n, kBlock));
             if (!s_ && mixed) {
                 // the mixed form re-bins every offset to its cell (in place)
                 const Item<HashMixedArgs> hm{h->P, HashMixedArgs{h->f_posr[1 - pf], h->f_cell2, h->nf, h->f_key,
@@ -471,8 +472,9 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
             si.push_back(sc);
             sb.push_back(n ? blocks_for(h->ncell, kScanTile) : 0);
             sp.push_back(n ? 1 : 0);
-            const ScatterArgs ca = s_ ? ScatterArgs{h->s_key, h->s_slot, start, h->s_tmp, h->ns, nullptr}
-                                      : ScatterArgs{h->f_key, h->f_slot, start, h->f_tmp, h->nf, nullptr};
+            // the scatter zeroes the counts again (set to zero at creation)
+            const ScatterArgs ca = s_ ? ScatterArgs{h->s_key, h->s_slot, start, h->s_tmp, h->ns, nullptr, 0, cnt}
+                                      : ScatterArgs{h->f_key, h->f_slot, start, h->f_tmp, h->nf, nullptr, 0, cnt};
             const Item<ScatterArgs> cc{h->P, ca};
             ci.push_back(cc);
             cb.push_back(blocks_for(n, kBlock));
@@ -485,7 +487,6 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
             rb.push_back(blocks_for(n, kBlock));
         }
     }
-    add_launch(pl, ab, L_ZERO, zi, zb);
     add_launch(pl, ab, L_HASH, hi, hb);
     add_launch(pl, ab, L_HASH_M, hmi, hmb);
     add_launch(pl, ab, L_SCAN_REDUCE, si, sb);
@@ -513,7 +514,7 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
     std::vector<Item<NlBuildArgs>> bi;
     std::vector<int> bb;
     for (fsim_sim *h : m) {
-        const int bg = std::min(blocks_for(h->nf, kNlBuildThreads), kGatedBuildGrid);
+        const int bg = std::min(blocks_for(h->nf, kNlBuildThreads), gated_build);
         const NlBuildArgs ba{h->f_x0,   h->f_lcell,  h->f_lstart, mixed ? h->v_abs : h->v_posr, h->v_start,
                              h->s_x0,   h->s_lstart, h->nf,       h->nl_cap,  h->nl_list,
                              h->nl_cnt, h->nl_state, h->d_flags,  h->nl_R2s,  h->nv,
@@ -1232,6 +1233,10 @@ fsim_status alloc_state(fsim_sim *h)
         CK(cudaMemsetAsync(h->s_x0, 0, sizeof(float4) * (ns ? ns : 1), h->stream));
         CK(cudaMemsetAsync(h->f_lstart, 0, sizeof(int) * (ncl + 1), h->stream));
         CK(cudaMemsetAsync(h->s_lstart, 0, sizeof(int) * (ncl + 1), h->stream));
+        // the per-step cell index starts from zero counts; each sort's scatter
+        // leaves them zero again
+        CK(cudaMemsetAsync(h->f_cnt, 0, sizeof(int) * nc, h->stream));
+        CK(cudaMemsetAsync(h->s_cnt, 0, sizeof(int) * nc, h->stream));
         CK(cudaStreamSynchronize(h->stream)); // `init` leaves scope
     }
     // staging for field copies (input order)

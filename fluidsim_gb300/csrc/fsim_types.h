@@ -112,6 +112,10 @@ struct ScatterArgs {
     int n;
     const int *gate;
     int grid;
+    // the sort's cell counts, which the hash filled and the scan has read:
+    // zeroed here cell by cell (every counted cell holds a particle), so that
+    // the next sort needs no zeroing launch (nullptr: left as they are)
+    int *reset;
 };
 
 // With a gate, a step that does not rebuild copies the state unpermuted; a
