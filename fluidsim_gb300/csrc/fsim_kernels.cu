@@ -429,6 +429,7 @@ __device__ __forceinline__ void rank_body(const DevParams &P, const RankArgs &A,
     A.ids[dst] = src;
     A.cell_out[src] = cell;
     if (A.cxyz_out) A.cxyz_out[src] = pack_cell(P, cell);
+    if (A.pos_out) A.pos_out[dst] = A.pos_in[src];
 }
 FSIM_BATCHED_KERNEL(kb_rank, RankArgs, rank_body, kBlock)
 
@@ -1071,17 +1072,15 @@ __device__ __forceinline__ void virt_body(const DevParams &P, const VirtArgs &A,
     int best_j = -1, best_orig = INT_MAX;
     for (int r = 0; r < rows.count; ++r) {
         for (int t = A.start_f[rows.base[r] + rows.z0], te = A.start_f[rows.base[r] + rows.z1]; t < te; ++t) {
-            const int j = A.ids_f ? A.ids_f[t] : t;
-            FSIM_DCHECK(j >= 0 && j < A.nf, 32u, continue);
-            const float4 q = A.fposr[j];
+            // with the index's position copy, the particle id only for a new best
+            const float4 q = A.fpos_t ? A.fpos_t[t] : A.fposr[A.ids_f ? A.ids_f[t] : t];
             const float d2 = dist2(q.x - xi.x, q.y - xi.y, q.z - xi.z);
-            if (d2 < best) {
-                best = d2;
-                best_j = j;
-                best_orig = A.forig[j];
-            } else if (d2 == best) {
+            if (d2 <= best) {
+                const int j = A.ids_f ? A.ids_f[t] : t;
+                FSIM_DCHECK(j >= 0 && j < A.nf, 32u, continue);
                 const int o = A.forig[j];
-                if (o < best_orig) {
+                if (d2 < best || o < best_orig) {
+                    best = d2;
                     best_j = j;
                     best_orig = o;
                 }
@@ -1181,12 +1180,12 @@ __device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs
         for (int r = 0; r < rows.count; ++r) {
             const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
             for (int tf = A.start_f[c0] + g, te = A.start_f[c1]; tf < te; tf += kSolidGroup) {
-                const int j = A.ids_f ? A.ids_f[tf] : tf;
-                FSIM_DCHECK(j >= 0 && j < A.nf, 64u, continue);
-                const float4 q = A.fposr[j];
+                const float4 q = A.fpos_t ? A.fpos_t[tf] : A.fposr[A.ids_f ? A.ids_f[tf] : tf];
                 const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
                 const float r2 = dist2(dx, dy, dz);
                 if (r2 < P.R2) {
+                    const int j = A.ids_f ? A.ids_f[tf] : tf;
+                    FSIM_DCHECK(j >= 0 && j < A.nf, 64u, continue);
                     const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
                     wsum += w;
                     psum += A.fvelp[j].w * w;
@@ -1758,19 +1757,20 @@ __device__ __forceinline__ void virt_mixed_body(const DevParams &P, const VirtAr
             for (int z = z0; z < z1; ++z) {
                 const float psz = fmaf(-(float)(z - cz), P.cdx[2], xi.z);
                 for (int t = A.start_f[rb + z], te = A.start_f[rb + z + 1]; t < te; ++t) {
-                    const int j = A.ids_f ? A.ids_f[t] : t;
-                    FSIM_DCHECK(j >= 0 && j < A.nf, 32u, continue);
-                    const float4 q = A.fposr[j];
+                    const float4 q = A.fpos_t ? A.fpos_t[t] : A.fposr[A.ids_f ? A.ids_f[t] : t];
                     const float d2 = dist2(q.x - psx, q.y - psy, q.z - psz);
-                    bool take = d2 < best;
-                    if (!take && d2 == best) take = A.forig[j] < best_orig;
-                    if (take) {
-                        best = d2;
-                        best_j = j;
-                        best_orig = A.forig[j];
-                        bsx = psx;
-                        bsy = psy;
-                        bsz = psz;
+                    if (d2 <= best) {
+                        const int j = A.ids_f ? A.ids_f[t] : t;
+                        FSIM_DCHECK(j >= 0 && j < A.nf, 32u, continue);
+                        const int o = A.forig[j];
+                        if (d2 < best || o < best_orig) {
+                            best = d2;
+                            best_j = j;
+                            best_orig = o;
+                            bsx = psx;
+                            bsy = psy;
+                            bsz = psz;
+                        }
                     }
                 }
             }
@@ -1808,6 +1808,14 @@ __device__ __forceinline__ void fluid_rel(const DevParams &P, const RowMixed &R,
     dz = q.z - fmaf(-(float)k, P.cdx[2], sz0);
 }
 
+// A candidate's particle id, read from the cell index only when asked for (a
+// walk that tests positions in index order needs it for the hits alone).
+struct SlotId {
+    const int *ids;
+    int t;
+    __device__ __forceinline__ operator int() const { return ids ? ids[t] : t; }
+};
+
 // The mixed-form row walk of a solid particle: calls f(j, q, dx, dy, dz) for
 // every fluid candidate of the 27 cells of solid cell `cell`, lanes of a group
 // of `G` taking every G-th candidate of a row.  `ids`: the per-step cell index
@@ -1816,7 +1824,8 @@ __device__ __forceinline__ void fluid_rel(const DevParams &P, const RowMixed &R,
 template <int G, class F>
 __device__ __forceinline__ void solid_fluid_walk_m(const DevParams &P, const int *__restrict__ start_f,
                                                    const int *__restrict__ ids, const float4 *__restrict__ fposr,
-                                                   int cell, float4 xi, int g, F &&f)
+                                                   int cell, float4 xi, int g, F &&f,
+                                                   const float4 *__restrict__ fpos_t = nullptr)
 {
     int cx, cy, cz;
     cell_xyz(P, cell, cx, cy, cz);
@@ -1839,11 +1848,10 @@ __device__ __forceinline__ void solid_fluid_walk_m(const DevParams &P, const int
             R.sx = fmaf(-(float)ox, P.cdx[0], sox);
             R.sy = fmaf(-(float)oy, P.cdx[1], soy);
             for (int t = start_f[rb + z0] + g, te = start_f[rb + z1]; t < te; t += G) {
-                const int j = ids ? ids[t] : t;
-                const float4 q = fposr[j];
+                const float4 q = fpos_t ? fpos_t[t] : fposr[ids ? ids[t] : t];
                 float dx, dy, dz;
                 fluid_rel(P, R, t, sz0, q, dx, dy, dz);
-                f(j, dx, dy, dz);
+                f(SlotId{ids, t}, dx, dy, dz);
             }
         }
     }
@@ -1859,14 +1867,16 @@ __device__ __forceinline__ void couple_mixed_body(const DevParams &P, const Coup
     if (valid) {
         const float4 xi = A.s_pos[i];
         solid_fluid_walk_m<kSolidGroup>(P, A.start_f, A.ids_f, A.fposr, A.s_cell[i], xi, g,
-                                        [&](int j, float dx, float dy, float dz) {
+                                        [&](SlotId s, float dx, float dy, float dz) {
                                             const float r2 = dist2(dx, dy, dz);
                                             if (r2 < P.R2) {
+                                                const int j = s;
                                                 const float w = (__expf(-r2 * P.h_inv2) - P.kc1) * P.kc2;
                                                 wsum += w;
                                                 psum += eos_delta(P, A.fvelp[j].w) * w;
                                             }
-                                        });
+                                        },
+                                        A.fpos_t);
         Rows rows;
         neighbor_rows(P, A.s_cell[i], rows);
         for (int r = 0; r < rows.count; ++r) {
@@ -2127,10 +2137,10 @@ __device__ __forceinline__ void solid_force_body(const DevParams &P, const Solid
         };
         if (MIXED) {
             solid_fluid_walk_m<kSolidGroup>(P, S.start_f, S.ids_f, S.fposr, S.cell[i], xi, g,
-                                            [&](int j, float dx, float dy, float dz) {
+                                            [&](SlotId s, float dx, float dy, float dz) {
                                                 const float r2 = dist2(dx, dy, dz);
                                                 if (r2 < P.R2) {
-                                                    const float4 u = S.fvelp[j];
+                                                    const float4 u = S.fvelp[(int)s];
                                                     traction(dx, dy, dz, r2, u, fmaf(P.rho0, u.w, P.rho0),
                                                              eos_delta(P, u.w));
                                                 }
@@ -2685,6 +2695,15 @@ __global__ void k_pack_records(const float4 *__restrict__ posr, const float4 *__
     if (cxyz) v.w = __uint_as_float(cxyz[i]);
     rec[2 * (size_t)i] = posr[i];
     rec[2 * (size_t)i + 1] = v;
+}
+
+// dst[t] = src[ids[t]]: positions set from the host, into the per-step
+// index's order (between the cell phase and the walks that read it)
+__global__ void k_gather_f4(const int *__restrict__ ids, const float4 *__restrict__ src, int n,
+                            float4 *__restrict__ dst)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = src[ids[t]];
 }
 
 // Positions set from the host: fold their squared displacement since the last
@@ -3242,6 +3261,11 @@ void launch_k_neighbor_counts_mixed(int grid, cudaStream_t st, const DevParams P
 void launch_k_neighbor_counts_nlm(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *cell_f, const unsigned *cxyz_f, const int *list, const int *cnt, int cap, const float4 *s_pos, const unsigned *cxyz_s, const float4 *v_posr, const unsigned *cxyz_v, int *out, int n)
 {
     k_neighbor_counts_nlm<<<grid, kBlock, 0, st>>>(P, fposr, cell_f, cxyz_f, list, cnt, cap, s_pos, cxyz_s, v_posr, cxyz_v, out, n);
+}
+
+void launch_k_gather_f4(int grid, cudaStream_t st, const int *ids, const float4 *src, int n, float4 *dst)
+{
+    k_gather_f4<<<grid, kBlock, 0, st>>>(ids, src, n, dst);
 }
 
 void launch_k_pack_records(int grid, cudaStream_t st, const float4 *posr, const float4 *velp, const unsigned *cxyz, int n, float4 *rec)

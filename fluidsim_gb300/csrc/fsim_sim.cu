@@ -115,6 +115,7 @@ struct fsim_sim {
     // absolute positions for the build (their v_posr are offsets from v_icell)
     int *f_cell2 = nullptr;
     float4 *v_abs = nullptr;
+    float4 *f_spos = nullptr;     // fluid positions in the per-step index's order (the wall and coupling walks)
     bool rec_live = false;        // a cell phase wrote f_rec and the fluid phase has not run yet
     // misc
     int *scan_partials = nullptr; // 2 * kMaxScanTiles
@@ -479,9 +480,9 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
             ci.push_back(cc);
             cb.push_back(blocks_for(n, kBlock));
             const RankArgs ra = s_ ? RankArgs{h->s_tmp, h->s_key, start, h->ns, h->s_ids, h->s_cell, h->s_cxyz,
-                                              h->d_flags}
+                                              h->d_flags, nullptr, nullptr}
                                    : RankArgs{h->f_tmp, h->f_key, start, h->nf, h->f_ids, h->f_cell, h->f_cxyz,
-                                              h->d_flags};
+                                              h->d_flags, h->f_posr[1 - pf], h->f_spos};
             const Item<RankArgs> rr{h->P, ra};
             ri.push_back(rr);
             rb.push_back(blocks_for(n, kBlock));
@@ -607,7 +608,7 @@ void plan_couple(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, i
     for (fsim_sim *h : m) {
         const CoupleArgs ca{h->s_pos[ps], h->s_cell,  h->s_start, h->f_posr[pf], h->f_velp[pf],
                             h->f_start,   h->s_np,    h->ns,      h->nf,         h->nl ? h->f_ids : nullptr,
-                            h->nl ? h->s_ids : nullptr};
+                            h->nl ? h->s_ids : nullptr,           h->nl ? h->f_spos : nullptr};
         const Item<CoupleArgs> ci{h->P, ca};
         it.push_back(ci);
         nb.push_back(h->nf && h->ns ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
@@ -620,8 +621,9 @@ void plan_virt(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int
     std::vector<Item<VirtArgs>> it;
     std::vector<int> nb;
     for (fsim_sim *h : m) {
-        const VirtArgs va{h->v_posr,  h->v_normal, h->nl ? h->v_icell : h->v_cell, h->f_posr[pf], h->f_velp[pf],
-                          h->f_orig[pf], h->f_start, h->v_posr, h->v_velp, h->nv, h->nf, h->nl ? h->f_ids : nullptr};
+        const VirtArgs va{h->v_posr,      h->v_normal, h->nl ? h->v_icell : h->v_cell, h->f_posr[pf],
+                          h->f_velp[pf],  h->f_orig[pf], h->f_start, h->v_posr, h->v_velp, h->nv, h->nf,
+                          h->nl ? h->f_ids : nullptr, h->nl ? h->f_spos : nullptr};
         const Item<VirtArgs> vi{h->P, va};
         it.push_back(vi);
         nb.push_back(blocks_for(h->nv, kBlock));
@@ -1221,7 +1223,8 @@ fsim_status alloc_state(fsim_sim *h)
             (st = dalloc(h, &h->f_lcnt, ncl)) || (st = dalloc(h, &h->f_lstart, ncl + 1)) ||
             (st = dalloc(h, &h->s_ids, ns)) || (st = dalloc(h, &h->s_lcell, ns)) ||
             (st = dalloc(h, &h->s_lcnt, ncl)) || (st = dalloc(h, &h->s_lstart, ncl + 1)) ||
-            (st = dalloc(h, &h->v_icell, nv)) || (st = dalloc(h, &h->f_rec, 2 * (size_t)nf)))
+            (st = dalloc(h, &h->v_icell, nv)) || (st = dalloc(h, &h->f_rec, 2 * (size_t)nf)) ||
+            (st = dalloc(h, &h->f_spos, nf)))
             return st;
         if (h->nl_check && ((st = dalloc(h, &h->f_cxyz, nf)) || (st = dalloc(h, &h->v_icxyz, nv)))) return st;
         if (h->mixed && ((st = dalloc(h, &h->f_cell2, nf)) || (st = dalloc(h, &h->v_abs, nv)))) return st;
@@ -1734,6 +1737,10 @@ fsim_status enqueue_permute_in(fsim_sim *h, int field, int n, const float *stg)
     if (h->nl && field == FSIM_FLUID_POS) {
         launch_k_nl_displacement(blocks_for(n, kBlock), h->stream, h->P, dst, h->mixed ? h->f_cell : nullptr, h->f_x0,
                                  n, h->nl_state);
+        CK_LAUNCH();
+    }
+    if (h->nl && field == FSIM_FLUID_POS && h->f_sorted) { // the index's position copy follows the state
+        launch_k_gather_f4(blocks_for(n, kBlock), h->stream, h->f_ids, h->f_posr[h->f_cur], n, h->f_spos);
         CK_LAUNCH();
     }
     if (h->nl && field < 10 && h->rec_live) { // between the cell and fluid phases: records follow the state

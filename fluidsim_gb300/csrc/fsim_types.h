@@ -174,6 +174,10 @@ struct RankArgs {
     int *ids, *cell_out;
     unsigned *cxyz_out;
     unsigned *flags;
+    // fluid: pos_out[slot] = pos_in[ids[slot]], the positions in index order
+    // that the wall and coupling walks test (nullptr: not written)
+    const float4 *pos_in;
+    float4 *pos_out;
 };
 
 // list decision: `nblocks` blocks per instance share the solid's displacement;
@@ -255,6 +259,7 @@ struct VirtArgs {
     float4 *v_posr, *v_velp;
     int n, nf;
     const int *ids_f;
+    const float4 *fpos_t; // with ids_f: fposr[ids_f[t]] for every index slot t
 };
 
 // solid normal and Shepard pressure
@@ -266,6 +271,7 @@ struct CoupleArgs {
     float4 *s_np;
     int n, nf;
     const int *ids_f, *ids_s;
+    const float4 *fpos_t; // with ids_f: fposr[ids_f[t]] for every index slot t
 };
 
 // mixed form: re-binning hash, per-cell references of the FP16 gather
@@ -575,6 +581,7 @@ void launch_k_neighbor_counts(int grid, cudaStream_t st, const DevParams P, cons
 void launch_k_neighbor_counts_nl(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *list, const int *cnt, int cap, const float4 *s_pos, const float4 *v_posr, int *out, int n);
 void launch_k_neighbor_counts_mixed(int grid, cudaStream_t st, const DevParams P, const DevParams Pv, const float4 *fposr, const int *cell_f, const int *start_f, const int *ids_f, const float4 *s_pos, const int *start_s, const int *ids_s, const float4 *v_posr, const int *start_v, const unsigned *v_cxyz, int *out, int n);
 void launch_k_neighbor_counts_nlm(int grid, cudaStream_t st, const DevParams P, const float4 *fposr, const int *cell_f, const unsigned *cxyz_f, const int *list, const int *cnt, int cap, const float4 *s_pos, const unsigned *cxyz_s, const float4 *v_posr, const unsigned *cxyz_v, int *out, int n);
+void launch_k_gather_f4(int grid, cudaStream_t st, const int *ids, const float4 *src, int n, float4 *dst);
 void launch_k_pack_records(int grid, cudaStream_t st, const float4 *posr, const float4 *velp, const unsigned *cxyz, int n, float4 *rec);
 void launch_k_nl_displacement(int grid, cudaStream_t st, const DevParams P, const float4 *posr, const int *cell, const float4 *x0, int n, NlState *nl);
 void launch_k_cells_of(int grid, cudaStream_t st, const DevParams P, const float4 *pos, int n, int *out, unsigned *packed);
