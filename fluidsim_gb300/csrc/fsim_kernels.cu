@@ -1981,7 +1981,10 @@ __device__ __forceinline__ float solid_pair_weight(const DevParams &P, float dx,
 // MIXED: L^-1 is formed in FP64 (cofactors, determinant, division) and rounded.
 // RESOLVE (the step's first sub-step): each list entry's neighbour slot is
 // resolved here, as kb_solid_slots would, and stored for the later sub-steps.
-template <bool MIXED, bool RESOLVE = false>
+// FORM_L (the step's first sub-step): L and its inverse are formed and stored;
+// the later sub-steps read the inverse back (L depends on the reference
+// configuration and the step's neighbour set only).
+template <bool MIXED, bool RESOLVE = false, bool FORM_L = RESOLVE>
 __device__ __forceinline__ void solid_deform_body(const DevParams &P, const SolidArgs &S, int blk)
 {
     const int t = blk * blockDim.x + threadIdx.x;
@@ -2019,7 +2022,7 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     F.m[3 * a + c] = fmaf(ra, dX[c], F.m[3 * a + c]);
-                    L.m[3 * a + c] = fmaf(la, dX[c], L.m[3 * a + c]);
+                    if (FORM_L) L.m[3 * a + c] = fmaf(la, dX[c], L.m[3 * a + c]);
                 }
             }
         }
@@ -2027,11 +2030,14 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         F.m[k] = group_sum(F.m[k]);
-        L.m[k] = group_sum(L.m[k]);
+        if (FORM_L) L.m[k] = group_sum(L.m[k]);
     }
     if (!valid || g) return;
     M3 Linv;
-    if (MIXED) {
+    if (!FORM_L) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Linv.m[k] = S.L[9 * i + k];
+    } else if (MIXED) {
         double l[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) l[k] = (double)L.m[k];
@@ -2082,7 +2088,7 @@ __device__ __forceinline__ void solid_deform_body(const DevParams &P, const Soli
     for (int k = 0; k < 9; ++k) {
         S.F[9 * i + k] = F.m[k];
         S.Pk[9 * i + k] = Pk.m[k];
-        S.L[9 * i + k] = Linv.m[k];
+        if (FORM_L) S.L[9 * i + k] = Linv.m[k];
         S.AV[9 * i + k] = AV.m[k];
     }
     float4 *pl = reinterpret_cast<float4 *>(S.PL + kPLStride * i);
@@ -2489,7 +2495,8 @@ __global__ void __launch_bounds__(kBlock, 3) kb_solid_fused(const Item<SolidArgs
             const int inst = locate_instance(F.bstart_w, F.ninst, b);
             if (k >= items[inst].A.nsub) continue;
             const DevParams P = items[inst].P;
-            solid_deform_body<MIXED>(P, items[inst].A, b - F.bstart_w[inst]);
+            if (k == 0) solid_deform_body<MIXED, false, true>(P, items[inst].A, b - F.bstart_w[inst]);
+            else solid_deform_body<MIXED>(P, items[inst].A, b - F.bstart_w[inst]);
         }
         grid_sync(F.barrier, ok, F.polls);
         if (!ok) break;

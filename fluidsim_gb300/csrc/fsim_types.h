@@ -323,8 +323,8 @@ struct SolidArgs {
     float4 *fl_org;
     int *nbr_slot;         // this step: sorted slot of each entry's neighbour, -1 if its cell is not adjacent
     int ne;                // list entries
-    const unsigned *cxyz;
     int nsub;              // this instance's solid sub-steps per step
+    const unsigned *cxyz;
     unsigned *flags;       // this instance's error flags
 };
 
