@@ -125,6 +125,42 @@ def test_lists_match_cell_walk_over_steps(precision):
 
 
 @pytest.mark.parametrize("precision", FORMS)
+def test_positions_set_after_the_cell_phase_reach_the_walks(precision):
+    """The wall and coupling walks test positions in the per-step index's
+    order (a copy the cell phase writes): positions written from the host
+    after the cell phase must reach that copy, so the walls and the solid's
+    pressure see them exactly as the cell walk (skin 0) does."""
+    cfg, pa = _moving_dam(0.1, vx=0.0, precision=precision)
+    cfg0, _ = _moving_dam(0.0, vx=0.0, precision=precision)
+    a = api.Simulation(cfg, pa, device=0)
+    b = api.Simulation(cfg0, pa, device=0)
+    shifted = pa.fluid_pos.copy()
+    shifted[:, 0] -= 0.2 * cfg.particle_diameter
+    for sim in (a, b):
+        sim.phase(api.PHASE_CELL)
+        sim.set("fluid_pos", shifted)  # both walk the index of the unshifted positions
+        sim.phase(api.PHASE_COUPLE)
+        sim.phase(api.PHASE_VIRT)
+    a.sync()
+    b.sync()
+    # the nearest fluid particle is order-independent: the walls agree bit for bit
+    for f in ("virt_rho", "virt_p", "virt_vel"):
+        assert np.array_equal(a.get(f), b.get(f)), f
+    # the Shepard sums follow each index's order within a cell: rounding only
+    e = nerr(a.get("solid_p"), b.get("solid_p").astype(np.float64))
+    assert e <= 1e-6, e
+    # and the walls did see the shift
+    with api.Simulation(cfg0, pa, device=0) as c:
+        c.phase(api.PHASE_CELL)
+        c.phase(api.PHASE_COUPLE)
+        c.phase(api.PHASE_VIRT)
+        c.sync()
+        assert not np.array_equal(c.get("virt_p"), b.get("virt_p"))
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("precision", FORMS)
 def test_set_positions_counts_as_displacement(precision):
     """Positions written from the host move particles like a step does: a
     shift beyond the rebuild allowance (about 0.05 R = 0.13 dx) rebuilds the
