@@ -1156,21 +1156,22 @@ __device__ __forceinline__ float warp_sum(float v)
 // kSolidGroup lanes share one solid particle: they split its candidates and
 // combine their sums with shuffles (a fixed pairing: deterministic).
 
+template <int G = kSolidGroup>
 __device__ __forceinline__ float group_sum(float v)
 {
 #pragma unroll
-    for (int o = 1; o < kSolidGroup; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
+    for (int o = 1; o < G; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
     return v;
 }
 
 // ------------------------------------------------------- fluid-solid coupling
 // solidCoupleUpdate (src/solid.cu:262-344): solid normal from the solid
 // neighbours' kernel gradients, solid pressure as the Shepard average of the
-// fluid pressure.  kSolidGroup lanes per solid particle.
+// fluid pressure.  kCoupleGroup lanes per solid particle.
 __device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs &A, int blk)
 {
     const int t = blk * blockDim.x + threadIdx.x;
-    const int i = t / kSolidGroup, g = t % kSolidGroup;
+    const int i = t / kCoupleGroup, g = t % kCoupleGroup;
     const bool valid = i < A.n;
     float nx = 0.0f, ny = 0.0f, nz = 0.0f, psum = 0.0f, wsum = 0.0f;
     if (valid) {
@@ -1179,7 +1180,7 @@ __device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs
         neighbor_rows(P, A.s_cell[i], rows);
         for (int r = 0; r < rows.count; ++r) {
             const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-            for (int tf = A.start_f[c0] + g, te = A.start_f[c1]; tf < te; tf += kSolidGroup) {
+            for (int tf = A.start_f[c0] + g, te = A.start_f[c1]; tf < te; tf += kCoupleGroup) {
                 const float4 q = A.fpos_t ? A.fpos_t[tf] : A.fposr[A.ids_f ? A.ids_f[tf] : tf];
                 const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
                 const float r2 = dist2(dx, dy, dz);
@@ -1191,7 +1192,7 @@ __device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs
                     psum += A.fvelp[j].w * w;
                 }
             }
-            for (int ts = A.start_s[c0] + g, te = A.start_s[c1]; ts < te; ts += kSolidGroup) {
+            for (int ts = A.start_s[c0] + g, te = A.start_s[c1]; ts < te; ts += kCoupleGroup) {
                 const int j = A.ids_s ? A.ids_s[ts] : ts;
                 FSIM_DCHECK(j >= 0 && j < A.n, 128u, continue);
                 const float4 q = A.s_pos[j];
@@ -1206,11 +1207,11 @@ __device__ __forceinline__ void couple_body(const DevParams &P, const CoupleArgs
             }
         }
     }
-    nx = group_sum(nx);
-    ny = group_sum(ny);
-    nz = group_sum(nz);
-    psum = group_sum(psum);
-    wsum = group_sum(wsum);
+    nx = group_sum<kCoupleGroup>(nx);
+    ny = group_sum<kCoupleGroup>(ny);
+    nz = group_sum<kCoupleGroup>(nz);
+    psum = group_sum<kCoupleGroup>(psum);
+    wsum = group_sum<kCoupleGroup>(wsum);
     if (!valid || g) return;
     const float l2 = nx * nx + ny * ny + nz * nz;
     if (l2 < FSIM_EPS_FOR_SUM) {
@@ -1861,12 +1862,12 @@ __device__ __forceinline__ void solid_fluid_walk_m(const DevParams &P, const int
 __device__ __forceinline__ void couple_mixed_body(const DevParams &P, const CoupleArgs &A, int blk)
 {
     const int t = blk * blockDim.x + threadIdx.x;
-    const int i = t / kSolidGroup, g = t % kSolidGroup;
+    const int i = t / kCoupleGroup, g = t % kCoupleGroup;
     const bool valid = i < A.n;
     float nx = 0.0f, ny = 0.0f, nz = 0.0f, psum = 0.0f, wsum = 0.0f;
     if (valid) {
         const float4 xi = A.s_pos[i];
-        solid_fluid_walk_m<kSolidGroup>(P, A.start_f, A.ids_f, A.fposr, A.s_cell[i], xi, g,
+        solid_fluid_walk_m<kCoupleGroup>(P, A.start_f, A.ids_f, A.fposr, A.s_cell[i], xi, g,
                                         [&](SlotId s, float dx, float dy, float dz) {
                                             const float r2 = dist2(dx, dy, dz);
                                             if (r2 < P.R2) {
@@ -1881,7 +1882,7 @@ __device__ __forceinline__ void couple_mixed_body(const DevParams &P, const Coup
         neighbor_rows(P, A.s_cell[i], rows);
         for (int r = 0; r < rows.count; ++r) {
             const int c0 = rows.base[r] + rows.z0, c1 = rows.base[r] + rows.z1;
-            for (int ts = A.start_s[c0] + g, te = A.start_s[c1]; ts < te; ts += kSolidGroup) {
+            for (int ts = A.start_s[c0] + g, te = A.start_s[c1]; ts < te; ts += kCoupleGroup) {
                 const float4 q = A.s_pos[A.ids_s ? A.ids_s[ts] : ts];
                 const float dx = q.x - xi.x, dy = q.y - xi.y, dz = q.z - xi.z;
                 const float r2 = dist2(dx, dy, dz);
@@ -1894,11 +1895,11 @@ __device__ __forceinline__ void couple_mixed_body(const DevParams &P, const Coup
             }
         }
     }
-    nx = group_sum(nx);
-    ny = group_sum(ny);
-    nz = group_sum(nz);
-    psum = group_sum(psum);
-    wsum = group_sum(wsum);
+    nx = group_sum<kCoupleGroup>(nx);
+    ny = group_sum<kCoupleGroup>(ny);
+    nz = group_sum<kCoupleGroup>(nz);
+    psum = group_sum<kCoupleGroup>(psum);
+    wsum = group_sum<kCoupleGroup>(wsum);
     if (!valid || g) return;
     const float l2 = nx * nx + ny * ny + nz * nz;
     if (l2 < FSIM_EPS_FOR_SUM) {

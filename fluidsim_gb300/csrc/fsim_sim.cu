@@ -611,7 +611,7 @@ void plan_couple(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, i
                             h->nl ? h->s_ids : nullptr,           h->nl ? h->f_spos : nullptr};
         const Item<CoupleArgs> ci{h->P, ca};
         it.push_back(ci);
-        nb.push_back(h->nf && h->ns ? blocks_for((long long)kSolidGroup * h->ns, kBlock) : 0);
+        nb.push_back(h->nf && h->ns ? blocks_for((long long)kCoupleGroup * h->ns, kBlock) : 0);
     }
     add_launch(pl, ab, m.empty() || !m[0]->mixed ? L_COUPLE : L_COUPLE_M, it, nb);
 }

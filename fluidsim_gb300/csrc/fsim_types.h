@@ -454,8 +454,11 @@ struct GridBarrier {
 // what the mixed-form field (un)permutes move
 enum MixedField { MF_POS = 0, MF_RHO = 1, MF_P = 2 };
 
-// lanes per solid particle in the solid sweeps and the coupling
+// lanes per solid particle in the solid sweeps, and in the coupling (whose
+// walks over the fluid of 27 cells are longer: more lanes measured faster
+// there, slower in the solid sweeps)
 constexpr int kSolidGroup = 4;
+constexpr int kCoupleGroup = 8;
 
 // mixed sweep: neighbour-list entry = particle index | 6-bit cell code << kCodeShift
 constexpr int kCodeShift = 26;                   // neighbour-list entry = j | cell code << 26

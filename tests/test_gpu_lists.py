@@ -135,7 +135,7 @@ def test_positions_set_after_the_cell_phase_reach_the_walks(precision):
     a = api.Simulation(cfg, pa, device=0)
     b = api.Simulation(cfg0, pa, device=0)
     shifted = pa.fluid_pos.copy()
-    shifted[:, 0] -= 0.2 * cfg.particle_diameter
+    shifted[:, 1] += 0.2 * cfg.particle_diameter  # along gravity: the walls' hydrostatic pressure moves
     for sim in (a, b):
         sim.phase(api.PHASE_CELL)
         sim.set("fluid_pos", shifted)  # both walk the index of the unshifted positions
