@@ -336,17 +336,21 @@ void add_sweep_launch(Plan &pl, ArenaBuilder &ab, const std::vector<Item<FluidSw
 // the list decision; on a rebuild, the counting sort of fluid and solid on the
 // list grid, else an unpermuted copy; the per-step impact-grid index; on a
 // rebuild, the list build.
-// Blocks a gated launch gets at most (8 per SM of a GB300; the list build,
-// whose blocks carry uneven work, 32 per SM), shared among a batch's
-// instances: each block loops over its element blocks when the step rebuilds
-// and returns at once when it does not, so the empty launches of a batch cost
-// what one instance's do.
+// Blocks a gated launch gets per instance at most (8 per SM of a GB300; the
+// list build, whose blocks carry uneven work, 32 per SM): each loops over its
+// element blocks when its instance rebuilds and returns at once when it does
+// not.  A grid shared by a batch's instances (equally, or in proportion to
+// their particles) measured slower: in a batch some member rebuilds in most
+// steps, and its sort and build then ran on a fraction of the GPU.
 constexpr int kGatedGrid = 8 * 152, kGatedBuildGrid = 32 * 152;
+
+int gated_grid(int grid, long long n, int block)
+{
+    return n > 0 ? (int)std::min<long long>(grid, blocks_for(n, block)) : 0;
+}
 
 void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, int pf, int ps)
 {
-    const int ninst = std::max(1, (int)m.size());
-    const int gated = std::max(1, kGatedGrid / ninst), gated_build = std::max(8, kGatedBuildGrid / ninst);
     std::vector<Item<NlDecideArgs>> di;
     std::vector<int> db;
     for (fsim_sim *h : m) {
@@ -364,7 +368,7 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
         std::vector<Item<MixedAbsArgs>> ai;
         std::vector<int> abk;
         for (fsim_sim *h : m) {
-            const int ag = std::min(blocks_for(h->nf, kBlock), gated);
+            const int ag = gated_grid(kGatedGrid, h->nf, kBlock);
             const Item<MixedAbsArgs> it{h->P, MixedAbsArgs{h->f_posr[pf], h->f_cell, h->f_rec, h->nf,
                                                            &h->nl_state->rebuild, ag}};
             ai.push_back(it);
@@ -383,11 +387,11 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
         for (int s_ = 0; s_ < 2; ++s_) {
             const int n = s_ ? h->ns : h->nf;
             int *lcnt = s_ ? h->s_lcnt : h->f_lcnt, *lstart = s_ ? h->s_lstart : h->f_lstart;
-            const int zn = n ? h->ncell_l : 0, zg = std::min(blocks_for(zn, kBlock), gated);
+            const int zn = n ? h->ncell_l : 0, zg = gated_grid(kGatedGrid, zn, kBlock);
             const Item<ZeroArgs> z{h->Pl, ZeroArgs{lcnt, zn, gate, zg}};
             zi.push_back(z);
             zb.push_back(zg);
-            const int hg = std::min(blocks_for(n, kBlock), gated);
+            const int hg = gated_grid(kGatedGrid, n, kBlock);
             const float4 *fpos = mixed ? h->f_rec : h->f_posr[pf];
             const HashArgs ha = s_ ? HashArgs{h->s_pos[ps], h->ns, h->s_key, h->s_slot, lcnt, h->d_flags, gate, hg}
                                    : HashArgs{fpos, h->nf, h->f_key, h->f_slot, lcnt, h->d_flags, gate, hg};
@@ -515,7 +519,7 @@ void plan_cell_nl(Plan &pl, ArenaBuilder &ab, const std::vector<fsim_sim *> &m, 
     std::vector<Item<NlBuildArgs>> bi;
     std::vector<int> bb;
     for (fsim_sim *h : m) {
-        const int bg = std::min(blocks_for(h->nf, kNlBuildThreads), gated_build);
+        const int bg = gated_grid(kGatedBuildGrid, h->nf, kNlBuildThreads);
         const NlBuildArgs ba{h->f_x0,   h->f_lcell,  h->f_lstart, mixed ? h->v_abs : h->v_posr, h->v_start,
                              h->s_x0,   h->s_lstart, h->nf,       h->nl_cap,  h->nl_list,
                              h->nl_cnt, h->nl_state, h->d_flags,  h->nl_R2s,  h->nv,
