@@ -180,6 +180,7 @@ def load():
         "fsim_batch_launches_per_step": (C.c_int, [P, C.POINTER(C.c_int)]),
         "fsim_batch_destroy": (C.c_int, [P]),
         "fsim_estimate_bytes": (C.c_int, [C.POINTER(Config), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_size_t)]),
+        "fsim_device_bytes": (C.c_int, [P, C.POINTER(C.c_size_t)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -197,7 +198,8 @@ EXPORTED = [
     "fsim_neighbor_counts", "fsim_get_cells", "fsim_write_vtk", "fsim_time_steps", "fsim_time_sweep",
     "fsim_launches_per_step", "fsim_host_alloc", "fsim_host_free", "fsim_counts", "fsim_get_derived",
     "fsim_cell_sort_noalloc", "fsim_batch_create", "fsim_batch_step", "fsim_batch_sync", "fsim_batch_time_steps",
-    "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes", "fsim_conservation",
+    "fsim_batch_launches_per_step", "fsim_batch_destroy", "fsim_estimate_bytes", "fsim_device_bytes",
+    "fsim_conservation",
     "fsim_measure_fp32_peak", "fsim_sweep_tuning", "fsim_batch_sweep_tuning", "fsim_snapshot_bytes",
     "fsim_snapshot_save", "fsim_snapshot_load", "fsim_snapshot_write", "fsim_snapshot_read", "fsim_probe",
     "fsim_write_vtk_binary", "fsim_batch_sync_members", "fsim_create_case", "fsim_case_counts",
@@ -550,6 +552,12 @@ class Simulation:
     def sweep_tuning(self):
         """(chosen shape or -1, [ms per shape]) of the sweep autotuner."""
         return _tuning(self.lib.fsim_sweep_tuning, self.h)
+
+    def device_bytes(self):
+        """Device memory the instance's own arrays hold (fsim_device_bytes)."""
+        out = C.c_size_t()
+        check(self.lib.fsim_device_bytes(self.h, C.byref(out)))
+        return out.value
 
     def conservation(self):
         """FP64 conservation totals (fsim_conservation) as a dict."""

@@ -132,7 +132,7 @@ struct fsim_sim {
     fsim_batch *batch = nullptr;   // set while the handle belongs to a batch
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> sweep_events;
-    std::vector<void *> allocations;
+    std::vector<std::pair<void *, size_t>> allocations; // the instance's device arrays and their bytes
 };
 
 namespace {
@@ -148,8 +148,19 @@ fsim_status dalloc(fsim_sim *h, T **p, size_t count)
         fsim_set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
         return FSIM_ENOMEM;
     }
-    h->allocations.push_back((void *)*p);
+    h->allocations.emplace_back((void *)*p, count * sizeof(T));
     return FSIM_OK;
+}
+
+// free a temporary that dalloc made
+void release(fsim_sim *h, void *p)
+{
+    cudaFree(p);
+    for (auto it = h->allocations.begin(); it != h->allocations.end(); ++it)
+        if (it->first == p) {
+            h->allocations.erase(it);
+            return;
+        }
 }
 
 void free_plan(Plan *pl);
@@ -167,7 +178,7 @@ void free_all(fsim_sim *h)
                 free_plan(pl);
                 pl = nullptr;
             }
-    for (void *p : h->allocations) cudaFree(p);
+    for (auto &a : h->allocations) cudaFree(a.first);
     h->allocations.clear();
     for (cudaEvent_t e : h->sweep_events) cudaEventDestroy(e);
     h->sweep_events.clear();
@@ -1077,14 +1088,7 @@ fsim_status sort_virtual(fsim_sim *h, const float *vpos_host, float4 *vpos_dev =
     if (st) return st;
     // temporaries are released now
     void *tmps[] = {d_xyz, tmp_pos, key, slot, tmp, cnt, orig0};
-    for (void *p : tmps) {
-        cudaFree(p);
-        for (auto it = h->allocations.begin(); it != h->allocations.end(); ++it)
-            if (*it == p) {
-                h->allocations.erase(it);
-                break;
-            }
-    }
+    for (void *p : tmps) release(h, p);
     return FSIM_OK;
 }
 
@@ -1284,8 +1288,7 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
                                                                                h->f_cell, nf, h->d_flags);
         CK_LAUNCH();
         CK(cudaStreamSynchronize(h->stream));
-        cudaFree(d_rho);
-        h->allocations.pop_back();
+        release(h, d_rho);
     }
     if (ns) {
         CK(cudaMemcpyAsync(stg, p->solid_pos, sizeof(float) * 3 * ns, cudaMemcpyHostToDevice, h->stream));
@@ -2715,14 +2718,7 @@ extern "C" fsim_status fsim_create_case(const fsim_config *cfg, const fsim_case 
     // generation temporaries are released now
     CK(cudaStreamSynchronize(h->stream));
     void *tmps[] = {d_base, d_hydro, d_vpos};
-    for (void *p : tmps) {
-        cudaFree(p);
-        for (auto it = h->allocations.begin(); it != h->allocations.end(); ++it)
-            if (*it == p) {
-                h->allocations.erase(it);
-                break;
-            }
-    }
+    for (void *p : tmps) release(h, p);
     if ((st = check_flags(h))) return fail(st);
     *out = h;
     return FSIM_OK;
@@ -3040,6 +3036,15 @@ extern "C" fsim_status fsim_batch_destroy(fsim_batch_t b)
     return FSIM_OK;
 }
 
+extern "C" fsim_status fsim_device_bytes(fsim_handle h, size_t *bytes)
+{
+    if (!h || !bytes) return FSIM_EINVAL;
+    size_t b = 0;
+    for (const auto &a : h->allocations) b += a.second;
+    *bytes = b;
+    return FSIM_OK;
+}
+
 extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, int n_solid, int n_virt,
                                            size_t *out)
 {
@@ -3067,12 +3072,13 @@ extern "C" fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, 
     if (cfg->neighbor_skin > 0.0f) {
         // fluid neighbour lists (as setup_lists sizes them) and the list-grid
         // sort, build state and per-step index (at most as many cells as nc):
-        // lists, list counts, ids, list cells, packed cells; x0 and the 32-byte
-        // records; the mixed form's carried cells and absolute wall positions
+        // lists, list counts, ids, list cells, packed cells; x0, the 32-byte
+        // records and the positions in the index's order; the mixed form's
+        // carried cells and absolute wall positions
         const double rs = std::sqrt((double)d.impact_distance_square) * (1.0 + cfg->neighbor_skin) /
                           (double)cfg->particle_diameter;
         const size_t cap = (((size_t)std::ceil(1.5 * 4.18879 * rs * rs * rs) + 16 + kNlGroup - 1) & ~size_t(kNlGroup - 1));
-        b += nf * (cap + 4) * sizeof(int) + nf * 3 * sizeof(float4);
+        b += nf * (cap + 4) * sizeof(int) + nf * 4 * sizeof(float4);
         b += ns * (sizeof(float4) + 2 * sizeof(int)) + nv * 2 * sizeof(int);
         if (cfg->precision == FSIM_PRECISION_MIXED) b += nf * sizeof(int) + nv * sizeof(float4);
         b += nc * sizeof(int) * 2 + (nc + 1) * sizeof(int) * 2 + sizeof(NlState);

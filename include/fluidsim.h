@@ -408,6 +408,11 @@ fsim_status fsim_cell_sort_noalloc(const fsim_derived *grid, const float *d_pos,
 /* Device memory an instance of this configuration and these particle
  * counts allocates (an upper estimate, for admission control). */
 fsim_status fsim_estimate_bytes(const fsim_config *cfg, int n_fluid, int n_solid, int n_virt, size_t *out);
+/* Device memory the instance's own arrays hold now (state, cell structures,
+ * neighbour lists, solid lists, staging); step plans, their graphs and the
+ * buffers of fsim_get_fields / fsim_set_fields are not counted.  The measure
+ * fsim_estimate_bytes bounds.  No counterpart in the reference. */
+fsim_status fsim_device_bytes(fsim_handle h, size_t *bytes);
 
 /* Point probes.  Replaces Probe::getData (src/probe.cu and include/probe.h:8-35
  * of the reference, a 2D helper left commented out there), in 3D: at each of
