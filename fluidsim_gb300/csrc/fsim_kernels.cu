@@ -1584,7 +1584,7 @@ __device__ __forceinline__ void unpack_cell(unsigned c, int &cx, int &cy, int &c
 // list build between builds; each step re-bins every offset to the cell it now
 // lies in (in place), and the per-step cell index (kb_rank) gives every
 // particle's cell and packed cell coordinates.  A fluid neighbour's record
-// (32 bytes, written with the per-cell references) is
+// (32 bytes, written by kb_mixed_records after the per-cell references) is
 //   (offset x y z, FP16 (delta, p) deviations | u v w, packed cell)
 // and a pair is taken exactly as the mixed cell walk takes it: the two cells
 // are neighbours, and r^2 < R^2 with the offset of i shifted by the cell

@@ -1325,7 +1325,7 @@ fsim_status create_impl(fsim_sim *h, const fsim_particles *p)
 
 // =================================================================== C ABI
 namespace {
-// Fluid neighbour lists (cfg.neighbor_skin > 0, plain form): list radius
+// Fluid neighbour lists (cfg.neighbor_skin > 0, both forms): list radius
 // Rs = R (1 + skin); a step rebuilds once any particle has moved more than
 // (Rs - R) / 2 less a rounding allowance since the last build, so that every
 // pair within R is in the lists.  The reference pairs particles within R in
