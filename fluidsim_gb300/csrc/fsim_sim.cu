@@ -133,6 +133,10 @@ struct fsim_sim {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> sweep_events;
     std::vector<std::pair<void *, size_t>> allocations; // the instance's device arrays and their bytes
+    // creation temporaries, freed at the instance's first step or batch entry
+    // rather than during creation: cudaFree waits for the whole device, and a
+    // server creates instances while a batch runs
+    std::vector<void *> deferred;
 };
 
 namespace {
@@ -152,15 +156,22 @@ fsim_status dalloc(fsim_sim *h, T **p, size_t count)
     return FSIM_OK;
 }
 
-// free a temporary that dalloc made
+// a temporary that dalloc made: no longer part of the instance, freed by
+// flush_deferred (at the first step or batch entry, or with the instance)
 void release(fsim_sim *h, void *p)
 {
-    cudaFree(p);
+    h->deferred.push_back(p);
     for (auto it = h->allocations.begin(); it != h->allocations.end(); ++it)
         if (it->first == p) {
             h->allocations.erase(it);
             return;
         }
+}
+
+void flush_deferred(fsim_sim *h)
+{
+    for (void *p : h->deferred) cudaFree(p);
+    h->deferred.clear();
 }
 
 void free_plan(Plan *pl);
@@ -180,6 +191,7 @@ void free_all(fsim_sim *h)
             }
     for (auto &a : h->allocations) cudaFree(a.first);
     h->allocations.clear();
+    flush_deferred(h);
     for (cudaEvent_t e : h->sweep_events) cudaEventDestroy(e);
     h->sweep_events.clear();
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -1079,7 +1091,7 @@ fsim_status sort_virtual(fsim_sim *h, const float *vpos_host, float4 *vpos_dev =
         if (e == cudaSuccess) e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     }
-    cudaFree(pl.arena);
+    h->deferred.push_back(pl.arena);
     pl.arena = nullptr;
     if (e != cudaSuccess) {
         fsim_set_error("sorting the wall particles failed: %s", cudaGetErrorString(e));
@@ -1495,6 +1507,7 @@ extern "C" fsim_status fsim_step(fsim_handle h, int nsteps)
         return FSIM_EINVAL;
     }
     DeviceGuard guard(h->device);
+    flush_deferred(h);
     for (int k = 0; k < nsteps; ++k) {
         fsim_status st = run_step_graph(h);
         if (st) return st;
@@ -1528,6 +1541,7 @@ extern "C" fsim_status fsim_run_phase(fsim_handle h, int phase)
         return FSIM_EINVAL;
     }
     DeviceGuard guard(h->device);
+    flush_deferred(h);
     Plan *&pl = h->phase_plans[phase][h->f_cur][h->s_cur];
     if (!pl) {
         fsim_status st = build_plan({h}, 1u << phase, h->f_cur, h->s_cur, &pl);
@@ -2119,6 +2133,7 @@ extern "C" fsim_status fsim_time_steps(fsim_handle h, int nsteps, float *ms)
         return FSIM_EINVAL;
     }
     DeviceGuard guard(h->device);
+    flush_deferred(h);
     // capture outside the timed region
     fsim_status st;
     CK(cudaEventRecord(h->ev0, h->stream));
@@ -2138,6 +2153,7 @@ extern "C" fsim_status fsim_time_sweep(fsim_handle h, int nsteps, float *total_m
         return FSIM_EINVAL;
     }
     DeviceGuard guard(h->device);
+    flush_deferred(h);
     while ((int)h->sweep_events.size() < 2 * nsteps) {
         cudaEvent_t e;
         CK(cudaEventCreate(&e));
@@ -2202,6 +2218,7 @@ extern "C" fsim_status fsim_time_phases(fsim_handle h, int nsteps, float *ms, in
         return FSIM_EINVAL;
     }
     DeviceGuard guard(h->device);
+    flush_deferred(h);
     double tot[5] = {0, 0, 0, 0, 0};
     std::vector<cudaEvent_t> ev;
     fsim_status st = FSIM_OK;
@@ -2885,7 +2902,10 @@ extern "C" fsim_status fsim_batch_create(fsim_handle *members, int n, fsim_batch
         return st;
     }
     b->members.assign(members, members + n);
-    for (fsim_sim *h : b->members) h->batch = b;
+    for (fsim_sim *h : b->members) {
+        flush_deferred(h);
+        h->batch = b;
+    }
     *out = b;
     return FSIM_OK;
 }
@@ -2935,6 +2955,7 @@ extern "C" fsim_status fsim_batch_add(fsim_batch_t b, fsim_handle h)
         return FSIM_EINVAL;
     }
     DeviceGuard guard(b->device);
+    flush_deferred(h);
     CK(cudaStreamSynchronize(b->stream));
     CK(cudaStreamSynchronize(h->stream));
     const int pf = b->members.empty() ? 0 : b->members[0]->f_cur;

@@ -151,6 +151,7 @@ class Server:
         be = self.backend
         reqs = sorted(requests, key=lambda r: r.arrival)
         waiting, active = [], []  # active entries: [request, instance, steps left, bytes]
+        pending = []  # admitted while the batch stepped: they join it at the next quantum
         prepared = {}
         st = {"nxt": 0, "used": 0, "load": 0, "completed": 0, "failed": 0, "work": 0, "rebuilds": 0, "joins": 0,
               "leaves": 0}
@@ -177,32 +178,24 @@ class Server:
             close_request(a[0], now, "failed" if error else "done", error)
             tm["retire"] += clock() - t_r
 
-        while st["completed"] < len(reqs):
+        def arrivals():
             now = clock() - t0
             while st["nxt"] < len(reqs) and reqs[st["nxt"]].arrival <= now:
                 waiting.append(reqs[st["nxt"]])
                 st["nxt"] += 1
-            changed = False
-            if self._cancel:
-                for r in [r for r in waiting if r.rid in self._cancel]:
-                    waiting.remove(r)
-                    prepared.pop(r.rid, None)
-                    close_request(r, now, "cancelled", "cancelled")
-                for a in [a for a in active if a[0].rid in self._cancel]:
-                    active.remove(a)
-                    if batch is not None:
-                        batch.close()
-                        batch = None
-                    retire(a, now, "cancelled")
-                    changed = True
+
+        def admit(running):
+            """Admit waiting requests first-come first-served while the budgets
+            allow; `running`: instances already on the GPU (active or pending)."""
+            out = []
             while waiting:
                 r = waiting[0]
                 if r.rid not in prepared:
                     prepared[r.rid] = be.prepare(r)
                 data, need, npart = prepared[r.rid]
-                if active and st["used"] + need > self.budget:
+                if running and st["used"] + need > self.budget:
                     break
-                if active and self.max_particles is not None and st["load"] + npart > self.max_particles:
+                if running and self.max_particles is not None and st["load"] + npart > self.max_particles:
                     break
                 waiting.pop(0)
                 del prepared[r.rid]
@@ -215,11 +208,36 @@ class Server:
                     continue
                 finally:
                     tm["admit"] += clock() - t_a
-                active.append([r, inst, r.steps, need])
+                out.append([r, inst, r.steps, need])
+                running = True
                 st["used"] += need
                 st["load"] += npart
-                changed = True
                 self.log.append(("admit", r.rid, clock() - t0))
+            return out
+
+        while st["completed"] < len(reqs):
+            arrivals()
+            now = clock() - t0
+            changed = bool(pending)
+            active.extend(pending)
+            pending = []
+            if self._cancel:
+                for r in [r for r in waiting if r.rid in self._cancel]:
+                    waiting.remove(r)
+                    prepared.pop(r.rid, None)
+                    close_request(r, now, "cancelled", "cancelled")
+                for a in [a for a in active if a[0].rid in self._cancel]:
+                    active.remove(a)
+                    if batch is not None:
+                        batch.close()
+                        batch = None
+                    retire(a, now, "cancelled")
+                    changed = True
+            if not active:
+                # nothing runs: admit now, there is nothing to overlap with
+                new = admit(False)
+                active.extend(new)
+                changed = changed or bool(new)
             if not active:
                 if batch is not None:
                     batch.close()
@@ -249,6 +267,12 @@ class Server:
             k = min(self.quantum, min(a[2] for a in active))
             t_s = clock()
             batch.step(k)
+            # while the quantum runs on the GPU: admit what has arrived (the new
+            # instances join at the next quantum)
+            arrivals()
+            t_p = clock()
+            pending = admit(True)
+            t_s += clock() - t_p  # admission time is counted as admission, not stepping
             status = be.member_status(batch)
             tm["step"] += clock() - t_s
             now = clock() - t0
