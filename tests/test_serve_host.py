@@ -183,3 +183,42 @@ def test_cancellation_of_waiting_and_running_requests():
     assert reqs[1].error == "cancelled" and reqs[0].error == "cancelled" and out["failed"] == 2
     assert be.steps_done[0] < 40 and 1 not in be.steps_done
     assert reqs[2].result == {"rid": 2} and not be.alive
+
+
+def test_admission_overlaps_the_running_quantum():
+    """A request that arrives while a quantum runs is created between the
+    quantum's launch and the wait for it (its creation overlaps the GPU work),
+    and joins the batch at the next quantum, not the running one."""
+    clock = FakeClock()
+    be = FakeBackend(clock, mem={0: 10, 1: 10})
+    calls = []
+    create, member_status, batch = be.create, be.member_status, be.batch
+
+    def rec_create(rid):
+        calls.append(("create", rid))
+        return create(rid)
+
+    def rec_status(b):
+        calls.append(("status", tuple(b.instances)))
+        return member_status(b)
+
+    def rec_batch(instances):
+        b = batch(instances)
+        step = b.step
+
+        def rec_step(k):
+            calls.append(("step", tuple(b.instances)))
+            step(k)
+
+        b.step = rec_step
+        return b
+
+    be.create, be.member_status, be.batch = rec_create, rec_status, rec_batch
+    reqs = _reqs([0.0, 0.003], [40, 10])
+    out = serve.Server(budget_bytes=100, backend=be, quantum=5).run(reqs, clock=clock, sleep=clock.sleep)
+    assert out["requests"] == 2 and not be.alive
+    k = calls.index(("create", 1))
+    # created right after a quantum of request 0 alone was launched, before its wait
+    assert calls[k - 1] == ("step", (0,)) and calls[k + 1] == ("status", (0,))
+    # and stepped with 0 from the next quantum on
+    assert ("step", (0, 1)) in calls[k + 1:]
