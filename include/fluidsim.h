@@ -197,7 +197,9 @@ typedef struct fsim_sim *fsim_handle;
 /* Copy a particle set to the device and build the initial cell structure.
  * Replaces Sim::initiate (include/sim.cuh:33-43: createCell, fillCell,
  * copyData) + MemoryCopy::copyConstant (src/memory_copy.cu:8-12).
- * device < 0 keeps the current device. */
+ * device < 0 keeps the current device.  Creation frees no device memory
+ * (which would wait for the whole GPU): its temporaries go at the instance's
+ * first step, phase or batch entry, or with the instance. */
 fsim_status fsim_create(const fsim_config *cfg, const fsim_particles *p,
                         int device, fsim_handle *out);
 /* The same case generated on the device straight into a new handle (no host
