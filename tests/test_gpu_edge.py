@@ -24,11 +24,17 @@ def _split(pa, fluid=True, solid=True, virt=True):
         pa.virt_pos if virt else E3)
 
 
+FORMS = [api.PRECISION_FP32, api.PRECISION_MIXED]
+
+
 def _vs_oracle(cfg, pa, steps, fields, tol=2e-4):
-    """The parity policy of the main tests: err(gpu, fp64) <= 2 err(fp32 oracle, fp64) + tol."""
+    """The parity policy of the main tests: err(gpu, fp64) <= 2 err(fp32 oracle, fp64) + tol
+    (the oracles restate the plain method; a mixed-form instance is held to it too)."""
     sim = api.Simulation(cfg, pa, device=0)
-    ref = orc.OracleSim(cfg, pa, "f64")
-    r32 = orc.OracleSim(cfg, pa, "f32")
+    plain = api.Config.from_buffer_copy(cfg)
+    plain.precision = api.PRECISION_FP32
+    ref = orc.OracleSim(plain, pa, "f64")
+    r32 = orc.OracleSim(plain, pa, "f32")
     for s in (sim, ref, r32):
         s.step(steps)
     sim.sync()
@@ -39,8 +45,9 @@ def _vs_oracle(cfg, pa, steps, fields, tol=2e-4):
     sim.close()
 
 
-def test_empty_instance():
-    cfg, _ = cases.tiny_box()
+@pytest.mark.parametrize("precision", FORMS)
+def test_empty_instance(precision):
+    cfg, _ = cases.tiny_box(precision=precision)
     pa = api.ParticleArrays(E3, E3, E1, E1, E3, E3, E3, np.zeros(0, np.int32), E3)
     with api.Simulation(cfg, pa, device=0) as sim:
         assert sim.n == {"fluid": 0, "solid": 0, "virt": 0}
@@ -51,13 +58,15 @@ def test_empty_instance():
         assert all(v == 0.0 for v in c.values())
 
 
-def test_fluid_only_no_walls():
-    cfg, pa = cases.make(cases.tiny_box(jitter=0.01, seed=2))
+@pytest.mark.parametrize("precision", FORMS)
+def test_fluid_only_no_walls(precision):
+    cfg, pa = cases.make(cases.tiny_box(jitter=0.01, seed=2, precision=precision))
     _vs_oracle(cfg, _split(pa, solid=False, virt=False), 3, ("fluid_pos", "fluid_vel", "fluid_rho", "fluid_p"))
 
 
-def test_solid_and_walls_without_fluid():
-    cfg, pa = cases.make(cases.tiny_box(jitter=0.01, seed=3))
+@pytest.mark.parametrize("precision", FORMS)
+def test_solid_and_walls_without_fluid(precision):
+    cfg, pa = cases.make(cases.tiny_box(jitter=0.01, seed=3, precision=precision))
     _vs_oracle(cfg, _split(pa, fluid=False), 3, ("solid_pos",), tol=1e-5)
 
 
